@@ -1,0 +1,215 @@
+/* htr_gb300 — C ABI of the GB300 (sm_103a) explicit right-hand side of HTR.
+ *
+ * Each entry point replaces one HTR Legion task on the RHS path.  The
+ * reference task bodies are `T::cpu_base_impl` / `T::gpu_base_impl`
+ * (signature src/Utils/task_helper.hpp:108-122) registered from
+ * register_rhs_tasks() (src/prometeo_rhs.h:39), register_sensor_tasks(),
+ * register_chem_tasks() and register_variables_tasks().  Where a task reads
+ * its arguments from `Args` and its data from Legion regions, the entry
+ * point here takes:
+ *
+ *   - `view`         per-field device pointers with byte strides (the Realm
+ *                    AffineAccessor of every field of Fluid_columns,
+ *                    src/prometeo_types.h:49-114);
+ *   - `my_fluid`     the task's execution rectangle (`r_MyFluid`, the index
+ *                    space of the region the task writes);
+ *   - `fluid_bounds` `Args::Fluid_bounds` (the whole grid, used for periodic
+ *                    wrap by warpPeriodic, src/Utils/PointDomain_helper.hpp:160-190);
+ *   - `mix`          a handle made by htr_load_mixture (replaces `Args::mix`
+ *                    and the `__constant__ Mix` that LoadMixtureTask fills,
+ *                    src/prometeo_mixture.cu:32-47);
+ *   - scalar task arguments (`RK_coeffs`, the `deltaTime` future, ...);
+ *   - `stream`       the CUDA stream to run on (the task's stream in Legion).
+ *
+ * Every call is asynchronous on `stream`, allocates nothing in steady state
+ * and returns an htr_status.  Buffers are owned by the caller and must stay
+ * valid until the stream has passed the call.  A field element is the
+ * reference's element type (double, int nType, bool sensor, or an array of
+ * double for VecNEq / VecNSp / Vec3) with components contiguous; strides
+ * are free (Legion's default layout is x fastest, one array per field).
+ */
+#ifndef HTR_RHS_H
+#define HTR_RHS_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#include "htr_mix.h"
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+typedef struct CUstream_st *htr_stream_t;
+
+typedef enum {
+  HTR_OK = 0,
+  HTR_ERR_ARGUMENT = 1,      /* null pointer, inverted rectangle, wrong EOS */
+  HTR_ERR_LAYOUT = 2,        /* stride not a multiple of the element size, misaligned base */
+  HTR_ERR_CUDA = 3,          /* a CUDA call failed (message in htr_last_error) */
+  HTR_ERR_ITERATION_CAP = 4, /* a device Newton / Rosenbrock loop hit its cap */
+  HTR_ERR_UNSUPPORTED = 5,   /* configuration outside this build (e.g. other mixtures) */
+  HTR_ERR_NO_DEVICE = 6      /* no usable sm_103 device */
+} htr_status;
+
+/* One field: address of grid point (0,0,0) (it may lie outside the
+ * allocation when the instance does not start at the origin) and byte
+ * strides between neighbouring points in x, y and z. */
+typedef struct {
+  void *base;
+  int64_t stride[3];
+} htr_field;
+
+/* Inclusive rectangle, like Legion::Rect<3>. */
+typedef struct {
+  int64_t lo[3];
+  int64_t hi[3];
+} htr_rect3;
+
+/* The fields of Fluid_columns that the RHS path touches, in declaration
+ * order (src/prometeo_types.h:49-114).  Unused fields may be left null. */
+typedef struct {
+  htr_field nType_x, nType_y, nType_z;       /* int  */
+  htr_field dcsi_e, deta_e, dzet_e;          /* double, Euler metrics */
+  htr_field dcsi_d, deta_d, dzet_d;          /* double, diffusion metrics */
+  htr_field dcsi_s, deta_s, dzet_s;          /* double, staggered metrics */
+  htr_field rho, mu, lam, Di, SoS;           /* Di: VecNSp */
+  htr_field pressure, temperature;
+  htr_field MassFracs, MolarFracs, velocity; /* VecNSp, VecNSp, Vec3 */
+  htr_field Conserved, Conserved_old, Conserved_t, Conserved_t_old; /* VecNEq */
+  htr_field shockSensorX, shockSensorY, shockSensorZ;               /* bool */
+  htr_field DucrosSensor;
+} htr_fluid_view;
+
+typedef struct htr_mixture_s *htr_mixture_t;
+
+/* --- device / mixture management ---------------------------------------- */
+
+/* Text of the last error on the calling thread ("" if none). */
+const char *htr_last_error(void);
+
+/* Replaces LoadMixtureTask (src/prometeo_mixture.cu:32-47): copies the
+ * mixture (a htr_constpropmix_t or htr_airmix_t, `bytes` = its size) to the
+ * current device and derives the per-species constants the kernels use. */
+int htr_load_mixture(int eos, const void *mix, size_t bytes, htr_mixture_t *out);
+int htr_free_mixture(htr_mixture_t mix);
+int htr_mixture_eos(htr_mixture_t mix);
+
+/* Builders for callers without the reference struct.  They restate the
+ * mixture constructors Mix(const Config&) of src/Mixtures/ConstPropMix.inl:31-51
+ * and src/Mixtures/AirMix.hpp:319-332 (+ StoreReferenceQuantities,
+ * src/Mixtures/MultiComponent.inl:438-487). */
+int htr_constpropmix_init(double gasConstant, double gamma, double prandtl, int viscosityModel,
+                          double p0, double p1, double p2, htr_constpropmix_t *out);
+int htr_airmix_init(double PRef, double TRef, double LRef, const double XiRef[HTR_AIR_NSPEC],
+                    htr_airmix_t *out);
+
+/* --- Euler fluxes (src/prometeo_rhs.hpp:171-366, src/prometeo_rhs.cc:35-406) --
+ * Conserved_t[p] += m_e[p] * (F(p+1/2) - F(p-1/2)) over `my_fluid`.
+ * Hybrid: KG split form where shockSensor is true at p-1, p, p+1, TENO
+ * otherwise.  rk_coeffs / delta_time feed the positivity limiter of
+ * multi-species mixtures (the `deltaTime` future of the reference task). */
+int htr_UpdateUsingHybridEulerFluxX(const htr_fluid_view *view, htr_rect3 my_fluid,
+                                    htr_rect3 fluid_bounds, const double rk_coeffs[2],
+                                    double delta_time, htr_mixture_t mix, htr_stream_t stream);
+int htr_UpdateUsingHybridEulerFluxY(const htr_fluid_view *view, htr_rect3 my_fluid,
+                                    htr_rect3 fluid_bounds, const double rk_coeffs[2],
+                                    double delta_time, htr_mixture_t mix, htr_stream_t stream);
+int htr_UpdateUsingHybridEulerFluxZ(const htr_fluid_view *view, htr_rect3 my_fluid,
+                                    htr_rect3 fluid_bounds, const double rk_coeffs[2],
+                                    double delta_time, htr_mixture_t mix, htr_stream_t stream);
+/* TENO (eps 1e-10), TENO-A (eps 1e-8) and TENO-LAD (eps 1e-16) everywhere
+ * (UpdateUsingTENOEulerFluxTask<dir, Op>, src/prometeo_rhs.hpp:243-310). */
+int htr_UpdateUsingTENOEulerFluxX(const htr_fluid_view *view, htr_rect3 my_fluid,
+                                  htr_rect3 fluid_bounds, const double rk_coeffs[2],
+                                  double delta_time, htr_mixture_t mix, htr_stream_t stream);
+int htr_UpdateUsingTENOEulerFluxY(const htr_fluid_view *view, htr_rect3 my_fluid,
+                                  htr_rect3 fluid_bounds, const double rk_coeffs[2],
+                                  double delta_time, htr_mixture_t mix, htr_stream_t stream);
+int htr_UpdateUsingTENOEulerFluxZ(const htr_fluid_view *view, htr_rect3 my_fluid,
+                                  htr_rect3 fluid_bounds, const double rk_coeffs[2],
+                                  double delta_time, htr_mixture_t mix, htr_stream_t stream);
+int htr_UpdateUsingTENOAEulerFluxX(const htr_fluid_view *view, htr_rect3 my_fluid,
+                                   htr_rect3 fluid_bounds, const double rk_coeffs[2],
+                                   double delta_time, htr_mixture_t mix, htr_stream_t stream);
+int htr_UpdateUsingTENOAEulerFluxY(const htr_fluid_view *view, htr_rect3 my_fluid,
+                                   htr_rect3 fluid_bounds, const double rk_coeffs[2],
+                                   double delta_time, htr_mixture_t mix, htr_stream_t stream);
+int htr_UpdateUsingTENOAEulerFluxZ(const htr_fluid_view *view, htr_rect3 my_fluid,
+                                   htr_rect3 fluid_bounds, const double rk_coeffs[2],
+                                   double delta_time, htr_mixture_t mix, htr_stream_t stream);
+int htr_UpdateUsingTENOLADEulerFluxX(const htr_fluid_view *view, htr_rect3 my_fluid,
+                                     htr_rect3 fluid_bounds, const double rk_coeffs[2],
+                                     double delta_time, htr_mixture_t mix, htr_stream_t stream);
+int htr_UpdateUsingTENOLADEulerFluxY(const htr_fluid_view *view, htr_rect3 my_fluid,
+                                     htr_rect3 fluid_bounds, const double rk_coeffs[2],
+                                     double delta_time, htr_mixture_t mix, htr_stream_t stream);
+int htr_UpdateUsingTENOLADEulerFluxZ(const htr_fluid_view *view, htr_rect3 my_fluid,
+                                     htr_rect3 fluid_bounds, const double rk_coeffs[2],
+                                     double delta_time, htr_mixture_t mix, htr_stream_t stream);
+/* Kennedy-Gruber skew-symmetric flux everywhere (src/prometeo_rhs.hpp:312-366). */
+int htr_UpdateUsingSkewSymmetricEulerFluxX(const htr_fluid_view *view, htr_rect3 my_fluid,
+                                           htr_rect3 fluid_bounds, htr_mixture_t mix,
+                                           htr_stream_t stream);
+int htr_UpdateUsingSkewSymmetricEulerFluxY(const htr_fluid_view *view, htr_rect3 my_fluid,
+                                           htr_rect3 fluid_bounds, htr_mixture_t mix,
+                                           htr_stream_t stream);
+int htr_UpdateUsingSkewSymmetricEulerFluxZ(const htr_fluid_view *view, htr_rect3 my_fluid,
+                                           htr_rect3 fluid_bounds, htr_mixture_t mix,
+                                           htr_stream_t stream);
+
+/* --- diffusion fluxes (src/prometeo_rhs.hpp:368-473, src/prometeo_rhs.cc:408-527) -- */
+int htr_UpdateUsingDiffusionFluxX(const htr_fluid_view *view, htr_rect3 my_fluid,
+                                  htr_rect3 fluid_bounds, htr_mixture_t mix, htr_stream_t stream);
+int htr_UpdateUsingDiffusionFluxY(const htr_fluid_view *view, htr_rect3 my_fluid,
+                                  htr_rect3 fluid_bounds, htr_mixture_t mix, htr_stream_t stream);
+int htr_UpdateUsingDiffusionFluxZ(const htr_fluid_view *view, htr_rect3 my_fluid,
+                                  htr_rect3 fluid_bounds, htr_mixture_t mix, htr_stream_t stream);
+
+/* --- shock sensors (src/prometeo_sensor.hpp:49-131, src/prometeo_sensor.cc:33-128) -- */
+int htr_UpdateDucrosSensor(const htr_fluid_view *view, htr_rect3 my_fluid,
+                           htr_rect3 fluid_bounds, double vorticityScale, htr_stream_t stream);
+int htr_UpdateShockSensorX(const htr_fluid_view *view, htr_rect3 my_fluid,
+                           htr_rect3 fluid_bounds, htr_mixture_t mix, htr_stream_t stream);
+int htr_UpdateShockSensorY(const htr_fluid_view *view, htr_rect3 my_fluid,
+                           htr_rect3 fluid_bounds, htr_mixture_t mix, htr_stream_t stream);
+int htr_UpdateShockSensorZ(const htr_fluid_view *view, htr_rect3 my_fluid,
+                           htr_rect3 fluid_bounds, htr_mixture_t mix, htr_stream_t stream);
+
+/* --- chemistry (src/prometeo_chem.hpp:96-150, src/prometeo_chem.cc:31-110) -- */
+int htr_AddChemistrySources(const htr_fluid_view *view, htr_rect3 my_fluid, htr_mixture_t mix,
+                            htr_stream_t stream);
+/* Implicit Rosenbrock chemistry over Integrator_deltaTime.  `status` (device
+ * int, may be null) receives HTR_ERR_ITERATION_CAP if any cell hit a cap. */
+int htr_UpdateChemistry(const htr_fluid_view *view, htr_rect3 my_fluid,
+                        double Integrator_deltaTime, htr_mixture_t mix, int *status,
+                        htr_stream_t stream);
+
+/* --- per-cell state refresh (src/prometeo_variables.hpp:52-210) ---------- */
+int htr_UpdatePropertiesFromPrimitive(const htr_fluid_view *view, htr_rect3 my_fluid,
+                                      htr_mixture_t mix, htr_stream_t stream);
+int htr_UpdateConservedFromPrimitive(const htr_fluid_view *view, htr_rect3 my_fluid,
+                                     htr_mixture_t mix, htr_stream_t stream);
+int htr_UpdatePrimitiveFromConserved(const htr_fluid_view *view, htr_rect3 my_fluid,
+                                     htr_mixture_t mix, htr_stream_t stream);
+
+/* --- time step (src/prometeo_cfl.hpp:55-190, src/prometeo.rg:1159-1166) --
+ * Writes max over my_fluid of the spectral radius to *result_dev (device
+ * double). */
+int htr_CalculateMaxSpectralRadius(const htr_fluid_view *view, htr_rect3 my_fluid,
+                                   htr_mixture_t mix, double *result_dev, htr_stream_t stream);
+
+/* --- SSP-RK3 bookkeeping (Regent tasks of src/prometeo_rk.rg:47-112) ---- */
+int htr_InitializeTemporaries(const htr_fluid_view *view, htr_rect3 my_fluid,
+                              htr_mixture_t mix, htr_stream_t stream);
+int htr_InitializeTimeDerivatives(const htr_fluid_view *view, htr_rect3 my_fluid,
+                                  int implicitChemistry, htr_mixture_t mix, htr_stream_t stream);
+/* stage in {1,2,3}: Conserved = C1*Conserved_old + C2*Conserved + C3*Conserved_t*dt. */
+int htr_UpdateVars(const htr_fluid_view *view, htr_rect3 my_fluid, int stage, double deltaTime,
+                   int implicitChemistry, htr_mixture_t mix, htr_stream_t stream);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* HTR_RHS_H */

@@ -1,0 +1,157 @@
+"""CPU oracles for the HTR explicit-RHS path.  TEST INFRASTRUCTURE ONLY.
+
+Only the test suite, the smoke check and the CPU-baseline leg of bench.py
+may load anything from this directory; the GPU product never does.
+
+Two oracles implement the same C ABI as the CUDA library (include/htr_rhs.h):
+
+* `ref`  — the reference solver's own CPU task code (HTR src/prometeo_*.cc),
+  compiled unmodified against a Legion stand-in by oracle/ref/Makefile into
+  oracle/_ref/libhtrref_<EOS>.so.  It can only be built where the reference
+  sources are present; it is the pin for everything else.
+* `port` — a from-scratch C++ restatement of the same algorithms
+  (oracle/port/), built into oracle/_build/libhtroracle.so on every machine.
+  It is checked against `ref` here and against golden vectors from `ref`
+  (tests/golden/) everywhere.
+
+`step` restates the driver order of one SSP-RK3 time step of the reference
+(MainLoopHeader + MainLoopBody, src/prometeo.rg:1153-1172 and 1342-1486,
+UpdateDerivatives :480-606, UpdatePrimitivesAndBCsFromConserved :428-478)
+on top of any library exporting the ABI.
+"""
+import ctypes as C
+import os
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+REF_DIR = os.path.join(HERE, "_ref")
+BUILD_DIR = os.path.join(HERE, "_build")
+
+RK_C = ((1.0, 0.0, 1.0), (3.0 / 4.0, 1.0 / 4.0, 1.0 / 4.0), (1.0 / 3.0, 2.0 / 3.0, 2.0 / 3.0))
+
+_cache = {}
+
+
+def _abi():
+    import sys
+    if "htr_gb300" not in sys.modules:
+        sys.path.insert(0, os.path.dirname(HERE))
+        import __graft_entry__  # noqa: F401  (registers the package)
+        __graft_entry__.load_package()
+    return sys.modules["htr_gb300.abi"]
+
+
+def ref_path(eos):
+    name = {1: "ConstPropMix", 2: "AirMix"}[eos]
+    return os.path.join(REF_DIR, f"libhtrref_{name}.so")
+
+
+def ref_lib(eos):
+    """The compiled reference for `eos`, or None where it was not built."""
+    p = ref_path(eos)
+    if not os.path.exists(p):
+        return None
+    key = ("ref", eos)
+    if key not in _cache:
+        lib = C.CDLL(p)
+        _abi().bind(lib, {"htr_ref_mix_offsets": [C.POINTER(C.c_longlong), C.c_int]})
+        lib.htr_ref_mix_sizeof.restype = C.c_size_t
+        _cache[key] = lib
+    return _cache[key]
+
+
+def port_path():
+    return os.path.join(BUILD_DIR, "libhtroracle.so")
+
+
+def port_lib():
+    """The from-scratch CPU restatement (built by build())."""
+    key = ("port",)
+    if key not in _cache:
+        p = port_path()
+        if not os.path.exists(p):
+            raise FileNotFoundError(f"{p} missing: run __graft_entry__.build()")
+        lib = C.CDLL(p)
+        _abi().bind(lib)
+        lib.htr_oracle_set_threads.argtypes = [C.c_int]
+        lib.htr_oracle_set_threads.restype = C.c_int
+        _cache[key] = lib
+    return _cache[key]
+
+
+def load_mixture(lib, eos, struct):
+    h = C.c_void_p()
+    st = lib.htr_load_mixture(eos, C.byref(struct), C.sizeof(struct), C.byref(h))
+    _abi().check(lib, st, "htr_load_mixture")
+    return h
+
+
+def spectral_dt(lib, fl, mixh, cfl):
+    v = fl.view()
+    r = C.c_double(0.0)
+    _abi().check(lib, lib.htr_CalculateMaxSpectralRadius(C.byref(v), fl.interior(), mixh,
+                                                        C.byref(r), None), "cfl")
+    return cfl / r.value
+
+
+def update_derivatives(lib, fl, mixh, stage, dt, scheme="Hybrid", chemistry=True):
+    """One explicit RHS evaluation in the reference's order (prometeo.rg:480-606)."""
+    A = _abi()
+    v = fl.view()
+    allr = fl.bounds()
+    inner = fl.interior()
+    fb = fl.bounds()
+    A.check(lib, lib.htr_InitializeTimeDerivatives(C.byref(v), allr, 0, mixh, None), "init_t")
+    if chemistry:
+        A.check(lib, lib.htr_AddChemistrySources(C.byref(v), inner, mixh, None), "chem")
+    rk = (C.c_double * 2)(RK_C[stage - 1][0], RK_C[stage - 1][1])
+    ddt = dt * RK_C[stage - 1][2]
+    for d in "ZYX":
+        if scheme == "SkewSymmetric":
+            fn = getattr(lib, f"htr_UpdateUsingSkewSymmetricEulerFlux{d}")
+            st = fn(C.byref(v), inner, fb, mixh, None)
+        else:
+            fn = getattr(lib, f"htr_UpdateUsing{scheme}EulerFlux{d}")
+            st = fn(C.byref(v), inner, fb, rk, ddt, mixh, None)
+        A.check(lib, st, f"euler {scheme} {d}")
+    for d in "ZYX":
+        fn = getattr(lib, f"htr_UpdateUsingDiffusionFlux{d}")
+        A.check(lib, fn(C.byref(v), inner, fb, mixh, None), f"diffusion {d}")
+
+
+def update_sensors(lib, fl, mixh, vorticity_scale):
+    A = _abi()
+    v = fl.view()
+    r = fl.bounds()
+    A.check(lib, lib.htr_UpdateDucrosSensor(C.byref(v), r, r, vorticity_scale, None), "ducros")
+    for d in "XYZ":
+        fn = getattr(lib, f"htr_UpdateShockSensor{d}")
+        A.check(lib, fn(C.byref(v), r, r, mixh, None), f"shock {d}")
+
+
+def refresh(lib, fl, mixh):
+    """UpdatePrimitivesAndBCsFromConserved for a fully periodic grid."""
+    A = _abi()
+    v = fl.view()
+    A.check(lib, lib.htr_UpdatePrimitiveFromConserved(C.byref(v), fl.interior(), mixh, None),
+            "prim")
+    A.check(lib, lib.htr_UpdatePropertiesFromPrimitive(C.byref(v), fl.bounds(), mixh, None),
+            "props")
+
+
+def step(lib, fl, mixh, scheme="Hybrid", vorticity_scale=1.0, cfl=0.8, dt=None, chemistry=True,
+         stages=3, hook=None):
+    """One SSP-RK3 time step of a periodic grid; returns the dt used."""
+    A = _abi()
+    if dt is None:
+        dt = spectral_dt(lib, fl, mixh, cfl)
+    if scheme == "Hybrid":
+        update_sensors(lib, fl, mixh, vorticity_scale)
+    v = fl.view()
+    A.check(lib, lib.htr_InitializeTemporaries(C.byref(v), fl.bounds(), mixh, None), "tmp")
+    for s in range(1, stages + 1):
+        update_derivatives(lib, fl, mixh, s, dt, scheme, chemistry)
+        if hook is not None:
+            hook(s, fl)
+        A.check(lib, lib.htr_UpdateVars(C.byref(v), fl.bounds(), s, dt, 0, mixh, None), "rk")
+        refresh(lib, fl, mixh)
+    return dt
