@@ -1,0 +1,414 @@
+// extern "C" entry points of libhtr_gb300 (declared in include/htr_rhs.h).
+//
+// Each entry point validates its arguments on the host (null fields,
+// rectangles, element alignment of bases and strides, mixture kind),
+// dispatches on the loaded mixture and enqueues the kernel(s) on the
+// caller's stream.  Nothing is allocated after htr_load_mixture.
+#include <cstdio>
+#include <cstring>
+#include <new>
+#include <string>
+
+#include "kernels.cuh"
+#include "mixture_host.h"
+
+struct htr_mixture_s {
+  int eos;
+  htr::ConstPropDev cp;
+  htr::AirDev air;
+};
+
+namespace {
+
+thread_local std::string g_err;
+
+int fail(int code, const char *fmt, const char *what = "") {
+  char buf[512];
+  std::snprintf(buf, sizeof(buf), fmt, what);
+  g_err = buf;
+  return code;
+}
+
+int cuda_status(cudaError_t e, const char *where) {
+  if (e == cudaSuccess) return HTR_OK;
+  g_err = std::string(where) + ": " + cudaGetErrorString(e);
+  return HTR_ERR_CUDA;
+}
+
+bool rect_ok(const htr_rect3 &r) {
+  for (int i = 0; i < 3; i++)
+    if (r.lo[i] > r.hi[i]) return false;
+  return true;
+}
+bool inside(const htr_rect3 &a, const htr_rect3 &b) {
+  for (int i = 0; i < 3; i++)
+    if (a.lo[i] < b.lo[i] || a.hi[i] > b.hi[i]) return false;
+  return true;
+}
+
+// field present, base and strides aligned to the element's alignment
+int check_field(const htr_field &f, size_t align, const char *name) {
+  if (f.base == nullptr) return fail(HTR_ERR_ARGUMENT, "field %s is null", name);
+  if (reinterpret_cast<uintptr_t>(f.base) % align != 0)
+    return fail(HTR_ERR_LAYOUT, "field %s: misaligned base", name);
+  for (int i = 0; i < 3; i++)
+    if (f.stride[i] % (int64_t)align != 0) return fail(HTR_ERR_LAYOUT, "field %s: stride not a multiple of the element alignment", name);
+  return HTR_OK;
+}
+
+#define HTR_REQ_D(V, F) \
+  if (int st_ = check_field((V).F, 8, #F)) return st_;
+#define HTR_REQ_I(V, F) \
+  if (int st_ = check_field((V).F, 4, #F)) return st_;
+#define HTR_REQ_B(V, F) \
+  if (int st_ = check_field((V).F, 1, #F)) return st_;
+
+int check_common(const htr_fluid_view *v, htr_mixture_t m, const htr_rect3 &my) {
+  if (v == nullptr) return fail(HTR_ERR_ARGUMENT, "null view%s");
+  if (m == nullptr) return fail(HTR_ERR_ARGUMENT, "null mixture%s");
+  if (!rect_ok(my)) return fail(HTR_ERR_ARGUMENT, "inverted execution rectangle%s");
+  return HTR_OK;
+}
+
+const htr_field &dirf(const htr_fluid_view &v, int d, int which) {
+  // which: 0 nType, 1 m_e, 2 m_d, 3 m_s, 4 sensor
+  const htr_field *t[5][3] = {{&v.nType_x, &v.nType_y, &v.nType_z},
+                              {&v.dcsi_e, &v.deta_e, &v.dzet_e},
+                              {&v.dcsi_d, &v.deta_d, &v.dzet_d},
+                              {&v.dcsi_s, &v.deta_s, &v.dzet_s},
+                              {&v.shockSensorX, &v.shockSensorY, &v.shockSensorZ}};
+  return *t[which][d];
+}
+
+template <class F> int with_mix(htr_mixture_t m, F &&f) {
+  if (m->eos == HTR_EOS_CONSTPROPMIX) return f(m->cp);
+  if (m->eos == HTR_EOS_AIRMIX) return f(m->air);
+  return fail(HTR_ERR_UNSUPPORTED, "unknown mixture kind%s");
+}
+
+int euler(const htr_fluid_view *v, htr_rect3 my, htr_rect3 fb, const double *rk, double dt,
+          htr_mixture_t m, int d, int scheme, int kind, htr_stream_t s) {
+  if (int st = check_common(v, m, my)) return st;
+  if (!rect_ok(fb) || !inside(my, fb)) return fail(HTR_ERR_ARGUMENT, "execution rectangle outside the grid bounds%s");
+  HTR_REQ_D(*v, Conserved);
+  HTR_REQ_D(*v, rho);
+  HTR_REQ_D(*v, MassFracs);
+  HTR_REQ_D(*v, velocity);
+  HTR_REQ_D(*v, pressure);
+  HTR_REQ_D(*v, Conserved_t);
+  if (int st = check_field(dirf(*v, d, 0), 4, "nType")) return st;
+  if (int st = check_field(dirf(*v, d, 1), 8, "m_e")) return st;
+  if (scheme != 1) {
+    HTR_REQ_D(*v, SoS);
+    if (m->eos == HTR_EOS_AIRMIX) HTR_REQ_D(*v, Conserved_old);
+  }
+  if (scheme == 0)
+    if (int st = check_field(dirf(*v, d, 4), 1, "shockSensor")) return st;
+  return with_mix(m, [&](const auto &mix) {
+    return cuda_status(htr::launch_euler(*v, my, fb, rk, dt, mix, d, scheme, kind, (cudaStream_t)s), "euler");
+  });
+}
+
+int diffusion(const htr_fluid_view *v, htr_rect3 my, htr_rect3 fb, htr_mixture_t m, int d, htr_stream_t s) {
+  if (int st = check_common(v, m, my)) return st;
+  if (!rect_ok(fb) || !inside(my, fb)) return fail(HTR_ERR_ARGUMENT, "execution rectangle outside the grid bounds%s");
+  HTR_REQ_D(*v, Conserved);
+  HTR_REQ_D(*v, temperature);
+  HTR_REQ_D(*v, MolarFracs);
+  HTR_REQ_D(*v, rho);
+  HTR_REQ_D(*v, mu);
+  HTR_REQ_D(*v, lam);
+  HTR_REQ_D(*v, Di);
+  HTR_REQ_D(*v, velocity);
+  HTR_REQ_D(*v, Conserved_t);
+  for (int e = 0; e < 3; e++) {
+    if (int st = check_field(dirf(*v, e, 0), 4, "nType")) return st;
+    if (int st = check_field(dirf(*v, e, 2), 8, "m_d")) return st;
+  }
+  if (int st = check_field(dirf(*v, d, 3), 8, "m_s")) return st;
+  return with_mix(m, [&](const auto &mix) {
+    return cuda_status(htr::launch_diffusion(*v, my, fb, mix, d, (cudaStream_t)s), "diffusion");
+  });
+}
+
+int neq_of(htr_mixture_t m) { return m->eos == HTR_EOS_AIRMIX ? 9 : 5; }
+int nspec_of(htr_mixture_t m) { return m->eos == HTR_EOS_AIRMIX ? 5 : 1; }
+
+}  // namespace
+
+extern "C" {
+
+const char *htr_last_error(void) { return g_err.c_str(); }
+
+int htr_load_mixture(int eos, const void *mix, size_t bytes, htr_mixture_t *out) {
+  if (mix == nullptr || out == nullptr) return fail(HTR_ERR_ARGUMENT, "null argument%s");
+  int dev = 0;
+  cudaError_t e = cudaGetDevice(&dev);
+  if (e != cudaSuccess) return fail(HTR_ERR_NO_DEVICE, "no CUDA device: %s", cudaGetErrorString(e));
+  cudaDeviceProp prop;
+  e = cudaGetDeviceProperties(&prop, dev);
+  if (e != cudaSuccess) return fail(HTR_ERR_NO_DEVICE, "cudaGetDeviceProperties: %s", cudaGetErrorString(e));
+  if (prop.major != 10 || prop.minor != 3)
+    return fail(HTR_ERR_NO_DEVICE, "this build targets sm_103 (GB300); device is %s", prop.name);
+  htr_mixture_s *m = new (std::nothrow) htr_mixture_s();
+  if (m == nullptr) return fail(HTR_ERR_ARGUMENT, "out of host memory%s");
+  m->eos = eos;
+  bool ok = false;
+  if (eos == HTR_EOS_CONSTPROPMIX && bytes == sizeof(htr_constpropmix_t))
+    ok = htr::derive(*static_cast<const htr_constpropmix_t *>(mix), m->cp);
+  else if (eos == HTR_EOS_AIRMIX && bytes == sizeof(htr_airmix_t))
+    ok = htr::derive(*static_cast<const htr_airmix_t *>(mix), m->air);
+  if (!ok) {
+    delete m;
+    return fail(HTR_ERR_ARGUMENT, "htr_load_mixture: unknown EOS, wrong struct size or unusable data%s");
+  }
+  *out = m;
+  return HTR_OK;
+}
+
+int htr_free_mixture(htr_mixture_t m) {
+  delete m;
+  return HTR_OK;
+}
+
+int htr_mixture_eos(htr_mixture_t m) { return m ? m->eos : 0; }
+
+#define HTR_EULER_EP(NAME, D, SCHEME, KIND)                                                         \
+  int NAME(const htr_fluid_view *v, htr_rect3 m, htr_rect3 b, const double rk[2], double dt,       \
+           htr_mixture_t mix, htr_stream_t s) {                                                     \
+    return euler(v, m, b, rk, dt, mix, D, SCHEME, KIND, s);                                         \
+  }
+HTR_EULER_EP(htr_UpdateUsingHybridEulerFluxX, 0, 0, 0)
+HTR_EULER_EP(htr_UpdateUsingHybridEulerFluxY, 1, 0, 0)
+HTR_EULER_EP(htr_UpdateUsingHybridEulerFluxZ, 2, 0, 0)
+HTR_EULER_EP(htr_UpdateUsingTENOEulerFluxX, 0, 2, 0)
+HTR_EULER_EP(htr_UpdateUsingTENOEulerFluxY, 1, 2, 0)
+HTR_EULER_EP(htr_UpdateUsingTENOEulerFluxZ, 2, 2, 0)
+HTR_EULER_EP(htr_UpdateUsingTENOAEulerFluxX, 0, 2, 1)
+HTR_EULER_EP(htr_UpdateUsingTENOAEulerFluxY, 1, 2, 1)
+HTR_EULER_EP(htr_UpdateUsingTENOAEulerFluxZ, 2, 2, 1)
+HTR_EULER_EP(htr_UpdateUsingTENOLADEulerFluxX, 0, 2, 2)
+HTR_EULER_EP(htr_UpdateUsingTENOLADEulerFluxY, 1, 2, 2)
+HTR_EULER_EP(htr_UpdateUsingTENOLADEulerFluxZ, 2, 2, 2)
+#undef HTR_EULER_EP
+
+#define HTR_SKEW_EP(NAME, D)                                                                        \
+  int NAME(const htr_fluid_view *v, htr_rect3 m, htr_rect3 b, htr_mixture_t mix, htr_stream_t s) { \
+    return euler(v, m, b, nullptr, 0.0, mix, D, 1, 0, s);                                           \
+  }
+HTR_SKEW_EP(htr_UpdateUsingSkewSymmetricEulerFluxX, 0)
+HTR_SKEW_EP(htr_UpdateUsingSkewSymmetricEulerFluxY, 1)
+HTR_SKEW_EP(htr_UpdateUsingSkewSymmetricEulerFluxZ, 2)
+#undef HTR_SKEW_EP
+
+#define HTR_DIFF_EP(NAME, D)                                                                        \
+  int NAME(const htr_fluid_view *v, htr_rect3 m, htr_rect3 b, htr_mixture_t mix, htr_stream_t s) { \
+    return diffusion(v, m, b, mix, D, s);                                                           \
+  }
+HTR_DIFF_EP(htr_UpdateUsingDiffusionFluxX, 0)
+HTR_DIFF_EP(htr_UpdateUsingDiffusionFluxY, 1)
+HTR_DIFF_EP(htr_UpdateUsingDiffusionFluxZ, 2)
+#undef HTR_DIFF_EP
+
+int htr_UpdateDucrosSensor(const htr_fluid_view *v, htr_rect3 my, htr_rect3 fb, double vorticityScale,
+                           htr_stream_t s) {
+  if (v == nullptr || !rect_ok(my) || !rect_ok(fb) || !inside(my, fb))
+    return fail(HTR_ERR_ARGUMENT, "bad view or rectangle%s");
+  HTR_REQ_D(*v, velocity);
+  HTR_REQ_D(*v, DucrosSensor);
+  for (int e = 0; e < 3; e++) {
+    if (int st = check_field(dirf(*v, e, 0), 4, "nType")) return st;
+    if (int st = check_field(dirf(*v, e, 2), 8, "m_d")) return st;
+  }
+  return cuda_status(htr::launch_ducros(*v, my, fb, vorticityScale, (cudaStream_t)s), "ducros");
+}
+
+static int shock(const htr_fluid_view *v, htr_rect3 my, htr_rect3 fb, htr_mixture_t m, int d, htr_stream_t s) {
+  if (int st = check_common(v, m, my)) return st;
+  if (!rect_ok(fb) || !inside(my, fb)) return fail(HTR_ERR_ARGUMENT, "execution rectangle outside the grid bounds%s");
+  HTR_REQ_D(*v, Conserved);
+  HTR_REQ_D(*v, DucrosSensor);
+  if (int st = check_field(dirf(*v, d, 0), 4, "nType")) return st;
+  if (int st = check_field(dirf(*v, d, 4), 1, "shockSensor")) return st;
+  return cuda_status(htr::launch_shock_sensor(*v, my, fb, nspec_of(m), 1 << d, (cudaStream_t)s), "shock sensor");
+}
+int htr_UpdateShockSensorX(const htr_fluid_view *v, htr_rect3 m, htr_rect3 b, htr_mixture_t x, htr_stream_t s) {
+  return shock(v, m, b, x, 0, s);
+}
+int htr_UpdateShockSensorY(const htr_fluid_view *v, htr_rect3 m, htr_rect3 b, htr_mixture_t x, htr_stream_t s) {
+  return shock(v, m, b, x, 1, s);
+}
+int htr_UpdateShockSensorZ(const htr_fluid_view *v, htr_rect3 m, htr_rect3 b, htr_mixture_t x, htr_stream_t s) {
+  return shock(v, m, b, x, 2, s);
+}
+
+int htr_AddChemistrySources(const htr_fluid_view *v, htr_rect3 my, htr_mixture_t m, htr_stream_t s) {
+  if (int st = check_common(v, m, my)) return st;
+  HTR_REQ_D(*v, rho);
+  HTR_REQ_D(*v, pressure);
+  HTR_REQ_D(*v, temperature);
+  HTR_REQ_D(*v, MassFracs);
+  HTR_REQ_D(*v, Conserved_t);
+  return with_mix(m, [&](const auto &mix) {
+    return cuda_status(htr::launch_chem_sources(*v, my, mix, (cudaStream_t)s), "chemistry sources");
+  });
+}
+
+int htr_UpdateChemistry(const htr_fluid_view *v, htr_rect3 my, double dt, htr_mixture_t m, int *status,
+                        htr_stream_t s) {
+  if (int st = check_common(v, m, my)) return st;
+  HTR_REQ_D(*v, Conserved);
+  HTR_REQ_D(*v, Conserved_t);
+  HTR_REQ_D(*v, Conserved_t_old);
+  HTR_REQ_D(*v, temperature);
+  return with_mix(m, [&](const auto &mix) {
+    return cuda_status(htr::launch_update_chemistry(*v, my, dt, mix, status, (cudaStream_t)s), "UpdateChemistry");
+  });
+}
+
+int htr_UpdatePropertiesFromPrimitive(const htr_fluid_view *v, htr_rect3 my, htr_mixture_t m, htr_stream_t s) {
+  if (int st = check_common(v, m, my)) return st;
+  HTR_REQ_D(*v, pressure);
+  HTR_REQ_D(*v, temperature);
+  HTR_REQ_D(*v, MolarFracs);
+  HTR_REQ_D(*v, MassFracs);
+  HTR_REQ_D(*v, rho);
+  HTR_REQ_D(*v, mu);
+  HTR_REQ_D(*v, lam);
+  HTR_REQ_D(*v, Di);
+  HTR_REQ_D(*v, SoS);
+  return with_mix(m, [&](const auto &mix) {
+    return cuda_status(htr::launch_properties(*v, my, mix, (cudaStream_t)s), "properties");
+  });
+}
+
+int htr_UpdateConservedFromPrimitive(const htr_fluid_view *v, htr_rect3 my, htr_mixture_t m, htr_stream_t s) {
+  if (int st = check_common(v, m, my)) return st;
+  HTR_REQ_D(*v, MassFracs);
+  HTR_REQ_D(*v, temperature);
+  HTR_REQ_D(*v, velocity);
+  HTR_REQ_D(*v, rho);
+  HTR_REQ_D(*v, Conserved);
+  return with_mix(m, [&](const auto &mix) {
+    return cuda_status(htr::launch_conserved(*v, my, mix, (cudaStream_t)s), "conserved");
+  });
+}
+
+int htr_UpdatePrimitiveFromConserved(const htr_fluid_view *v, htr_rect3 my, htr_mixture_t m, htr_stream_t s) {
+  if (int st = check_common(v, m, my)) return st;
+  HTR_REQ_D(*v, Conserved);
+  HTR_REQ_D(*v, temperature);
+  HTR_REQ_D(*v, pressure);
+  HTR_REQ_D(*v, MolarFracs);
+  HTR_REQ_D(*v, velocity);
+  return with_mix(m, [&](const auto &mix) {
+    return cuda_status(htr::launch_primitive(*v, my, mix, nullptr, (cudaStream_t)s), "primitive");
+  });
+}
+
+int htr_CalculateMaxSpectralRadius(const htr_fluid_view *v, htr_rect3 my, htr_mixture_t m, double *result,
+                                   htr_stream_t s) {
+  if (int st = check_common(v, m, my)) return st;
+  if (result == nullptr) return fail(HTR_ERR_ARGUMENT, "null result%s");
+  HTR_REQ_D(*v, dcsi_d);
+  HTR_REQ_D(*v, deta_d);
+  HTR_REQ_D(*v, dzet_d);
+  HTR_REQ_D(*v, temperature);
+  HTR_REQ_D(*v, MassFracs);
+  HTR_REQ_D(*v, velocity);
+  HTR_REQ_D(*v, rho);
+  HTR_REQ_D(*v, mu);
+  HTR_REQ_D(*v, lam);
+  HTR_REQ_D(*v, Di);
+  HTR_REQ_D(*v, SoS);
+  return with_mix(m, [&](const auto &mix) {
+    return cuda_status(htr::launch_spectral_radius(*v, my, mix, result, (cudaStream_t)s), "spectral radius");
+  });
+}
+
+int htr_InitializeTemporaries(const htr_fluid_view *v, htr_rect3 my, htr_mixture_t m, htr_stream_t s) {
+  if (int st = check_common(v, m, my)) return st;
+  HTR_REQ_D(*v, Conserved);
+  HTR_REQ_D(*v, Conserved_old);
+  return cuda_status(htr::launch_copy_conserved(*v, my, neq_of(m), (cudaStream_t)s), "InitializeTemporaries");
+}
+
+int htr_InitializeTimeDerivatives(const htr_fluid_view *v, htr_rect3 my, int implicit, htr_mixture_t m,
+                                  htr_stream_t s) {
+  if (int st = check_common(v, m, my)) return st;
+  HTR_REQ_D(*v, Conserved_t);
+  if (implicit) HTR_REQ_D(*v, Conserved_t_old);
+  return cuda_status(htr::launch_init_rhs(*v, my, neq_of(m), implicit, (cudaStream_t)s), "InitializeTimeDerivatives");
+}
+
+int htr_UpdateVars(const htr_fluid_view *v, htr_rect3 my, int stage, double dt, int implicit, htr_mixture_t m,
+                   htr_stream_t s) {
+  if (int st = check_common(v, m, my)) return st;
+  if (stage < 1 || stage > 3) return fail(HTR_ERR_ARGUMENT, "stage must be 1, 2 or 3%s");
+  HTR_REQ_D(*v, Conserved);
+  HTR_REQ_D(*v, Conserved_old);
+  HTR_REQ_D(*v, Conserved_t);
+  return cuda_status(htr::launch_rk_update(*v, my, neq_of(m), stage, dt, implicit, (cudaStream_t)s), "UpdateVars");
+}
+
+// One SSP-RK3 time step of a periodic grid in the reference's driver order.
+int htr_rk3_step(const htr_fluid_view *v, htr_rect3 inner, htr_rect3 fb, const htr_step_params *p,
+                 htr_mixture_t m, double *dt_used, int *status_dev, htr_stream_t s) {
+  if (p == nullptr) return fail(HTR_ERR_ARGUMENT, "null step parameters%s");
+  if (int st = check_common(v, m, inner)) return st;
+  const cudaStream_t cs = (cudaStream_t)s;
+  double dt = p->deltaTime;
+  if (p->cfl > 0.0) {
+    // the radius lands in Conserved_t[first cell][0], which the stage overwrites anyway
+    double *scratch = reinterpret_cast<double *>(static_cast<char *>(v->Conserved_t.base) +
+                                                 inner.lo[0] * v->Conserved_t.stride[0] +
+                                                 inner.lo[1] * v->Conserved_t.stride[1] +
+                                                 inner.lo[2] * v->Conserved_t.stride[2]);
+    if (int st = htr_CalculateMaxSpectralRadius(v, inner, m, scratch, s)) return st;
+    double r = 0.0;
+    if (int st = cuda_status(cudaMemcpyAsync(&r, scratch, sizeof(double), cudaMemcpyDeviceToHost, cs), "dt read")) return st;
+    if (int st = cuda_status(cudaStreamSynchronize(cs), "dt sync")) return st;
+    if (!(r > 0.0)) return fail(HTR_ERR_ARGUMENT, "non-positive spectral radius%s");
+    dt = p->cfl / r;
+  }
+  if (!(dt > 0.0)) return fail(HTR_ERR_ARGUMENT, "non-positive time step%s");
+  if (dt_used) *dt_used = dt;
+  static const double RK[3][3] = {{1.0, 0.0, 1.0}, {3.0 / 4.0, 1.0 / 4.0, 1.0 / 4.0}, {1.0 / 3.0, 2.0 / 3.0, 2.0 / 3.0}};
+  int st;
+  if (p->scheme == HTR_SCHEME_HYBRID) {
+    if ((st = htr_UpdateDucrosSensor(v, fb, fb, p->vorticityScale, s))) return st;
+    if ((st = check_field(v->shockSensorX, 1, "shockSensorX")) || (st = check_field(v->shockSensorY, 1, "shockSensorY")) ||
+        (st = check_field(v->shockSensorZ, 1, "shockSensorZ")))
+      return st;
+    if ((st = cuda_status(htr::launch_shock_sensor(*v, fb, fb, nspec_of(m), 7, cs), "shock sensors"))) return st;
+  }
+  if ((st = htr_InitializeTemporaries(v, fb, m, s))) return st;
+  for (int stage = 1; stage <= 3; stage++) {
+    const double rk[2] = {RK[stage - 1][0], RK[stage - 1][1]};
+    const double sdt = dt * RK[stage - 1][2];
+    if ((st = htr_InitializeTimeDerivatives(v, fb, 0, m, s))) return st;
+    if (p->explicitChemistry)
+      if ((st = htr_AddChemistrySources(v, inner, m, s))) return st;
+    for (int d = 2; d >= 0; d--) {
+      if (p->scheme == HTR_SCHEME_SKEW)
+        st = euler(v, inner, fb, nullptr, 0.0, m, d, 1, 0, s);
+      else if (p->scheme == HTR_SCHEME_HYBRID)
+        st = euler(v, inner, fb, rk, sdt, m, d, 0, 0, s);
+      else
+        st = euler(v, inner, fb, rk, sdt, m, d, 2, p->scheme - 1, s);
+      if (st) return st;
+    }
+    for (int d = 2; d >= 0; d--)
+      if ((st = diffusion(v, inner, fb, m, d, s))) return st;
+    if ((st = htr_UpdateVars(v, fb, stage, dt, 0, m, s))) return st;
+    if ((st = check_common(v, m, inner))) return st;
+    if ((st = with_mix(m, [&](const auto &mix) {
+           return cuda_status(htr::launch_primitive(*v, inner, mix, status_dev, cs), "primitive");
+         })))
+      return st;
+    if ((st = htr_UpdatePropertiesFromPrimitive(v, fb, m, s))) return st;
+  }
+  return HTR_OK;
+}
+
+}  // extern "C"

@@ -1,0 +1,53 @@
+// Launchers of the htr_gb300 kernels (host-callable, one per kernel family).
+#pragma once
+
+#include "common.cuh"
+
+namespace htr {
+
+struct ConstPropDev;
+struct AirDev;
+
+// scheme: 0 hybrid, 1 skew-symmetric, 2 TENO-only; kind: 0 TENO, 1 TENO-A, 2 TENO-LAD
+template <class Mix>
+cudaError_t launch_euler(const htr_fluid_view &v, const htr_rect3 &my, const htr_rect3 &fb,
+                         const double *rk, double dt, const Mix &mix, int dir, int scheme, int kind,
+                         cudaStream_t s);
+
+template <class Mix>
+cudaError_t launch_diffusion(const htr_fluid_view &v, const htr_rect3 &my, const htr_rect3 &fb,
+                             const Mix &mix, int dir, cudaStream_t s);
+
+cudaError_t launch_ducros(const htr_fluid_view &v, const htr_rect3 &my, const htr_rect3 &fb,
+                          double vorticityScale, cudaStream_t s);
+// dirmask: bit d set = compute the sensor of direction d
+cudaError_t launch_shock_sensor(const htr_fluid_view &v, const htr_rect3 &my, const htr_rect3 &fb,
+                                int nspec, int dirmask, cudaStream_t s);
+
+template <class Mix>
+cudaError_t launch_chem_sources(const htr_fluid_view &v, const htr_rect3 &my, const Mix &mix,
+                                cudaStream_t s);
+template <class Mix>
+cudaError_t launch_properties(const htr_fluid_view &v, const htr_rect3 &my, const Mix &mix,
+                              cudaStream_t s);
+template <class Mix>
+cudaError_t launch_conserved(const htr_fluid_view &v, const htr_rect3 &my, const Mix &mix,
+                             cudaStream_t s);
+template <class Mix>
+cudaError_t launch_primitive(const htr_fluid_view &v, const htr_rect3 &my, const Mix &mix,
+                             int *status, cudaStream_t s);
+template <class Mix>
+cudaError_t launch_spectral_radius(const htr_fluid_view &v, const htr_rect3 &my, const Mix &mix,
+                                   double *result, cudaStream_t s);
+template <class Mix>
+cudaError_t launch_update_chemistry(const htr_fluid_view &v, const htr_rect3 &my, double dt,
+                                    const Mix &mix, int *status, cudaStream_t s);
+
+// SSP-RK3 bookkeeping; neq = number of conserved components
+cudaError_t launch_copy_conserved(const htr_fluid_view &v, const htr_rect3 &my, int neq, cudaStream_t s);
+cudaError_t launch_init_rhs(const htr_fluid_view &v, const htr_rect3 &my, int neq, int implicit,
+                            cudaStream_t s);
+cudaError_t launch_rk_update(const htr_fluid_view &v, const htr_rect3 &my, int neq, int stage,
+                             double dt, int implicit, cudaStream_t s);
+
+}  // namespace htr

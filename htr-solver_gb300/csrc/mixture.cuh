@@ -1,0 +1,384 @@
+// Device-side mixture models: thermodynamics, transport and kinetics.
+//
+// The physics is that of HTR's Mixtures (src/Mixtures/ConstPropMix.inl,
+// Species.inl, MultiComponent.inl, Reaction.inl).  Host code
+// (mixture.cpp) folds every temperature-independent sub-expression of those
+// formulas into the constants below once per loaded mixture, keeping the
+// operand order of the reference wherever a value can feed a TENO selection
+// flag (enthalpy, heat capacity, the Newton temperature solve, the pressure
+// derivatives), so those stay bit-identical to the CPU.
+#pragma once
+
+#include "common.cuh"
+
+namespace htr {
+
+constexpr double kRGAS = 8.3144598;
+
+// ---------------------------------------------------------------------------
+struct ConstPropDev {
+  static constexpr int NS = 1;
+  static constexpr int NE = 5;
+  static constexpr bool kReactive = false;
+  double R, gamma, Prandtl;
+  int visc;
+  double cVisc, plTRef, plVRef, suS, suT, suV;
+
+  HTR_HD double MolarWeightFromYi(const double *) const { return kRGAS / R; }
+  HTR_HD double MolarWeightFromXi(const double *) const { return kRGAS / R; }
+  HTR_HD void MolarFractions(double *X, double, const double *Y) const { X[0] = Y[0]; }
+  HTR_HD void MassFractions(double *Y, double, const double *X) const { Y[0] = X[0]; }
+  HTR_HD double RhoFromRhoYi(const double *r) const { return r[0]; }
+  HTR_HD void YiFromRhoYi(double *Y, double rho, const double *r) const { Y[0] = r[0] / rho; }
+  HTR_HD void ClipYi(double *) const {}
+  HTR_HD double Rho(double P, double T, double) const { return P / (R * T); }
+  HTR_HD double HeatCapacity(double, const double *) const { return gamma / (gamma - 1) * R; }
+  HTR_HD double SpeciesEnthalpy(int, double T) const { return gamma / (gamma - 1) * R * T; }
+  HTR_HD double SpeciesMolarWeight(int) const { return kRGAS / R; }
+  HTR_HD double InternalEnergy(double T, const double *) const { return T * R / (gamma - 1.0); }
+  HTR_HD double TFromInternalEnergy(double e0, double, const double *, int *) const {
+    return e0 * (gamma - 1.0) / R;
+  }
+  HTR_HD double TFromRhoAndP(double rho, double MixW, double P) const { return P * MixW / (rho * kRGAS); }
+  HTR_HD double PFromRhoAndT(double rho, double MixW, double T) const { return rho * kRGAS * T / MixW; }
+  HTR_D double Viscosity(double T, const double *) const {
+    if (visc == HTR_VISC_CONSTANT) return cVisc;
+    if (visc == HTR_VISC_POWERLAW) return plVRef * pow((T / plTRef), 0.7);
+    return (suV * pow((T / suT), 1.5)) * ((suT + suS) / (T + suS));
+  }
+  HTR_D double HeatConductivity(double T, const double *X) const {
+    const double cp = gamma / (gamma - 1) * R;
+    return cp / Prandtl * Viscosity(T, X);
+  }
+  HTR_HD double Gamma(double, double, const double *) const { return gamma; }
+  HTR_D double SpeedOfSound(double T, double g, double) const { return sqrt(g * R * T); }
+  HTR_HD void Diffusivity(double *D, double, double, double, const double *) const { D[0] = 0.0; }
+  HTR_HD void ProductionRates(double *w, double, double, double, const double *) const { w[0] = 0.0; }
+  HTR_HD double dpde(double rho, double g) const { return rho * (g - 1); }
+  HTR_HD void dpdrhoi(double *d, double, double T, const double *) const { d[0] = R * T; }
+};
+
+// ---------------------------------------------------------------------------
+struct AirReac {  // one reaction, standard or third-body
+  double A;
+  float n, EovR;
+  int nEd, nPd, nTb;
+  int ed[2], pd[2], tb[5];
+  float nuE[2], nuP[2], eff[5];
+  bool backward;
+};
+
+struct AirDev {
+  static constexpr int NS = 5;
+  static constexpr int NE = 9;
+  static constexpr bool kReactive = true;
+  // species
+  double W[NS], rOvW[NS], RoW[NS];  // RoW = RGAS/W (same value as rOvW, named per formula)
+  float TS1[NS], TS2[NS];
+  double cp[NS][3][7];   // NASA coefficients c0..c6 per range (0 high, 1 mid, 2 low)
+  double hc[NS][3][8];   // enthalpy: -c0, c1, c7, c2, c3*0.50, c4/3, c5*0.25, c6/5
+  double gc[NS][3][9];   // free enthalpy: -0.5*c0, c1, c2, c7, c8, c3, c4/3, c5/6, c6
+  // transport
+  double muNum[NS];      // PI*W/Na*kb  (mu numerator is 5*sqrt(muNum*T))
+  double muDen[NS];      // 16*PI*sigma^2
+  double kbOveps[NS];
+  int geom[NS];
+  double sdDen[NS];      // 8*PI*sigma^2 (self diffusion denominator)
+  double zrot298[NS];    // Z298*FZrot(298)
+  double pi15;           // PI^1.5
+  double wilkeA[NS][NS]; // (W_j/W_i)^0.25
+  double wilkeB[NS][NS]; // sqrt(8*(1 + W_i/W_j))
+  double difNum[NS][NS]; // 2*PI*kb^3*Na*invWij  (num = 3*sqrt(difNum*T^3))
+  double difDen[NS][NS]; // 16*PI*sigma_ij^2
+  double difEps[NS][NS]; // kb/eps_ij
+  // kinetics (2 standard + 3 third-body)
+  AirReac reac[5];
+  // reference scales
+  double TRef, PRef, rhoRef, iMixWRef, ieRef, iCpRef, imuRef, ilamRef, iDiRef, iwiRef;
+
+  HTR_HD int range(int i, double T) const { return (T > TS2[i]) ? 0 : ((T > TS1[i]) ? 1 : 2); }
+
+  // Species.inl:84-101
+  HTR_D double Cp(int i, double T, double Tinv) const {
+    const double *c = cp[i][range(i, T)];
+    return rOvW[i] * (c[0] * Tinv * Tinv + c[1] * Tinv + c[2] +
+                      T * (c[3] + T * (c[4] + T * (c[5] + T * c[6]))));
+  }
+  // Species.inl:125-143 (logT = log(T), Tinv = 1/T)
+  HTR_D double Enthalpy(int i, double T, double Tinv, double logT) const {
+    const double *c = hc[i][range(i, T)];
+    const double E = c[0] * Tinv + c[1] * logT + c[2] + T * (c[3] + T * (c[4] + T * (c[5] + T * (c[6] + c[7] * T))));
+    return E * rOvW[i];
+  }
+  // Species.inl:103-123
+  HTR_D double FreeEnthalpy(int i, double T, double Tinv, double logT) const {
+    const double *c = gc[i][range(i, T)];
+    const double G = c[0] * Tinv * Tinv + c[1] * Tinv * (1.0 + logT) + c[2] * (1.0 - logT) + c[3] * Tinv - c[4];
+    return G - 0.5 * T * (c[5] + T * (c[6] + T * (c[7] + 0.1 * T * c[8])));
+  }
+
+  HTR_HD void ClipYi(double *Y) const {
+#pragma unroll
+    for (int i = 0; i < NS; i++) {
+      Y[i] = smax(Y[i], 1e-60);
+      Y[i] = smin(Y[i], 1.0);
+    }
+  }
+  HTR_HD double MolarWeightFromYi(const double *Y) const {
+    double w = 0.0;
+#pragma unroll
+    for (int i = 0; i < NS; i++) w += Y[i] / W[i];
+    return 1.0 / w;
+  }
+  HTR_HD double MolarWeightFromXi(const double *X) const {
+    double w = 0.0;
+#pragma unroll
+    for (int i = 0; i < NS; i++) w += X[i] * W[i];
+    return w;
+  }
+  HTR_HD void MolarFractions(double *X, double MixW, const double *Y) const {
+#pragma unroll
+    for (int i = 0; i < NS; i++) X[i] = Y[i] * MixW / W[i];
+  }
+  HTR_HD void MassFractions(double *Y, double MixW, const double *X) const {
+#pragma unroll
+    for (int i = 0; i < NS; i++) Y[i] = X[i] * W[i] / MixW;
+  }
+  HTR_HD double RhoFromRhoYi(const double *r) const {
+    double rho = 0.0;
+#pragma unroll
+    for (int i = 0; i < NS; i++) rho += r[i];
+    return rho;
+  }
+  HTR_HD void YiFromRhoYi(double *Y, double rho, const double *r) const {
+    const double irho = 1.0 / rho;
+#pragma unroll
+    for (int i = 0; i < NS; i++) Y[i] = irho * r[i];
+  }
+  HTR_HD double Rho(double P, double T, double MixW) const { return P * MixW * iMixWRef / T; }
+  HTR_D double HeatCapacity(double Tn, const double *Y) const {
+    const double T = Tn * TRef;
+    const double Tinv = 1.0 / T;
+    double c = 0.0;
+#pragma unroll
+    for (int i = 0; i < NS; i++) c += Y[i] * Cp(i, T, Tinv);
+    return c * iCpRef;
+  }
+  HTR_D double SpeciesEnthalpy(int i, double Tn) const {
+    const double T = Tn * TRef;
+    return Enthalpy(i, T, 1.0 / T, log(T)) * ieRef;
+  }
+  HTR_D void SpeciesEnthalpies(double *h, double Tn) const {
+    const double T = Tn * TRef;
+    const double Tinv = 1.0 / T, logT = log(T);
+#pragma unroll
+    for (int i = 0; i < NS; i++) h[i] = Enthalpy(i, T, Tinv, logT) * ieRef;
+  }
+  HTR_HD double SpeciesMolarWeight(int i) const { return W[i]; }
+  HTR_D double InternalEnergy(double Tn, const double *Y) const {
+    const double T = Tn * TRef;
+    const double Tinv = 1.0 / T, logT = log(T);
+    double e = 0.0;
+#pragma unroll
+    for (int i = 0; i < NS; i++) e += Y[i] * (Enthalpy(i, T, Tinv, logT) - kRGAS * T / W[i]);
+    return e * ieRef;
+  }
+  // MultiComponent.inl:188-209; *its (optional) receives the iteration count.
+  HTR_D double TFromInternalEnergy(double e0, double T, const double *Y, int *its) const {
+    const int MAXITS = 1000;
+    const double TOL = 1e-8;
+    double dfdT = 1.0;
+    int j = 0;
+    for (; j < MAXITS; j++) {
+      const double f = e0 - InternalEnergy(T, Y);
+      if (fabs(f / dfdT) < TOL) break;
+      dfdT = 0.0;
+      const double Td = T * TRef;
+      const double Tinv = 1.0 / Td;
+#pragma unroll
+      for (int i = 0; i < NS; i++) dfdT += Y[i] * (Cp(i, Td, Tinv) - kRGAS / W[i]) * iCpRef;
+      T += f / dfdT;
+    }
+    if (its) *its = j;
+    return T;
+  }
+  HTR_HD double TFromRhoAndP(double rho, double MixW, double P) const { return P * MixW * iMixWRef / rho; }
+  HTR_HD double PFromRhoAndT(double rho, double MixW, double T) const { return rho * T / (MixW * iMixWRef); }
+  HTR_D double Gamma(double T, double MixW, const double *Y) const {
+    const double c = HeatCapacity(T, Y);
+    const double Wr = MixW * iMixWRef;
+    return c / (c - 1.0 / Wr);
+  }
+  HTR_D double SpeedOfSound(double T, double g, double MixW) const { return sqrt(g * T / (MixW * iMixWRef)); }
+  HTR_HD double dpde(double rho, double g) const { return rho * (g - 1); }
+  HTR_D void dpdrhoi(double *d, double g, double Tn, const double *Y) const {
+    const double T = Tn * TRef;
+    const double Tinv = 1.0 / T, logT = log(T);
+    double e = 0.0;
+#pragma unroll
+    for (int i = 0; i < NS; i++) {
+      d[i] = Enthalpy(i, T, Tinv, logT) - kRGAS * T / W[i];
+      e += Y[i] * d[i];
+    }
+#pragma unroll
+    for (int i = 0; i < NS; i++) d[i] = (kRGAS * T / W[i] + (g - 1) * (e - d[i])) * ieRef;
+  }
+
+  // --- transport (Species.inl:145-351, MultiComponent.inl:231-311) ----------
+  static HTR_D double omega_mu(double T) {
+    const double num = 3.3530622607 + T * (2.53272006 + T * (2.9024238575 + T * 0.11186138893));
+    const double den = 0.8662326188 + T * (1.3913958626 + T * (3.158490576 + T * (0.18973411754 + T * 0.00018682962894)));
+    return num / den;
+  }
+  static HTR_D double omega_D(double T) {
+    const double num = 6.8728271691 + T * (9.4122316321 + T * (7.7442359037 + T * 0.23424661229));
+    const double den = 1.45337701568 + T * (5.2269794238 + T * (9.7108519575 + T * (0.46539437353 + T * 0.00041908394781)));
+    return num / den;
+  }
+  HTR_D double Mu(int i, double T) const {
+    return 5 * sqrt(muNum[i] * T) / (muDen[i] * omega_mu(T * kbOveps[i]));
+  }
+  // T in kelvin; mu = Mu(i, T); Tinv = 1/T
+  HTR_D double Lam(int i, double T, double Tinv, double mu) const {
+    const double PI = 3.1415926535898;
+    if (geom[i] == 0) return 15.0 / 4 * mu * kRGAS / W[i];
+    const double CvROvR = (geom[i] == 1) ? 1.0 : 1.5;
+    const double CvT = 1.5 * kRGAS;
+    const double CvR = CvROvR * kRGAS;
+    const double CvV = Cp(i, T, Tinv) * W[i] - ((geom[i] == 1) ? 3.5 : 4.0) * kRGAS;
+    const double Dkk = 3 * sqrt(PI * 1.38064852e-23 * T * W[i] / 6.02214086e23) /
+                       (sdDen[i] * omega_D(T * kbOveps[i]));
+    const double fV = Dkk / mu;
+    const double tmp = 1.0 / (kbOveps[i] * T);
+    const double st = sqrt(tmp);
+    const double fz = 1 + 0.5 * pi15 * st + (2 + 0.25 * PI * PI) * tmp + pi15 * (tmp * st);
+    const double Zrot = zrot298[i] / fz;
+    const double A = 2.5 - fV;
+    const double B = Zrot + 2 / PI * (5. / 3 * CvROvR + fV);
+    const double fT = 2.5 * (1. - 2 * CvR * A / (PI * CvT * B));
+    const double fR = fV * (1. + 2 * A / (PI * B));
+    return mu / W[i] * (fT * CvT + fR * CvR + fV * CvV);
+  }
+  // viscosity, conductivity, mixture-averaged diffusivities in one pass
+  HTR_D void Transport(double Tn, double Pn, double MixW, const double *X, double &mu, double &lam,
+                       double *D) const {
+    const double T = Tn * TRef;
+    const double P = Pn * PRef;
+    const double Tinv = 1.0 / T;
+    double muk[NS], smu[NS], ismu[NS];
+#pragma unroll
+    for (int i = 0; i < NS; i++) {
+      muk[i] = Mu(i, T);
+      smu[i] = sqrt(muk[i]);
+      ismu[i] = 1.0 / smu[i];
+    }
+    double m = 0.0;
+#pragma unroll
+    for (int i = 0; i < NS; i++) {
+      double den = 0.0;
+#pragma unroll
+      for (int j = 0; j < NS; j++) {
+        double Phi = 1 + smu[i] * ismu[j] * wilkeA[i][j];
+        Phi *= Phi / wilkeB[i][j];
+        den += X[j] * Phi;
+      }
+      m += X[i] * muk[i] / den;
+    }
+    mu = m * imuRef;
+    double a = 0.0, b = 0.0;
+#pragma unroll
+    for (int i = 0; i < NS; i++) {
+      const double l = Lam(i, T, Tinv, muk[i]);
+      a += X[i] * l;
+      b += X[i] / l;
+    }
+    lam = 0.5 * (a + 1.0 / b) * ilamRef;
+    const double sT3 = sqrt(T * T * T);
+#pragma unroll
+    for (int i = 0; i < NS; i++) D[i] = 0.0;
+#pragma unroll
+    for (int i = 0; i < NS; i++)
+#pragma unroll
+      for (int j = 0; j < i; j++) {
+        const double dij = 3 * sqrt(difNum[i][j]) * sT3 / (difDen[i][j] * P * omega_D(T * difEps[i][j]));
+        const double inv = 1.0 / dij;
+        D[i] += X[j] * inv;
+        D[j] += X[i] * inv;
+      }
+#pragma unroll
+    for (int i = 0; i < NS; i++) {
+      double num = 0.0;
+#pragma unroll
+      for (int j = 0; j < NS; j++)
+        if (j != i) num += X[j] * W[j];
+      D[i] = num / (MixW * D[i]) * iDiRef;
+    }
+  }
+
+  // --- kinetics (Reaction.inl, MultiComponent.inl:370-415) ------------------
+  HTR_D void ProductionRates(double *w, double rhon, double Pn, double Tn, const double *Y) const {
+    const double T = Tn * TRef;
+    const double P = Pn * PRef;
+    const double rho = rhon * rhoRef;
+    const double Tinv = 1.0 / T, logT = log(T);
+    const double lnRP = log(kRGAS / P);
+    double G[NS], C[NS];
+#pragma unroll
+    for (int i = 0; i < NS; i++) {
+      w[i] = 0.0;
+      C[i] = Y[i] * rho / W[i];
+      G[i] = FreeEnthalpy(i, T, Tinv, logT);
+    }
+    const double cM = P / (kRGAS * T);
+#pragma unroll
+    for (int k = 0; k < 5; k++) {
+      const AirReac &r = reac[k];
+      double Kf = r.A;
+      if (r.n != 0.0f) Kf *= exp(double(r.n) * logT);
+      if (fabsf(r.EovR) > 1e-5f) Kf *= exp(-double(r.EovR) * Tinv);
+      double a = 1.0;
+#pragma unroll
+      for (int i = 0; i < 2; i++)
+        if (i < r.nEd) a *= (r.nuE[i] == 1.0f) ? C[r.ed[i]] : pow(C[r.ed[i]], double(r.nuE[i]));
+      double Kb = 0.0, b = 1.0;
+      if (r.backward) {
+        double sumNu = 0.0, sumNuG = 0.0;
+#pragma unroll
+        for (int i = 0; i < 2; i++)
+          if (i < r.nEd) {
+            sumNu -= r.nuE[i];
+            sumNuG -= r.nuE[i] * G[r.ed[i]];
+          }
+#pragma unroll
+        for (int i = 0; i < 2; i++)
+          if (i < r.nPd) {
+            sumNu += r.nuP[i];
+            sumNuG += r.nuP[i] * G[r.pd[i]];
+          }
+        const double lnKc = -sumNuG - sumNu * (logT + lnRP);
+        Kb = Kf * exp(-lnKc);
+#pragma unroll
+        for (int i = 0; i < 2; i++)
+          if (i < r.nPd) b *= (r.nuP[i] == 1.0f) ? C[r.pd[i]] : pow(C[r.pd[i]], double(r.nuP[i]));
+      }
+      double c = 1.0;
+      if (r.nTb > 0) {
+        c = cM;
+#pragma unroll
+        for (int i = 0; i < 5; i++)
+          if (i < r.nTb) c += C[r.tb[i]] * (r.eff[i] - 1.0);
+      }
+      const double R = c * (Kf * a - Kb * b);
+#pragma unroll
+      for (int i = 0; i < 2; i++)
+        if (i < r.nEd) w[r.ed[i]] -= r.nuE[i] * R;
+#pragma unroll
+      for (int i = 0; i < 2; i++)
+        if (i < r.nPd) w[r.pd[i]] += r.nuP[i] * R;
+    }
+#pragma unroll
+    for (int i = 0; i < NS; i++) w[i] *= W[i] * iwiRef;
+  }
+};
+
+}  // namespace htr

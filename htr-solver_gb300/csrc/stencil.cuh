@@ -1,0 +1,308 @@
+// Stencil tables, exact integer powers and the TENO / Kennedy-Gruber
+// operators on the device.
+//
+// Node types, offsets and coefficients are those of HTR
+// (src/prometeo_metric_coeffs.h:54-66, src/prometeo_metric_coeffs_macros.h);
+// the operators follow src/prometeo_metric.inl.  Translation units that
+// include this header and evaluate TENO selection flags are compiled with
+// -fmad=false: every + - * / and sqrt is then rounded exactly as the
+// reference's host build rounds it, and the only non-elementary operation,
+// x^n with n in {4, 6, 12}, is evaluated in double-double arithmetic
+// (Dekker two-product via fma) and rounded once, i.e. correctly rounded.
+#pragma once
+
+#include "common.cuh"
+
+namespace htr {
+
+enum NodeType { Std = 0, L_S, Lp1_S, Lp2_S, Rm3_S, Rm2_S, Rm1_S, R_S, L_C, Lp1_C, Rm2_C, Rm1_C, R_C };
+
+struct NodeDev {
+  int8_t off[5];
+  int8_t kgOrder;
+  double rp[4][6], rm[4][6];
+  double cp[4], cm[4];
+  float interp[2], grad[2];
+  double kg[3];
+};
+
+#define HTR_Z6 {0, 0, 0, 0, 0, 0}
+#define HTR_STD_W {9.0 / 20.0, 6.0 / 20.0, 1.0 / 20.0, 4.0 / 20.0}
+static __constant__ NodeDev kNode[13] = {
+    {{-2, -1, 1, 2, 3}, 3,
+     {{0.0, -1.0 / 6.0, 5.0 / 6.0, 2.0 / 6.0, 0.0, 0.0}, {0.0, 0.0, 2.0 / 6.0, 5.0 / 6.0, -1.0 / 6.0, 0.0},
+      {2.0 / 6.0, -7.0 / 6.0, 11.0 / 6.0, 0.0, 0.0, 0.0}, {0.0, 0.0, 3.0 / 12.0, 13.0 / 12.0, -5.0 / 12.0, 1.0 / 12.0}},
+     {{0.0, 0.0, 2.0 / 6.0, 5.0 / 6.0, -1.0 / 6.0, 0.0}, {0.0, -1.0 / 6.0, 5.0 / 6.0, 2.0 / 6.0, 0.0, 0.0},
+      {0.0, 0.0, 0.0, 11.0 / 6.0, -7.0 / 6.0, 2.0 / 6.0}, {1.0 / 12.0, -5.0 / 12.0, 13.0 / 12.0, 3.0 / 12.0, 0.0, 0.0}},
+     HTR_STD_W, HTR_STD_W, {0.5f, 0.5f}, {0.5f, 0.5f}, {3.0 / 4.0, -3.0 / 20.0, 1.0 / 60.0}},
+    {{0, 0, 1, 1, 1}, 0,
+     {{0, 0, 1.0, 0, 0, 0}, {0, 0, 1.0, 0, 0, 0}, {0, 0, 1.0, 0, 0, 0}, {0, 0, 1.0, 0, 0, 0}},
+     {{0, 0, 1.0, 0, 0, 0}, {0, 0, 1.0, 0, 0, 0}, {0, 0, 1.0, 0, 0, 0}, {0, 0, 1.0, 0, 0, 0}},
+     HTR_STD_W, HTR_STD_W, {1.0f, 0.0f}, {0.0f, 2.0f}, {0.0, 0.0, 0.0}},
+    {{-1, -1, 1, 2, 3}, 1,
+     {{0.0, -2.0 / 4.0, 5.0 / 4.0, 1.0 / 4.0, 0.0, 0.0}, {0.0, 0.0, 2.0 / 6.0, 5.0 / 6.0, -1.0 / 6.0, 0.0},
+      HTR_Z6, {0.0, 0.0, 3.0 / 12.0, 13.0 / 12.0, -5.0 / 12.0, 1.0 / 12.0}},
+     {{0.0, 0.0, 2.0 / 6.0, 5.0 / 6.0, -1.0 / 6.0, 0.0}, {0.0, -2.0 / 4.0, 5.0 / 4.0, 1.0 / 4.0, 0.0, 0.0},
+      {0.0, 0.0, 0.0, 11.0 / 6.0, -7.0 / 6.0, 2.0 / 6.0}, HTR_Z6},
+     {2.0 / 4.0, 1.0 / 4.0, 0.0, 1.0 / 4.0}, {7.0 / 16.0, 8.0 / 16.0, 1.0 / 16.0, 0.0},
+     {0.5f, 0.5f}, {1.0f, 0.5f}, {0.5, 0.0, 0.0}},
+    {{-2, -1, 1, 2, 3}, 2,
+     {{0.0, -1.0 / 6.0, 5.0 / 6.0, 2.0 / 6.0, 0.0, 0.0}, {0.0, 0.0, 2.0 / 6.0, 5.0 / 6.0, -1.0 / 6.0, 0.0},
+      {1.0, -2.0, 2.0, 0.0, 0.0, 0.0}, {0.0, 0.0, 3.0 / 12.0, 13.0 / 12.0, -5.0 / 12.0, 1.0 / 12.0}},
+     {{0.0, 0.0, 2.0 / 6.0, 5.0 / 6.0, -1.0 / 6.0, 0.0}, {0.0, -1.0 / 6.0, 5.0 / 6.0, 2.0 / 6.0, 0.0, 0.0},
+      {0.0, 0.0, 0.0, 11.0 / 6.0, -7.0 / 6.0, 2.0 / 6.0}, {3.0 / 9.0, -7.0 / 9.0, 11.0 / 9.0, 2.0 / 9.0, 0.0, 0.0}},
+     {47.0 / 100.0, 27.0 / 100.0, 10.0 / 100.0, 16.0 / 100.0},
+     {39.0 / 100.0, 27.0 / 100.0, 4.0 / 100.0, 30.0 / 100.0},
+     {0.5f, 0.5f}, {0.5f, 0.5f}, {2.0 / 3.0, -1.0 / 12.0, 0.0}},
+    {{-2, -1, 1, 2, 3}, 2,
+     {{0.0, -1.0 / 6.0, 5.0 / 6.0, 2.0 / 6.0, 0.0, 0.0}, {0.0, 0.0, 2.0 / 6.0, 5.0 / 6.0, -1.0 / 6.0, 0.0},
+      {2.0 / 6.0, -7.0 / 6.0, 11.0 / 6.0, 0.0, 0.0, 0.0}, {0.0, 0.0, 2.0 / 9.0, 11.0 / 9.0, -7.0 / 9.0, 3.0 / 9.0}},
+     {{0.0, 0.0, 2.0 / 6.0, 5.0 / 6.0, -1.0 / 6.0, 0.0}, {0.0, -1.0 / 6.0, 5.0 / 6.0, 2.0 / 6.0, 0.0, 0.0},
+      {0.0, 0.0, 0.0, 2.0, -2.0, 1.0}, {1.0 / 12.0, -5.0 / 12.0, 13.0 / 12.0, 3.0 / 12.0, 0.0, 0.0}},
+     {39.0 / 100.0, 27.0 / 100.0, 4.0 / 100.0, 30.0 / 100.0},
+     {47.0 / 100.0, 27.0 / 100.0, 10.0 / 100.0, 16.0 / 100.0},
+     {0.5f, 0.5f}, {0.5f, 0.5f}, {2.0 / 3.0, -1.0 / 12.0, 0.0}},
+    {{-2, -1, 1, 2, 2}, 1,
+     {{0.0, -1.0 / 6.0, 5.0 / 6.0, 2.0 / 6.0, 0.0, 0.0}, {0.0, 0.0, 1.0 / 4.0, 5.0 / 4.0, -2.0 / 4.0, 0.0},
+      {2.0 / 6.0, -7.0 / 6.0, 11.0 / 6.0, 0.0, 0.0, 0.0}, HTR_Z6},
+     {{0.0, 0.0, 1.0 / 4.0, 5.0 / 4.0, -2.0 / 4.0, 0.0}, {0.0, -1.0 / 6.0, 5.0 / 6.0, 2.0 / 6.0, 0.0, 0.0},
+      HTR_Z6, {1.0 / 12.0, -5.0 / 12.0, 13.0 / 12.0, 3.0 / 12.0, 0.0, 0.0}},
+     {7.0 / 16.0, 8.0 / 16.0, 1.0 / 16.0, 0.0}, {2.0 / 4.0, 1.0 / 4.0, 0.0, 1.0 / 4.0},
+     {0.5f, 0.5f}, {0.5f, 0.5f}, {0.5, 0.0, 0.0}},
+    {{-1, -1, 1, 1, 1}, 0,
+     {{0, 0, 0, 1.0, 0, 0}, {0, 0, 0, 1.0, 0, 0}, {0, 0, 0, 1.0, 0, 0}, {0, 0, 0, 1.0, 0, 0}},
+     {{0, 0, 0, 1.0, 0, 0}, {0, 0, 0, 1.0, 0, 0}, {0, 0, 0, 1.0, 0, 0}, {0, 0, 0, 1.0, 0, 0}},
+     HTR_STD_W, HTR_STD_W, {0.0f, 1.0f}, {0.5f, 1.0f}, {0.0, 0.0, 0.0}},
+    {{-1, -1, 0, 0, 0}, 0, {HTR_Z6, HTR_Z6, HTR_Z6, HTR_Z6}, {HTR_Z6, HTR_Z6, HTR_Z6, HTR_Z6},
+     {0, 0, 0, 0}, {0, 0, 0, 0}, {0.5f, 0.5f}, {2.0f, 0.0f}, {0.0, 0.0, 0.0}},
+    {{0, 0, 1, 2, 2}, 1, {{0, 0, 1.0, 0, 0, 0}, HTR_Z6, HTR_Z6, HTR_Z6},
+     {{0, 0, 0, 1.0, 0, 0}, HTR_Z6, HTR_Z6, HTR_Z6}, {1.0, 0.0, 0.0, 0.0}, {1.0, 0.0, 0.0, 0.0},
+     {0.5f, 0.5f}, {0.0f, 1.0f}, {0.5, 0.0, 0.0}},
+    {{-1, -1, 1, 2, 2}, 2,
+     {{0.0, -1.0 / 6.0, 5.0 / 6.0, 2.0 / 6.0, 0.0, 0.0}, {0.0, 0.0, 2.0 / 6.0, 5.0 / 6.0, -1.0 / 6.0, 0.0}, HTR_Z6, HTR_Z6},
+     {{0.0, 0.0, 2.0 / 6.0, 5.0 / 6.0, -1.0 / 6.0, 0.0}, {0.0, -1.0 / 6.0, 5.0 / 6.0, 2.0 / 6.0, 0.0, 0.0}, HTR_Z6, HTR_Z6},
+     {1.0 / 2.0, 1.0 / 2.0, 0.0, 0.0}, {1.0 / 2.0, 1.0 / 2.0, 0.0, 0.0},
+     {0.5f, 0.5f}, {0.5f, 0.5f}, {2.0 / 3.0, -1.0 / 12.0, 0.0}},
+    {{-1, -1, 1, 2, 2}, 2,
+     {{0.0, -1.0 / 6.0, 5.0 / 6.0, 2.0 / 6.0, 0.0, 0.0}, {0.0, 0.0, 2.0 / 6.0, 5.0 / 6.0, -1.0 / 6.0, 0.0}, HTR_Z6, HTR_Z6},
+     {{0.0, 0.0, 2.0 / 6.0, 5.0 / 6.0, -1.0 / 6.0, 0.0}, {0.0, -1.0 / 6.0, 5.0 / 6.0, 2.0 / 6.0, 0.0, 0.0}, HTR_Z6, HTR_Z6},
+     {1.0 / 2.0, 1.0 / 2.0, 0.0, 0.0}, {1.0 / 2.0, 1.0 / 2.0, 0.0, 0.0},
+     {0.5f, 0.5f}, {0.5f, 0.5f}, {2.0 / 3.0, -1.0 / 12.0, 0.0}},
+    {{-1, -1, 1, 1, 1}, 1, {{0, 0, 1.0, 0, 0, 0}, HTR_Z6, HTR_Z6, HTR_Z6},
+     {{0, 0, 0, 1.0, 0, 0}, HTR_Z6, HTR_Z6, HTR_Z6}, {1.0, 0.0, 0.0, 0.0}, {1.0, 0.0, 0.0, 0.0},
+     {0.5f, 0.5f}, {0.5f, 0.5f}, {0.5, 0.0, 0.0}},
+    {{-1, -1, 0, 0, 0}, 0, {HTR_Z6, HTR_Z6, HTR_Z6, HTR_Z6}, {HTR_Z6, HTR_Z6, HTR_Z6, HTR_Z6},
+     {0, 0, 0, 0}, {0, 0, 0, 0}, {0.5f, 0.5f}, {1.0f, 0.0f}, {0.0, 0.0, 0.0}},
+};
+#undef HTR_Z6
+#undef HTR_STD_W
+
+// Powers of ten as float (TENO cut-offs).
+static __constant__ float kP10[14] = {1,    1e-1, 1e-2, 1e-3,  1e-4,  1e-5,  1e-6,
+                                      1e-7, 1e-8, 1e-9, 1e-10, 1e-11, 1e-12, 1e-13};
+
+HTR_D double interp2(int t, double a, double b) {
+  return __dadd_rn(__dmul_rn(double(kNode[t].interp[0]), a), __dmul_rn(double(kNode[t].interp[1]), b));
+}
+HTR_D double deriv(int t, double xm1, double x, double xp1, double m) {
+  return __dmul_rn(__dadd_rn(__dmul_rn(double(kNode[t].grad[0]), __dsub_rn(x, xm1)),
+                             __dmul_rn(double(kNode[t].grad[1]), __dsub_rn(xp1, x))),
+                   m);
+}
+
+// ---------------------------------------------------------------------------
+// correctly rounded x^n in double-double (Dekker / Knuth error-free products)
+// ---------------------------------------------------------------------------
+struct DD {
+  double h, l;
+};
+HTR_D DD dd_sq(double x) {
+  DD r;
+  r.h = __dmul_rn(x, x);
+  r.l = __fma_rn(x, x, -r.h);
+  return r;
+}
+HTR_D DD dd_mul_d(DD a, double x) {  // (a.h + a.l) * x
+  DD r;
+  const double p = __dmul_rn(a.h, x);
+  const double e = __fma_rn(a.h, x, -p);
+  const double l = __fma_rn(a.l, x, e);
+  r.h = __dadd_rn(p, l);
+  r.l = __dsub_rn(l, __dsub_rn(r.h, p));
+  return r;
+}
+HTR_D DD dd_square(DD a) {  // (a.h + a.l)^2, dropping a.l^2
+  DD r;
+  const double p = __dmul_rn(a.h, a.h);
+  const double e = __fma_rn(a.h, a.h, -p);
+  const double l = __fma_rn(__dadd_rn(a.h, a.h), a.l, e);
+  r.h = __dadd_rn(p, l);
+  r.l = __dsub_rn(l, __dsub_rn(r.h, p));
+  return r;
+}
+HTR_D double dd_round(DD a) {
+  // an overflowed leading term is returned as is (the error terms are NaN there)
+  return isinf(a.h) ? a.h : __dadd_rn(a.h, a.l);
+}
+HTR_D double pow4_exact(double x) { return dd_round(dd_square(dd_sq(x))); }
+HTR_D DD pow6_dd(double x) { return dd_square(dd_mul_d(dd_sq(x), x)); }
+HTR_D double pow6_exact(double x) { return dd_round(pow6_dd(x)); }
+HTR_D double pow12_exact(double x) {
+  const DD s = pow6_dd(x);
+  if (isinf(s.h)) return s.h;
+  return dd_round(dd_square(s));
+}
+
+// ---------------------------------------------------------------------------
+// smoothness measures of the four TENO candidates (metric.inl:442-449)
+// ---------------------------------------------------------------------------
+struct Smooth {
+  double s1, s2, s3, s4, tau6;
+};
+HTR_D Smooth smoothness(double ym2, double ym1, double y, double yp1, double yp2, double yp3) {
+  const double C13 = 13.0 / 12.0, C23 = 3.0 / 12.0, C14 = 1.0 / 36.0, C24 = 13.0 / 12.0,
+               C34 = 781.0 / 720.0;
+  Smooth s;
+  double a1, a2, a3;
+  a1 = (ym1 - 2 * y + yp1);
+  a2 = (ym1 - yp1);
+  s.s1 = C13 * a1 * a1 + C23 * a2 * a2;
+  a1 = (y - 2 * yp1 + yp2);
+  a2 = (3 * y - 4 * yp1 + yp2);
+  s.s2 = C13 * a1 * a1 + C23 * a2 * a2;
+  a1 = (ym2 - 2 * ym1 + y);
+  a2 = (3 * y - 4 * ym1 + ym2);
+  s.s3 = C13 * a1 * a1 + C23 * a2 * a2;
+  a1 = (-11 * y + 18 * yp1 - 9 * yp2 + 2 * yp3);
+  a2 = (2 * y - 5 * yp1 + 4 * yp2 - yp3);
+  a3 = (-y + 3 * yp1 - 3 * yp2 + yp3);
+  s.s4 = C14 * a1 * a1 + C24 * a2 * a2 + C34 * a3 * a3;
+  s.tau6 = fabs(s.s4 - (s.s3 + s.s2 + 4 * s.s1) / 6);
+  return s;
+}
+
+enum TenoKind { kTENO = 0, kTENOA = 1, kTENOLAD = 2 };
+
+// One TENO reconstruction at face c+1/2 from y = (c-2 .. c+3); MINUS gives
+// the right-biased value (metric.inl:431-1038).  Returns the 4 selection
+// flags in *mask (bit k = stencil k kept).
+template <int KIND, bool MINUS>
+HTR_D double teno(double ym2, double ym1, double y, double yp1, double yp2, double yp3, int t,
+                  unsigned *mask) {
+  // optimal weights of this side (tables indexed directly: constant space)
+  const double W0 = MINUS ? kNode[t].cm[0] : kNode[t].cp[0];
+  const double W1 = MINUS ? kNode[t].cm[1] : kNode[t].cp[1];
+  const double W2 = MINUS ? kNode[t].cm[2] : kNode[t].cp[2];
+  const double W3 = MINUS ? kNode[t].cm[3] : kNode[t].cp[3];
+  const Smooth s = MINUS ? smoothness(yp3, yp2, yp1, y, ym1, ym2) : smoothness(ym2, ym1, y, yp1, yp2, yp3);
+  const double eps = KIND == kTENO ? 1e-10 : (KIND == kTENOA ? 1e-8 : 1e-16);
+  const double chi1 = s.tau6 / (s.s1 + eps);
+  const double chi2 = s.tau6 / (s.s2 + eps);
+  const double chi3 = s.tau6 / (s.s3 + eps);
+  const double chi4 = s.tau6 / (s.s4 + eps);
+  double a1 = pow6_exact(1 + chi1);
+  double a2 = pow6_exact(1 + chi2);
+  double a3 = pow6_exact(1 + chi3);
+  double a4 = pow6_exact(1 + chi4);
+  double cut;
+  bool zero_unused = true;
+  if (KIND == kTENO) {
+    cut = 1e-6;
+  } else if (KIND == kTENOA) {
+    if (t == Std) {
+      zero_unused = false;
+      const double rc = 0.2;
+      const double Ren_eps = 0.9 * rc * 1e-16 / (1.0 - 0.9 * rc);
+      const double Ren_irc = 1.0 / rc;
+      const double v2 = fabs(ym1 - ym2), v3 = fabs(y - ym1), v4 = fabs(yp1 - y);
+      const double v5 = fabs(yp2 - yp1), v6 = fabs(yp3 - yp2);
+      double eta = smin((2 * v2 * v3 + Ren_eps) / (v2 * v2 + v3 * v3 + Ren_eps),
+                        (2 * v3 * v4 + Ren_eps) / (v3 * v3 + v4 * v4 + Ren_eps));
+      eta = smin(eta, (2 * v4 * v5 + Ren_eps) / (v4 * v4 + v5 * v5 + Ren_eps));
+      eta = smin(eta, (2 * v5 * v6 + Ren_eps) / (v5 * v5 + v6 * v6 + Ren_eps));
+      const double delta = 1 - smin(eta * Ren_irc, 1.0);
+      const double decay = pow4_exact(1 - delta) * (1 + 4 * delta);
+      const int power = min(max(int(floor(9.5 - 3.5 * (1 - decay))), 0), 13);
+      cut = double(kP10[power]);
+    } else {
+      cut = double(kP10[4]);
+    }
+  } else {
+    const double chiMax = smax(chi1, smax(chi2, smax(chi3, chi4)));
+    const double theta = 1.0 / (1 + chiMax * 1e-1);
+    const int power = min(max(int(floor(3.0 + 9.5 * theta)), 0), 13);
+    cut = double(kP10[power]);
+  }
+  if (zero_unused) {
+    if (W0 < 1e-10) a1 = 0.0;
+    if (W1 < 1e-10) a2 = 0.0;
+    if (W2 < 1e-10) a3 = 0.0;
+    if (W3 < 1e-10) a4 = 0.0;
+  }
+  const double a = 1.0 / (a1 + a2 + a3 + a4);
+  const int b1 = (a1 * a < cut) ? 0 : 1;
+  const int b2 = (a2 * a < cut) ? 0 : 1;
+  const int b3 = (a3 * a < cut) ? 0 : 1;
+  const int b4 = (a4 * a < cut) ? 0 : 1;
+  if (mask) *mask = unsigned(b1) | (unsigned(b2) << 1) | (unsigned(b3) << 2) | (unsigned(b4) << 3);
+  const double base = MINUS ? yp1 : y;
+  double v[4];
+  if (t == Std) {
+    // zero entries of the standard stencils skipped: adding an exact zero
+    // does not change a rounded sum.
+    if (!MINUS) {
+      v[0] = ym1 * (-1.0 / 6.0) + y * (5.0 / 6.0) + yp1 * (2.0 / 6.0) - base;
+      v[1] = y * (2.0 / 6.0) + yp1 * (5.0 / 6.0) + yp2 * (-1.0 / 6.0) - base;
+      v[2] = ym2 * (2.0 / 6.0) + ym1 * (-7.0 / 6.0) + y * (11.0 / 6.0) - base;
+      v[3] = y * (3.0 / 12.0) + yp1 * (13.0 / 12.0) + yp2 * (-5.0 / 12.0) + yp3 * (1.0 / 12.0) - base;
+    } else {
+      v[0] = y * (2.0 / 6.0) + yp1 * (5.0 / 6.0) + yp2 * (-1.0 / 6.0) - base;
+      v[1] = ym1 * (-1.0 / 6.0) + y * (5.0 / 6.0) + yp1 * (2.0 / 6.0) - base;
+      v[2] = yp1 * (11.0 / 6.0) + yp2 * (-7.0 / 6.0) + yp3 * (2.0 / 6.0) - base;
+      v[3] = ym2 * (1.0 / 12.0) + ym1 * (-5.0 / 12.0) + y * (13.0 / 12.0) + yp1 * (3.0 / 12.0) - base;
+    }
+  } else {
+#pragma unroll
+    for (int k = 0; k < 4; k++) {
+      const double r0 = MINUS ? kNode[t].rm[k][0] : kNode[t].rp[k][0];
+      const double r1 = MINUS ? kNode[t].rm[k][1] : kNode[t].rp[k][1];
+      const double r2 = MINUS ? kNode[t].rm[k][2] : kNode[t].rp[k][2];
+      const double r3 = MINUS ? kNode[t].rm[k][3] : kNode[t].rp[k][3];
+      const double r4 = MINUS ? kNode[t].rm[k][4] : kNode[t].rp[k][4];
+      const double r5 = MINUS ? kNode[t].rm[k][5] : kNode[t].rp[k][5];
+      v[k] = ym2 * r0 + ym1 * r1 + y * r2 + yp1 * r3 + yp2 * r4 + yp3 * r5 - base;
+    }
+  }
+  const double c1 = W0 * b1, c2 = W1 * b2, c3 = W2 * b3, c4 = W3 * b4;
+  const double ia = 1.0 / (c1 + c2 + c3 + c4);
+  const double w1 = c1 * ia, w2 = c2 * ia, w3 = c3 * ia, w4 = c4 * ia;
+  return base + w1 * v[0] + w2 * v[1] + w3 * v[2] + w4 * v[3];
+}
+
+// Shock sensor of the hybrid scheme on a positive scalar (metric.inl:351-403).
+HTR_D bool teno_a_sensor(double ym2, double ym1, double y, double yp1, double yp2, double yp3,
+                         int t, double Phi) {
+  const double rc = 0.2;
+  const double Ren_eps = 0.9 * rc * 1e-6 / (1.0 - 0.9 * rc);
+  const double Ren_irc = 1.0 / rc;
+  if (t == L_S || t == Rm1_S) return true;
+  if (t == L_C || t == Rm1_C) {
+    const double v1 = (t == L_C) ? yp1 - y : y - ym1;
+    const double v2 = (t == L_C) ? yp2 - yp1 : yp1 - y;
+    const double eta = (fabs(2.0 * v1 * v2) + Ren_eps) / (v1 * v1 + v2 * v2 + Ren_eps);
+    return ((1.0 - smin(1.0, Ren_irc * eta)) < 0.5);
+  }
+  const Smooth s = smoothness(ym2, ym1, y, yp1, yp2, yp3);
+  const double eps = 1e-8;
+  const double a1 = pow6_exact(1 + s.tau6 / (s.s1 + eps));
+  const double a2 = pow6_exact(1 + s.tau6 / (s.s2 + eps));
+  const double a3 = pow6_exact(1 + s.tau6 / (s.s3 + eps));
+  const double a4 = pow6_exact(1 + s.tau6 / (s.s4 + eps));
+  const double a = 1.0 / (a1 + a2 + a3 + a4);
+  const double decay = pow12_exact(1 - Phi) * (1 + 12 * Phi);
+  const int power = min(max(int(floor(12.5 - 11.5 * (1 - decay))), 0), 13);
+  const double cut = double(kP10[power]);
+  return ((a1 * a > cut) && (a2 * a > cut) && (a3 * a > cut) && (a4 * a > cut));
+}
+
+}  // namespace htr

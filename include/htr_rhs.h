@@ -208,6 +208,34 @@ int htr_InitializeTimeDerivatives(const htr_fluid_view *view, htr_rect3 my_fluid
 int htr_UpdateVars(const htr_fluid_view *view, htr_rect3 my_fluid, int stage, double deltaTime,
                    int implicitChemistry, htr_mixture_t mix, htr_stream_t stream);
 
+/* --- fused time step (the driver of src/prometeo.rg:1153-1172, 1342-1486) --
+ * Not a reference task: one whole SSP-RK3 step of a periodic grid
+ * (sensors once per step, then per stage: RHS in the reference's order
+ * chemistry -> Euler Z,Y,X -> diffusion Z,Y,X, RK update, primitive and
+ * property refresh), asynchronous on `stream`.  With cfl > 0 the step size
+ * is cfl / max spectral radius (one device-to-host read of the radius);
+ * otherwise deltaTime is used and the call issues no synchronisation, so it
+ * can be captured in a CUDA graph. */
+typedef enum {
+  HTR_SCHEME_HYBRID = 0,
+  HTR_SCHEME_TENO = 1,
+  HTR_SCHEME_TENOA = 2,
+  HTR_SCHEME_TENOLAD = 3,
+  HTR_SCHEME_SKEW = 4
+} htr_scheme;
+
+typedef struct {
+  int scheme;               /* htr_scheme */
+  double vorticityScale;    /* Ducros sensor scale of the hybrid scheme */
+  double cfl;               /* > 0: CFL-based step size */
+  double deltaTime;         /* used when cfl <= 0 */
+  int explicitChemistry;    /* add chemistry sources to the RHS */
+} htr_step_params;
+
+int htr_rk3_step(const htr_fluid_view *view, htr_rect3 interior, htr_rect3 fluid_bounds,
+                 const htr_step_params *params, htr_mixture_t mix, double *dt_used,
+                 int *status_dev, htr_stream_t stream);
+
 #ifdef __cplusplus
 }
 #endif

@@ -18,15 +18,11 @@
 
 #include "htr_rhs.h"
 #include "mixtures.hpp"
+#include "port.hpp"
 #include "stencils.hpp"
 
 using namespace oport;
 
-struct htr_mixture_s {
-  int eos;
-  ConstProp cp;
-  Air air;
-};
 
 namespace {
 

@@ -1,0 +1,50 @@
+"""One small hybrid RHS evaluation on cuda:0 checked against the CPU oracle."""
+import ctypes as C
+
+import numpy as np
+
+
+def run():
+    import torch
+
+    from htr_gb300 import runtime
+
+    import oracle
+    from tests import util
+
+    port = oracle.port_lib()
+    fl, h, m = util.make_state(port, "tg", (12, 10, 8), seed=1)
+    host = fl.copy()
+    oracle.update_sensors(port, host, h, 1.0)
+    oracle.update_derivatives(port, host, h, 1, 0.01, "Hybrid", chemistry=False)
+    gh = runtime.load_mixture(fl.meta["eos"], m)
+    dev = fl.to_device("cuda:0")
+    gpu = runtime.lib()
+    v = dev.view()
+    r = dev.bounds()
+    s = runtime.stream_handle()
+    util.call(gpu, "htr_UpdateDucrosSensor", C.byref(v), r, r, 1.0, s)
+    for d in "XYZ":
+        util.call(gpu, f"htr_UpdateShockSensor{d}", C.byref(v), r, r, gh, s)
+    util.call(gpu, "htr_InitializeTimeDerivatives", C.byref(v), r, 0, gh, s)
+    rk = (C.c_double * 2)(1.0, 0.0)
+    for d in "ZYX":
+        util.call(gpu, f"htr_UpdateUsingHybridEulerFlux{d}", C.byref(v), r, r, rk, 0.01, gh, s)
+    for d in "ZYX":
+        util.call(gpu, f"htr_UpdateUsingDiffusionFlux{d}", C.byref(v), r, r, gh, s)
+    torch.cuda.synchronize()
+    out = dev.to_host()
+    for d in "XYZ":
+        assert np.array_equal(out[f"shockSensor{d}"], host[f"shockSensor{d}"]), d
+    err = util.rel_err(out["Conserved_t"], host["Conserved_t"]).max()
+    assert err <= util.RHS_REL_TOL, err
+    print(f"smoke ok: max rel err {err:.3e}")
+
+
+if __name__ == "__main__":
+    import os
+    import sys
+    sys.path.insert(0, os.path.dirname(os.path.dirname(os.path.abspath(__file__))))
+    import __graft_entry__
+    __graft_entry__.load_package()
+    run()
