@@ -1,0 +1,379 @@
+"""Benchmark of the GB300 explicit RHS: FP64 RHS cell-updates/s.
+
+Workload: 3-D periodic 256^3 box of 5-species reacting air (AirMix, 2 + 3
+Park-type reactions), seeded synthetic fields (T 300-8000 K, p 0.1-10 bar,
+Dirichlet mass fractions, Mach 0.5-3 solenoidal + compressive velocity),
+hybrid TENO / Kennedy-Gruber Euler flux with the Ducros/TENO-A shock sensor,
+diffusion with mixture-averaged transport, explicit chemistry sources, SSP
+RK3.  One "step" is one RK3 time step (3 full RHS evaluations + state
+refresh); a cell-update is one full RHS evaluation of one cell.
+
+    python bench.py [--gpus N] [--steps K] [--warmup W] [--impl reference] [--n 256]
+
+The step size is fixed for the run: min(CFL 0.8 acoustic step, half the
+fastest chemical time scale of the initial state), so that explicit
+chemistry stays stable; the RHS work per step does not depend on it.
+
+Prints one JSON line (rank 0).  N > 1 runs N independent replicas (one grid
+per GPU, no data exchange); value is the total over ranks.
+"""
+import argparse
+import ctypes as C
+import json
+import os
+import subprocess
+import sys
+import threading
+import time
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+import __graft_entry__  # noqa: E402
+
+__graft_entry__.load_package()
+from htr_gb300 import abi, workloads  # noqa: E402
+
+METRIC = "FP64 RHS cell-updates/s"
+UNIT = "cell-updates/s"
+# Compulsory bytes of one full-RHS cell-update at the reference field layout
+# (5-species air): every input field read once, Conserved_t written once.
+BYTES_PER_CELL_UPDATE_AIR = 495
+MEASURED_PEAKS = os.path.join(ROOT, "MEASURED_PEAKS.json")
+
+
+def dist_env():
+    ws = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    return ws, rank, local
+
+
+def hbm_peak():
+    try:
+        with open(MEASURED_PEAKS) as f:
+            return float(json.load(f)["hbm_gbs"]), "measured"
+    except Exception:
+        return 6800.0, "fallback"
+
+
+class ClockSampler:
+    """Samples nvidia-smi clocks and throttle reasons during the timed region."""
+    Q = ("clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.hw_slowdown,"
+         "clocks_event_reasons.hw_thermal_slowdown,clocks_event_reasons.sw_thermal_slowdown,"
+         "clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, index):
+        self.index = index
+        self.proc = None
+        self.lines = []
+
+    def start(self):
+        try:
+            self.proc = subprocess.Popen(["nvidia-smi", "-i", str(self.index), f"--query-gpu={self.Q}",
+                                          "--format=csv,noheader,nounits", "-lms", "200"],
+                                         stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+            self.t = threading.Thread(target=self._read, daemon=True)
+            self.t.start()
+        except Exception:
+            self.proc = None
+
+    def _read(self):
+        for line in self.proc.stdout:
+            self.lines.append(line.strip())
+
+    def stop(self):
+        if self.proc is None:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["nvidia-smi unavailable"]}
+        self.proc.terminate()
+        try:
+            self.proc.wait(timeout=5)
+        except Exception:
+            self.proc.kill()
+        sm, smax, reasons = [], [], set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for line in self.lines:
+            parts = [p.strip() for p in line.split(",")]
+            if len(parts) < 7:
+                continue
+            try:
+                sm.append(float(parts[0]))
+                smax.append(float(parts[1]))
+            except ValueError:
+                continue
+            for n, v in zip(names, parts[3:7]):
+                if v.lower() == "active":
+                    reasons.add(n)
+        return {"sm_mhz": float(np.median(sm)) if sm else None,
+                "sm_max_mhz": float(max(smax)) if smax else None,
+                "reasons": sorted(reasons), "samples": len(sm)}
+
+
+def build_state(n, seed, device, lib, runtime):
+    fl = workloads.air_box(n, seed=seed)
+    eos = fl.meta["eos"]
+    m = workloads.make_mixture_struct(lib, eos, fl.meta["mix"])
+    gh = runtime.load_mixture(eos, m)
+    dev = fl.to_device(device)
+    del fl
+    workloads.derive_state(lib, dev, gh, runtime.stream_handle())
+    return dev, gh, m
+
+
+def choose_dt(dev, gh, lib, runtime):
+    """min(CFL 0.8 acoustic step, 0.5 x fastest chemical time scale)."""
+    import torch
+    v = dev.view()
+    out = torch.zeros(1, dtype=torch.float64, device=dev.device)
+    s = runtime.stream_handle()
+    abi.check(lib, lib.htr_CalculateMaxSpectralRadius(C.byref(v), dev.interior(), gh,
+                                                      C.cast(C.c_void_p(out.data_ptr()), C.POINTER(C.c_double)), s), "cfl")
+    abi.check(lib, lib.htr_InitializeTimeDerivatives(C.byref(v), dev.bounds(), 0, gh, s), "init")
+    abi.check(lib, lib.htr_AddChemistrySources(C.byref(v), dev.interior(), gh, s), "chem")
+    torch.cuda.synchronize()
+    w = dev["Conserved_t"][..., :5].abs()
+    rhoi = dev["Conserved"][..., :5]
+    rho = dev["rho"][..., None]
+    sig = rhoi > 1e-3 * rho
+    tau = torch.where(sig, rhoi / w.clamp_min(1e-300), torch.full_like(rhoi, float("inf"))).min().item()
+    return min(0.8 / out.item(), 0.5 * tau)
+
+
+def kernel_profile(dev, gh, lib, runtime, dt, reps=1):
+    """CUDA-event time of each kernel family over one RHS stage (untimed pass)."""
+    import torch
+    v = dev.view()
+    s = runtime.stream_handle()
+    inner, fb = dev.interior(), dev.bounds()
+    rk = (C.c_double * 2)(1.0, 0.0)
+    calls = {
+        "ducros+shock": lambda: (lib.htr_UpdateDucrosSensor(C.byref(v), fb, fb, 1.0, s),
+                                 [getattr(lib, f"htr_UpdateShockSensor{d}")(C.byref(v), fb, fb, gh, s) for d in "XYZ"]),
+        "chemistry": lambda: lib.htr_AddChemistrySources(C.byref(v), inner, gh, s),
+        "euler_hybrid_z": lambda: lib.htr_UpdateUsingHybridEulerFluxZ(C.byref(v), inner, fb, rk, dt, gh, s),
+        "euler_hybrid_y": lambda: lib.htr_UpdateUsingHybridEulerFluxY(C.byref(v), inner, fb, rk, dt, gh, s),
+        "euler_hybrid_x": lambda: lib.htr_UpdateUsingHybridEulerFluxX(C.byref(v), inner, fb, rk, dt, gh, s),
+        "diffusion_z": lambda: lib.htr_UpdateUsingDiffusionFluxZ(C.byref(v), inner, fb, gh, s),
+        "diffusion_y": lambda: lib.htr_UpdateUsingDiffusionFluxY(C.byref(v), inner, fb, gh, s),
+        "diffusion_x": lambda: lib.htr_UpdateUsingDiffusionFluxX(C.byref(v), inner, fb, gh, s),
+        "properties": lambda: lib.htr_UpdatePropertiesFromPrimitive(C.byref(v), fb, gh, s),
+        "primitive": lambda: lib.htr_UpdatePrimitiveFromConserved(C.byref(v), inner, gh, s),
+    }
+    out = {}
+    stream = torch.cuda.current_stream()
+    for name, fn in calls.items():
+        fn()
+        stream.synchronize()
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record(stream)
+        for _ in range(reps):
+            fn()
+        e1.record(stream)
+        e1.synchronize()
+        out[name] = e0.elapsed_time(e1) / reps
+    return out
+
+
+# compulsory bytes per cell of each kernel family (5-species air, fields read
+# once, written fields counted once; Conserved_t read-modify-write = 2 x 72)
+KERNEL_BYTES = {
+    "euler_hybrid": 8 * (9 + 9 + 1 + 5 + 3 + 1 + 1 + 1) + 4 + 1 + 2 * 72,
+    "diffusion": 8 * (9 + 1 + 5 + 1 + 1 + 1 + 5 + 3 + 1 + 3) + 3 * 4 + 2 * 72,
+    "properties": 8 * (1 + 1 + 5) + 8 * (5 + 1 + 1 + 1 + 5 + 1),
+    "primitive": 8 * (9 + 1) + 8 * (1 + 1 + 5 + 3),
+    "chemistry": 8 * (1 + 1 + 1 + 5) + 2 * 8 * 5,
+}
+
+
+def fp64_peak(lib):
+    lib.htr_probe_fp64_tflops.argtypes = [C.c_int, C.POINTER(C.c_double)]
+    lib.htr_probe_fp64_tflops.restype = C.c_int
+    t = C.c_double(0)
+    if lib.htr_probe_fp64_tflops(200000, C.byref(t)) != 0:
+        return None
+    return t.value
+
+
+def run_gpu(args):
+    import torch
+    ws, rank, local = dist_env()
+    if ws > 1:
+        import torch.distributed as dist
+        dist.init_process_group("nccl", init_method="env://")
+    torch.cuda.set_device(local)
+    device = f"cuda:{local}"
+    from htr_gb300 import runtime
+    lib = runtime.lib()
+    dev, gh, mstruct = build_state(args.n, 1234 + rank, device, lib, runtime)
+    ncell = dev.ncells
+    dt = choose_dt(dev, gh, lib, runtime)
+    stream = torch.cuda.current_stream()
+
+    def barrier():
+        if ws > 1:
+            torch.distributed.barrier()
+        torch.cuda.synchronize()
+
+    for _ in range(args.warmup):
+        runtime.rk3_step(dev, gh, dt=dt, chemistry=True)
+    barrier()
+    clocks = ClockSampler(local)
+    clocks.start()
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    e0.record(stream)
+    for _ in range(args.steps):
+        runtime.rk3_step(dev, gh, dt=dt, chemistry=True)
+    e1.record(stream)
+    barrier()
+    clk = clocks.stop()
+    ms = e0.elapsed_time(e1)
+    t = torch.tensor([ms], dtype=torch.float64, device=device)
+    if ws > 1:
+        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
+    ms_max = t.item()
+    total_updates = 3.0 * ncell * args.steps * ws
+    value = total_updates / (ms_max * 1e-3)
+
+    # end-to-end through the public API with pinned host buffers: per step the
+    # time-dependent state goes host -> device, the step runs, Conserved comes back
+    state_fields = ["Conserved", "pressure", "temperature", "MassFracs", "MolarFracs", "velocity",
+                    "rho", "mu", "lam", "Di", "SoS"]
+    host = {k: torch.empty_like(dev[k], device="cpu").pin_memory() for k in state_fields}
+    for k in state_fields:
+        host[k].copy_(dev[k])
+    out_host = torch.empty_like(dev["Conserved"], device="cpu").pin_memory()
+    torch.cuda.synchronize()
+    h2d = sum(host[k].numel() * host[k].element_size() for k in state_fields)
+    d2h = out_host.numel() * out_host.element_size()
+    e2e_steps = max(1, min(args.steps, 3))
+    barrier()
+    f0, f1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    f0.record(stream)
+    for _ in range(e2e_steps):
+        for k in state_fields:
+            dev[k].copy_(host[k], non_blocking=True)
+        runtime.rk3_step(dev, gh, dt=dt, chemistry=True)
+        out_host.copy_(dev["Conserved"], non_blocking=True)
+    f1.record(stream)
+    barrier()
+    e2e_ms = f0.elapsed_time(f1)
+    t = torch.tensor([e2e_ms], dtype=torch.float64, device=device)
+    if ws > 1:
+        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
+    e2e_value = 3.0 * ncell * e2e_steps * ws / (t.item() * 1e-3)
+
+    result = None
+    if rank == 0:
+        prof = kernel_profile(dev, gh, lib, runtime, dt)
+        fam = {}
+        for k, val in prof.items():
+            f = k.rsplit("_", 1)[0] if k.startswith(("euler", "diffusion")) else k
+            fam[f] = fam.get(f, 0.0) + val
+        dominant = max(prof, key=prof.get)
+        fdom = dominant.rsplit("_", 1)[0] if dominant.startswith(("euler", "diffusion")) else dominant
+        peak, peak_src = hbm_peak()
+        bytes_launch = KERNEL_BYTES.get(fdom, BYTES_PER_CELL_UPDATE_AIR) * ncell
+        achieved = bytes_launch / (prof[dominant] * 1e-3) / 1e9
+        fp64 = fp64_peak(lib)
+        result = {
+            "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": ws, "steps": args.steps,
+            "warmup": args.warmup, "ms_per_step": ms_max / args.steps, "higher_is_better": True,
+            "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
+            "config": {"workload": f"periodic {args.n}^3 box, 5-species air (AirMix), hybrid TENO/KG + "
+                                   f"diffusion + explicit chemistry, SSP-RK3",
+                       "grid": [args.n] * 3, "cells": ncell, "species": 5, "scheme": "Hybrid",
+                       "chemistry": "explicit", "rk_stages_per_step": 3, "dt": dt,
+                       "l2": "inputs larger than L2 (state ~%.1f GB)" % (ncell * 480 / 1e9),
+                       "parallelism": f"replicas x{ws}" if ws > 1 else "single GPU"},
+            "e2e": {"value": e2e_value, "unit": UNIT, "h2d_bytes_per_step": int(h2d),
+                    "d2h_bytes_per_step": int(d2h), "steps": e2e_steps},
+            "roofline": {"bound": "hbm", "kernel": dominant, "achieved": achieved, "peak": peak,
+                         "unit": "GB/s", "frac": achieved / peak, "peak_source": peak_src,
+                         "traffic": None, "bytes_per_launch": bytes_launch,
+                         "launch_ms": prof[dominant]},
+            "fp64": {"peak_tflops_probe": fp64, "note": "measured in this run by a DFMA-chain probe"},
+            "kernel_ms_per_stage": prof,
+            "gpu_launches": args.steps * (2 + 1 + 3 * 11),
+            "clocks": clk,
+        }
+        if args.cpu_baseline:
+            result["cpu_baseline"] = cpu_baseline(args.cpu_seconds)
+    if ws > 1:
+        torch.distributed.barrier()
+        torch.distributed.destroy_process_group()
+    return result
+
+
+def cpu_baseline(budget_s=20.0, n=48, impl_label="port"):
+    """The CPU oracle (all host threads) on a bounded sample of the same workload."""
+    import oracle
+    lib = oracle.ref_lib(abi.HTR_EOS_AIRMIX)
+    kind = "reference"
+    if lib is None:
+        lib = oracle.port_lib()
+        kind = "port"
+    threads = os.cpu_count() or 1
+    if kind == "port":
+        lib.htr_oracle_set_threads(threads)
+    fl = workloads.air_box(n, seed=1234)
+    m = workloads.make_mixture_struct(lib, abi.HTR_EOS_AIRMIX, fl.meta["mix"])
+    h = oracle.load_mixture(lib, abi.HTR_EOS_AIRMIX, m)
+    workloads.derive_state(lib, fl, h)
+    oracle.update_sensors(lib, fl, h, 1.0)
+    v = fl.view()
+    lib.htr_InitializeTemporaries(C.byref(v), fl.bounds(), h, None)
+    evals = 0
+    t0 = time.perf_counter()
+    while True:
+        oracle.update_derivatives(lib, fl, h, 1, 1e-9, "Hybrid", chemistry=True)
+        evals += 1
+        if time.perf_counter() - t0 > budget_s or evals >= 50:
+            break
+    el = time.perf_counter() - t0
+    return {"value": evals * fl.ncells / el, "unit": UNIT, "cores": threads, "kind": kind,
+            "sample": f"{evals} full RHS evaluations (chemistry, hybrid Euler Z/Y/X, diffusion Z/Y/X) "
+                      f"of a {n}^3 box of the same workload, {el:.1f} s"}
+
+
+def run_reference(args):
+    ws, rank, _ = dist_env()
+    if rank != 0:
+        return None
+    base = cpu_baseline(budget_s=max(5.0, args.cpu_seconds / max(1, args.steps + args.warmup)))
+    # K timed samples after W warm-up samples, each a bounded RHS sample
+    vals = []
+    for i in range(args.warmup + args.steps):
+        b = cpu_baseline(budget_s=max(2.0, args.cpu_seconds / max(1, args.steps + args.warmup)))
+        if i >= args.warmup:
+            vals.append(b["value"])
+    value = float(np.median(vals)) if vals else base["value"]
+    return {"impl": "reference", "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": ws,
+            "steps": args.steps, "warmup": args.warmup, "higher_is_better": True, "scaling": "weak",
+            "vs_baseline": None, "dtype": "f64", "data": "synthetic",
+            "config": {"workload": f"periodic {args.n}^3 box, 5-species air (AirMix), hybrid TENO/KG + "
+                                   f"diffusion + explicit chemistry, SSP-RK3", "grid": [args.n] * 3,
+                       "sample_grid": [48] * 3},
+            "cpu_baseline": {"value": value, "unit": UNIT, "cores": base["cores"], "kind": base["kind"],
+                             "sample": base["sample"]},
+            "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+
+
+def main():
+    p = argparse.ArgumentParser()
+    p.add_argument("--gpus", type=int, default=1)
+    p.add_argument("--steps", type=int, default=3)
+    p.add_argument("--warmup", type=int, default=3)
+    p.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
+    p.add_argument("--n", type=int, default=256)
+    p.add_argument("--cpu-seconds", type=float, default=20.0)
+    p.add_argument("--no-cpu-baseline", dest="cpu_baseline", action="store_false")
+    args = p.parse_args()
+    res = run_reference(args) if args.impl == "reference" else run_gpu(args)
+    if res is not None:
+        print(json.dumps(res), flush=True)
+
+
+if __name__ == "__main__":
+    main()

@@ -3,7 +3,7 @@ import ctypes as C
 
 import numpy as np
 
-from htr_gb300 import abi, workloads
+from htr_gb300 import abi, workloads  # noqa: F401  (re-exported for tests)
 
 import oracle
 
