@@ -141,49 +141,47 @@ def choose_dt(dev, gh, lib, runtime):
     return min(0.8 / out.item(), 0.5 * tau)
 
 
-def kernel_profile(dev, gh, lib, runtime, dt, reps=1):
-    """CUDA-event time of each kernel family over one RHS stage (untimed pass)."""
-    import torch
+STAGE_KERNELS = ["prepass", "kg_faces_z", "kg_faces_y", "kg_faces_x", "teno_faces",
+                 "diffusion_faces_z", "diffusion_faces_y", "diffusion_faces_x", "stage_update"]
+
+
+def kernel_profile(dev, gh, lib, runtime, dt, reps=3):
+    """CUDA-event time of each kernel of one fused RHS stage (median of reps
+    untimed stages, after the timed region), via htr_rk3_stage_profile."""
+    from htr_gb300 import runtime as rt
+    lib.htr_rk3_stage_profile.argtypes = [C.POINTER(abi.htr_fluid_view), abi.htr_rect3, abi.htr_rect3,
+                                          C.POINTER(rt.htr_step_params), C.c_void_p, C.c_void_p, C.c_size_t,
+                                          C.POINTER(C.c_float), C.c_void_p]
+    lib.htr_rk3_stage_profile.restype = C.c_int
     v = dev.view()
-    s = runtime.stream_handle()
     inner, fb = dev.interior(), dev.bounds()
-    rk = (C.c_double * 2)(1.0, 0.0)
-    calls = {
-        "ducros+shock": lambda: (lib.htr_UpdateDucrosSensor(C.byref(v), fb, fb, 1.0, s),
-                                 [getattr(lib, f"htr_UpdateShockSensor{d}")(C.byref(v), fb, fb, gh, s) for d in "XYZ"]),
-        "chemistry": lambda: lib.htr_AddChemistrySources(C.byref(v), inner, gh, s),
-        "euler_hybrid_z": lambda: lib.htr_UpdateUsingHybridEulerFluxZ(C.byref(v), inner, fb, rk, dt, gh, s),
-        "euler_hybrid_y": lambda: lib.htr_UpdateUsingHybridEulerFluxY(C.byref(v), inner, fb, rk, dt, gh, s),
-        "euler_hybrid_x": lambda: lib.htr_UpdateUsingHybridEulerFluxX(C.byref(v), inner, fb, rk, dt, gh, s),
-        "diffusion_z": lambda: lib.htr_UpdateUsingDiffusionFluxZ(C.byref(v), inner, fb, gh, s),
-        "diffusion_y": lambda: lib.htr_UpdateUsingDiffusionFluxY(C.byref(v), inner, fb, gh, s),
-        "diffusion_x": lambda: lib.htr_UpdateUsingDiffusionFluxX(C.byref(v), inner, fb, gh, s),
-        "properties": lambda: lib.htr_UpdatePropertiesFromPrimitive(C.byref(v), fb, gh, s),
-        "primitive": lambda: lib.htr_UpdatePrimitiveFromConserved(C.byref(v), inner, gh, s),
-    }
-    out = {}
-    stream = torch.cuda.current_stream()
-    for name, fn in calls.items():
-        fn()
-        stream.synchronize()
-        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
-        e0.record(stream)
-        for _ in range(reps):
-            fn()
-        e1.record(stream)
-        e1.synchronize()
-        out[name] = e0.elapsed_time(e1) / reps
-    return out
+    p = rt.htr_step_params(rt.SCHEMES["Hybrid"], 1.0, 0.0, dt, 1)
+    nb = lib.htr_rk3_workspace_bytes(inner, gh)
+    ws = rt._workspace.get(nb, dev.device)
+    runs = []
+    for _ in range(reps):
+        out = (C.c_float * len(STAGE_KERNELS))()
+        abi.check(lib, lib.htr_rk3_stage_profile(C.byref(v), inner, fb, C.byref(p), gh, C.c_void_p(ws), nb, out,
+                                                 runtime.stream_handle()), "stage profile")
+        runs.append(list(out))
+    med = np.median(np.array(runs), axis=0)
+    return {k: float(m) for k, m in zip(STAGE_KERNELS, med)}
 
 
-# compulsory bytes per cell of each kernel family (5-species air, fields read
-# once, written fields counted once; Conserved_t read-modify-write = 2 x 72)
+# Algorithmic bytes per cell of each fused-stage kernel (5-species air; each
+# value the kernel needs read once, each value it produces written once;
+# face buffers hold 9 doubles per face, about one face per cell and direction)
+NE, NS = 9, 5
 KERNEL_BYTES = {
-    "euler_hybrid": 8 * (9 + 9 + 1 + 5 + 3 + 1 + 1 + 1) + 4 + 1 + 2 * 72,
-    "diffusion": 8 * (9 + 1 + 5 + 1 + 1 + 1 + 5 + 3 + 1 + 3) + 3 * 4 + 2 * 72,
-    "properties": 8 * (1 + 1 + 5) + 8 * (5 + 1 + 1 + 1 + 5 + 1),
-    "primitive": 8 * (9 + 1) + 8 * (1 + 1 + 5 + 3),
-    "chemistry": 8 * (1 + 1 + 1 + 5) + 2 * 8 * 5,
+    # u, X, rhoE, p, rho, 3 metrics, 3 node types -> 9 gradients, MixW, H
+    "prepass": 8 * (3 + NS + 1 + 1 + 1 + 3) + 3 * 4 + 8 * 11,
+    # rho, p, H, Y, u, sensor, node type -> one face flux
+    "kg_faces": 8 * (3 + NS + 3) + 1 + 4 + 8 * NE,
+    # rhoYi, T, X, rho, mu, lam, Di, u, m_s, node type, 6 gradients, MixW -> face flux
+    "diffusion_faces": 8 * (NS + 1 + NS + 1 + 1 + 1 + NS + 3 + 1 + 6 + 1) + 4 + 8 * NE,
+    # 6 face fluxes/2 x 2 families, 6 metrics, Y, rho, p, T, Conserved_old, Conserved
+    # -> Conserved_t, Conserved, T, p, rho, mu, lam, SoS, X, u, Di, Y
+    "stage_update": 8 * (6 * NE + 6 + NS + 3 + 2 * NE) + 8 * (2 * NE + 6 + NS + 3 + NS + NS),
 }
 
 
@@ -267,15 +265,12 @@ def run_gpu(args):
     result = None
     if rank == 0:
         prof = kernel_profile(dev, gh, lib, runtime, dt)
-        fam = {}
-        for k, val in prof.items():
-            f = k.rsplit("_", 1)[0] if k.startswith(("euler", "diffusion")) else k
-            fam[f] = fam.get(f, 0.0) + val
         dominant = max(prof, key=prof.get)
-        fdom = dominant.rsplit("_", 1)[0] if dominant.startswith(("euler", "diffusion")) else dominant
+        fdom = dominant.rsplit("_", 1)[0] if dominant[-2:] in ("_x", "_y", "_z") else dominant
         peak, peak_src = hbm_peak()
-        bytes_launch = KERNEL_BYTES.get(fdom, BYTES_PER_CELL_UPDATE_AIR) * ncell
-        achieved = bytes_launch / (prof[dominant] * 1e-3) / 1e9
+        per_cell = KERNEL_BYTES.get(fdom)
+        bytes_launch = per_cell * ncell if per_cell is not None else None
+        achieved = bytes_launch / (prof[dominant] * 1e-3) / 1e9 if bytes_launch else None
         fp64 = fp64_peak(lib)
         result = {
             "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": ws, "steps": args.steps,
@@ -290,12 +285,14 @@ def run_gpu(args):
             "e2e": {"value": e2e_value, "unit": UNIT, "h2d_bytes_per_step": int(h2d),
                     "d2h_bytes_per_step": int(d2h), "steps": e2e_steps},
             "roofline": {"bound": "hbm", "kernel": dominant, "achieved": achieved, "peak": peak,
-                         "unit": "GB/s", "frac": achieved / peak, "peak_source": peak_src,
-                         "traffic": None, "bytes_per_launch": bytes_launch,
-                         "launch_ms": prof[dominant]},
+                         "unit": "GB/s", "frac": (achieved / peak) if achieved else None,
+                         "peak_source": peak_src, "traffic": None, "bytes_per_launch": bytes_launch,
+                         "bytes_per_cell": per_cell, "launch_ms": prof[dominant]},
             "fp64": {"peak_tflops_probe": fp64, "note": "measured in this run by a DFMA-chain probe"},
             "kernel_ms_per_stage": prof,
-            "gpu_launches": args.steps * (2 + 1 + 3 * 11),
+            # per step: Ducros + shock sensors + Conserved_old copy, then per stage
+            # prepass, 3 KG, 1 TENO, 3 diffusion, 1 update
+            "gpu_launches": args.steps * (3 + 3 * 9),
             "clocks": clk,
         }
         if args.cpu_baseline:

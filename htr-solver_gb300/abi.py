@@ -26,6 +26,15 @@ STATUS_NAMES = {
 }
 
 
+HTR_OK = 0
+HTR_ERR_ARGUMENT = 1
+HTR_ERR_LAYOUT = 2
+HTR_ERR_CUDA = 3
+HTR_ERR_ITERATION_CAP = 4
+HTR_ERR_UNSUPPORTED = 5
+HTR_ERR_NO_DEVICE = 6
+
+
 class HtrError(RuntimeError):
     pass
 

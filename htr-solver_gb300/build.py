@@ -16,7 +16,7 @@ OUT_DIR = os.path.join(HERE, "_build")
 LIB = os.path.join(OUT_DIR, "libhtr_gb300.so")
 
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
-EXACT_TUS = {"euler.cu", "sensor.cu"}
+EXACT_TUS = {"euler.cu", "sensor.cu", "stage_euler.cu"}
 
 
 def nvcc():

@@ -11,6 +11,7 @@
 
 #include "kernels.cuh"
 #include "mixture_host.h"
+#include "stage.cuh"
 
 struct htr_mixture_s {
   int eos;
@@ -134,9 +135,99 @@ int diffusion(const htr_fluid_view *v, htr_rect3 my, htr_rect3 fb, htr_mixture_t
 int neq_of(htr_mixture_t m) { return m->eos == HTR_EOS_AIRMIX ? 9 : 5; }
 int nspec_of(htr_mixture_t m) { return m->eos == HTR_EOS_AIRMIX ? 5 : 1; }
 
+
+int check_step_fields(const htr_fluid_view *v, htr_mixture_t m) {
+  HTR_REQ_D(*v, rho);
+  HTR_REQ_D(*v, mu);
+  HTR_REQ_D(*v, lam);
+  HTR_REQ_D(*v, Di);
+  HTR_REQ_D(*v, SoS);
+  HTR_REQ_D(*v, pressure);
+  HTR_REQ_D(*v, temperature);
+  HTR_REQ_D(*v, MassFracs);
+  HTR_REQ_D(*v, MolarFracs);
+  HTR_REQ_D(*v, velocity);
+  HTR_REQ_D(*v, Conserved);
+  HTR_REQ_D(*v, Conserved_old);
+  HTR_REQ_D(*v, Conserved_t);
+  for (int d = 0; d < 3; d++) {
+    if (int st = check_field(dirf(*v, d, 0), 4, "nType")) return st;
+    for (int k = 1; k <= 3; k++)
+      if (int st = check_field(dirf(*v, d, k), 8, "metric")) return st;
+    if (int st = check_field(dirf(*v, d, 4), 1, "shockSensor")) return st;
+  }
+  (void)m;
+  return HTR_OK;
+}
+
+}  // namespace
+
+extern "C" int htr_InitializeTemporaries(const htr_fluid_view *, htr_rect3, htr_mixture_t, htr_stream_t);
+extern "C" int htr_UpdateDucrosSensor(const htr_fluid_view *, htr_rect3, htr_rect3, double, htr_stream_t);
+extern "C" int htr_CalculateMaxSpectralRadius(const htr_fluid_view *, htr_rect3, htr_mixture_t, double *, htr_stream_t);
+
+namespace {
+
+// Step size, sensors (once per step) and Conserved_old (src/prometeo.rg:1342-1380).
+int step_prologue(const htr_fluid_view *v, htr_rect3 inner, htr_rect3 fb, const htr_step_params *p,
+                  htr_mixture_t m, double *dt_out, htr_stream_t s) {
+  if (p == nullptr) return fail(HTR_ERR_ARGUMENT, "null step parameters%s");
+  if (int st = check_common(v, m, inner)) return st;
+  if (p->scheme < HTR_SCHEME_HYBRID || p->scheme > HTR_SCHEME_SKEW) return fail(HTR_ERR_ARGUMENT, "unknown scheme%s");
+  const cudaStream_t cs = (cudaStream_t)s;
+  double dt = p->deltaTime;
+  if (p->cfl > 0.0) {
+    // the radius lands in Conserved_t[first cell][0], which the stage overwrites anyway
+    double *scratch = reinterpret_cast<double *>(static_cast<char *>(v->Conserved_t.base) +
+                                                 inner.lo[0] * v->Conserved_t.stride[0] +
+                                                 inner.lo[1] * v->Conserved_t.stride[1] +
+                                                 inner.lo[2] * v->Conserved_t.stride[2]);
+    if (int st = htr_CalculateMaxSpectralRadius(v, inner, m, scratch, s)) return st;
+    double r = 0.0;
+    if (int st = cuda_status(cudaMemcpyAsync(&r, scratch, sizeof(double), cudaMemcpyDeviceToHost, cs), "dt read")) return st;
+    if (int st = cuda_status(cudaStreamSynchronize(cs), "dt sync")) return st;
+    if (!(r > 0.0)) return fail(HTR_ERR_ARGUMENT, "non-positive spectral radius%s");
+    dt = p->cfl / r;
+  }
+  if (!(dt > 0.0)) return fail(HTR_ERR_ARGUMENT, "non-positive time step%s");
+  *dt_out = dt;
+  int st;
+  if (p->scheme == HTR_SCHEME_HYBRID) {
+    if ((st = htr_UpdateDucrosSensor(v, fb, fb, p->vorticityScale, s))) return st;
+    if ((st = check_field(v->shockSensorX, 1, "shockSensorX")) || (st = check_field(v->shockSensorY, 1, "shockSensorY")) ||
+        (st = check_field(v->shockSensorZ, 1, "shockSensorZ")))
+      return st;
+    if ((st = cuda_status(htr::launch_shock_sensor(*v, fb, fb, nspec_of(m), 7, cs), "shock sensors"))) return st;
+  }
+  return htr_InitializeTemporaries(v, fb, m, s);
+}
+
+// Three stages of the fused pipeline (one prepass, Euler KG + TENO faces,
+// diffusion faces and one per-cell update kernel per stage).
+int fused_step(const htr_fluid_view *v, htr_rect3 inner, htr_rect3 fb, const htr_step_params *p,
+               htr_mixture_t m, const htr::StageWorkspace &w, double *dt_used, int *status_dev, htr_stream_t s) {
+  double dt = 0.0;
+  if (int st = step_prologue(v, inner, fb, p, m, &dt, s)) return st;
+  if (dt_used) *dt_used = dt;
+  htr::StageParams sp;
+  sp.scheme = p->scheme == HTR_SCHEME_HYBRID ? 0 : (p->scheme == HTR_SCHEME_SKEW ? 1 : 2);
+  sp.kind = p->scheme == HTR_SCHEME_TENOA ? htr::kTENOA : (p->scheme == HTR_SCHEME_TENOLAD ? htr::kTENOLAD : htr::kTENO);
+  sp.chemistry = p->explicitChemistry ? 1 : 0;
+  sp.dt = dt;
+  for (int stage = 1; stage <= 3; stage++) {
+    sp.stage = stage;
+    if (int st = with_mix(m, [&](const auto &mix) {
+          return cuda_status(htr::launch_stage(*v, inner, fb, mix, w, sp, status_dev, (cudaStream_t)s), "stage");
+        }))
+      return st;
+  }
+  return HTR_OK;
+}
+
 }  // namespace
 
 extern "C" {
+
 
 const char *htr_last_error(void) { return g_err.c_str(); }
 
@@ -354,35 +445,12 @@ int htr_UpdateVars(const htr_fluid_view *v, htr_rect3 my, int stage, double dt, 
 // One SSP-RK3 time step of a periodic grid in the reference's driver order.
 int htr_rk3_step(const htr_fluid_view *v, htr_rect3 inner, htr_rect3 fb, const htr_step_params *p,
                  htr_mixture_t m, double *dt_used, int *status_dev, htr_stream_t s) {
-  if (p == nullptr) return fail(HTR_ERR_ARGUMENT, "null step parameters%s");
-  if (int st = check_common(v, m, inner)) return st;
-  const cudaStream_t cs = (cudaStream_t)s;
-  double dt = p->deltaTime;
-  if (p->cfl > 0.0) {
-    // the radius lands in Conserved_t[first cell][0], which the stage overwrites anyway
-    double *scratch = reinterpret_cast<double *>(static_cast<char *>(v->Conserved_t.base) +
-                                                 inner.lo[0] * v->Conserved_t.stride[0] +
-                                                 inner.lo[1] * v->Conserved_t.stride[1] +
-                                                 inner.lo[2] * v->Conserved_t.stride[2]);
-    if (int st = htr_CalculateMaxSpectralRadius(v, inner, m, scratch, s)) return st;
-    double r = 0.0;
-    if (int st = cuda_status(cudaMemcpyAsync(&r, scratch, sizeof(double), cudaMemcpyDeviceToHost, cs), "dt read")) return st;
-    if (int st = cuda_status(cudaStreamSynchronize(cs), "dt sync")) return st;
-    if (!(r > 0.0)) return fail(HTR_ERR_ARGUMENT, "non-positive spectral radius%s");
-    dt = p->cfl / r;
-  }
-  if (!(dt > 0.0)) return fail(HTR_ERR_ARGUMENT, "non-positive time step%s");
-  if (dt_used) *dt_used = dt;
   static const double RK[3][3] = {{1.0, 0.0, 1.0}, {3.0 / 4.0, 1.0 / 4.0, 1.0 / 4.0}, {1.0 / 3.0, 2.0 / 3.0, 2.0 / 3.0}};
+  const cudaStream_t cs = (cudaStream_t)s;
+  double dt = 0.0;
   int st;
-  if (p->scheme == HTR_SCHEME_HYBRID) {
-    if ((st = htr_UpdateDucrosSensor(v, fb, fb, p->vorticityScale, s))) return st;
-    if ((st = check_field(v->shockSensorX, 1, "shockSensorX")) || (st = check_field(v->shockSensorY, 1, "shockSensorY")) ||
-        (st = check_field(v->shockSensorZ, 1, "shockSensorZ")))
-      return st;
-    if ((st = cuda_status(htr::launch_shock_sensor(*v, fb, fb, nspec_of(m), 7, cs), "shock sensors"))) return st;
-  }
-  if ((st = htr_InitializeTemporaries(v, fb, m, s))) return st;
+  if ((st = step_prologue(v, inner, fb, p, m, &dt, s))) return st;
+  if (dt_used) *dt_used = dt;
   for (int stage = 1; stage <= 3; stage++) {
     const double rk[2] = {RK[stage - 1][0], RK[stage - 1][1]};
     const double sdt = dt * RK[stage - 1][2];
@@ -409,6 +477,64 @@ int htr_rk3_step(const htr_fluid_view *v, htr_rect3 inner, htr_rect3 fb, const h
     if ((st = htr_UpdatePropertiesFromPrimitive(v, fb, m, s))) return st;
   }
   return HTR_OK;
+}
+
+size_t htr_rk3_workspace_bytes(htr_rect3 interior, htr_mixture_t m) {
+  if (m == nullptr || !rect_ok(interior)) return 0;
+  return htr::stage_workspace_bytes(interior, neq_of(m));
+}
+
+int htr_rk3_step_ws(const htr_fluid_view *v, htr_rect3 inner, htr_rect3 fb, const htr_step_params *p,
+                    htr_mixture_t m, void *workspace, size_t workspace_bytes, double *dt_used,
+                    int *status_dev, htr_stream_t s) {
+  int st;
+  if ((st = check_common(v, m, inner))) return st;
+  if ((st = check_step_fields(v, m))) return st;
+  for (int i = 0; i < 3; i++)
+    if (inner.lo[i] != fb.lo[i] || inner.hi[i] != fb.hi[i])
+      return fail(HTR_ERR_UNSUPPORTED, "the fused step needs a grid periodic in every direction (interior == bounds)%s");
+  htr::StageWorkspace w;
+  if (!htr::stage_workspace_carve(workspace, workspace_bytes, inner, neq_of(m), w))
+    return fail(HTR_ERR_ARGUMENT, "workspace null or smaller than htr_rk3_workspace_bytes%s");
+  if (reinterpret_cast<uintptr_t>(workspace) % 256 != 0) return fail(HTR_ERR_LAYOUT, "workspace not 256-byte aligned%s");
+  return fused_step(v, inner, fb, p, m, w, dt_used, status_dev, s);
+}
+
+int htr_rk3_stage_profile(const htr_fluid_view *v, htr_rect3 inner, htr_rect3 fb, const htr_step_params *p,
+                          htr_mixture_t m, void *workspace, size_t workspace_bytes, float *ms_out,
+                          htr_stream_t s) {
+  int st;
+  if (p == nullptr || ms_out == nullptr) return fail(HTR_ERR_ARGUMENT, "null argument%s");
+  if ((st = check_common(v, m, inner))) return st;
+  if ((st = check_step_fields(v, m))) return st;
+  for (int i = 0; i < 3; i++)
+    if (inner.lo[i] != fb.lo[i] || inner.hi[i] != fb.hi[i])
+      return fail(HTR_ERR_UNSUPPORTED, "the fused step needs a grid periodic in every direction (interior == bounds)%s");
+  htr::StageWorkspace w;
+  if (!htr::stage_workspace_carve(workspace, workspace_bytes, inner, neq_of(m), w))
+    return fail(HTR_ERR_ARGUMENT, "workspace null or smaller than htr_rk3_workspace_bytes%s");
+  if (!(p->deltaTime > 0.0)) return fail(HTR_ERR_ARGUMENT, "non-positive time step%s");
+  htr::StageParams sp;
+  sp.scheme = p->scheme == HTR_SCHEME_HYBRID ? 0 : (p->scheme == HTR_SCHEME_SKEW ? 1 : 2);
+  sp.kind = p->scheme == HTR_SCHEME_TENOA ? htr::kTENOA : (p->scheme == HTR_SCHEME_TENOLAD ? htr::kTENOLAD : htr::kTENO);
+  sp.chemistry = p->explicitChemistry ? 1 : 0;
+  sp.dt = p->deltaTime;
+  sp.stage = 1;
+  cudaEvent_t ev[htr::kStageKernels + 1];
+  int made = 0;
+  cudaError_t e = cudaSuccess;
+  for (; made <= htr::kStageKernels && e == cudaSuccess; made++) e = cudaEventCreate(&ev[made]);
+  if (e == cudaSuccess)
+    st = with_mix(m, [&](const auto &mix) {
+      return cuda_status(htr::launch_stage(*v, inner, fb, mix, w, sp, nullptr, (cudaStream_t)s, ev), "stage");
+    });
+  else
+    st = cuda_status(e, "event create");
+  if (st == HTR_OK) st = cuda_status(cudaEventSynchronize(ev[htr::kStageKernels]), "stage sync");
+  for (int k = 0; st == HTR_OK && k < htr::kStageKernels; k++)
+    st = cuda_status(cudaEventElapsedTime(&ms_out[k], ev[k], ev[k + 1]), "event time");
+  for (int k = 0; k < made; k++) cudaEventDestroy(ev[k]);
+  return st;
 }
 
 }  // extern "C"

@@ -58,6 +58,9 @@ HTR_HD long long wrap_plus(long long p, long long lo, long long size, int off) {
   return (p + off - lo) % size + lo;
 }
 
+// TENO flavours: standard, adaptive-cutoff TENO-A, TENO-LAD
+enum TenoKind { kTENO = 0, kTENOA = 1, kTENOLAD = 2 };
+
 // min / max with the operand semantics of std::min / std::max.
 HTR_HD double smin(double a, double b) { return (b < a) ? b : a; }
 HTR_HD double smax(double a, double b) { return (a < b) ? b : a; }

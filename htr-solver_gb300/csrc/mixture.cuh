@@ -73,23 +73,29 @@ struct AirDev {
   static constexpr int NE = 9;
   static constexpr bool kReactive = true;
   // species
-  double W[NS], rOvW[NS], RoW[NS];  // RoW = RGAS/W (same value as rOvW, named per formula)
+  double W[NS], rOvW[NS];  // rOvW = RGAS/W
   float TS1[NS], TS2[NS];
   double cp[NS][3][7];   // NASA coefficients c0..c6 per range (0 high, 1 mid, 2 low)
   double hc[NS][3][8];   // enthalpy: -c0, c1, c7, c2, c3*0.50, c4/3, c5*0.25, c6/5
   double gc[NS][3][9];   // free enthalpy: -0.5*c0, c1, c2, c7, c8, c3, c4/3, c5/6, c6
-  // transport
+  // transport (T-independent factors of Species.inl:145-351, MultiComponent.inl:231-311)
   double muNum[NS];      // PI*W/Na*kb  (mu numerator is 5*sqrt(muNum*T))
   double muDen[NS];      // 16*PI*sigma^2
+  double muC[NS];        // 5*sqrt(muNum)/muDen:  mu_i = muC * sqrt(T) / omega_mu
   double kbOveps[NS];
+  double isqKbOveps[NS]; // 1/sqrt(kbOveps)
+  double iW[NS];         // 1/W
   int geom[NS];
   double sdDen[NS];      // 8*PI*sigma^2 (self diffusion denominator)
+  double sdC[NS];        // 3*sqrt(PI*kb*W/Na)/sdDen:  Dkk = sdC * sqrt(T) / omega_D
   double zrot298[NS];    // Z298*FZrot(298)
   double pi15;           // PI^1.5
   double wilkeA[NS][NS]; // (W_j/W_i)^0.25
   double wilkeB[NS][NS]; // sqrt(8*(1 + W_i/W_j))
+  double wilkeBi[NS][NS];// 1/wilkeB
   double difNum[NS][NS]; // 2*PI*kb^3*Na*invWij  (num = 3*sqrt(difNum*T^3))
   double difDen[NS][NS]; // 16*PI*sigma_ij^2
+  double difK[NS][NS];   // difDen/(3*sqrt(difNum)):  1/D_ij = difK * P * omega_D / T^1.5
   double difEps[NS][NS]; // kb/eps_ij
   // kinetics (2 standard + 3 third-body)
   AirReac reac[5];
@@ -238,37 +244,34 @@ struct AirDev {
   HTR_D double Mu(int i, double T) const {
     return 5 * sqrt(muNum[i] * T) / (muDen[i] * omega_mu(T * kbOveps[i]));
   }
-  // T in kelvin; mu = Mu(i, T); Tinv = 1/T
-  HTR_D double Lam(int i, double T, double Tinv, double mu) const {
-    const double PI = 3.1415926535898;
-    if (geom[i] == 0) return 15.0 / 4 * mu * kRGAS / W[i];
-    const double CvROvR = (geom[i] == 1) ? 1.0 : 1.5;
-    const double CvT = 1.5 * kRGAS;
-    const double CvR = CvROvR * kRGAS;
-    const double CvV = Cp(i, T, Tinv) * W[i] - ((geom[i] == 1) ? 3.5 : 4.0) * kRGAS;
-    const double Dkk = 3 * sqrt(PI * 1.38064852e-23 * T * W[i] / 6.02214086e23) /
-                       (sdDen[i] * omega_D(T * kbOveps[i]));
-    const double fV = Dkk / mu;
-    const double tmp = 1.0 / (kbOveps[i] * T);
-    const double st = sqrt(tmp);
-    const double fz = 1 + 0.5 * pi15 * st + (2 + 0.25 * PI * PI) * tmp + pi15 * (tmp * st);
-    const double Zrot = zrot298[i] / fz;
-    const double A = 2.5 - fV;
-    const double B = Zrot + 2 / PI * (5. / 3 * CvROvR + fV);
-    const double fT = 2.5 * (1. - 2 * CvR * A / (PI * CvT * B));
-    const double fR = fV * (1. + 2 * A / (PI * B));
-    return mu / W[i] * (fT * CvT + fR * CvR + fV * CvV);
+  // rational fits as numerator / denominator pairs (one division saved per use)
+  static HTR_D void omega_mu_nd(double T, double &n, double &d) {
+    n = 3.3530622607 + T * (2.53272006 + T * (2.9024238575 + T * 0.11186138893));
+    d = 0.8662326188 + T * (1.3913958626 + T * (3.158490576 + T * (0.18973411754 + T * 0.00018682962894)));
   }
-  // viscosity, conductivity, mixture-averaged diffusivities in one pass
+  static HTR_D void omega_D_nd(double T, double &n, double &d) {
+    n = 6.8728271691 + T * (9.4122316321 + T * (7.7442359037 + T * 0.23424661229));
+    d = 1.45337701568 + T * (5.2269794238 + T * (9.7108519575 + T * (0.46539437353 + T * 0.00041908394781)));
+  }
+  // Viscosity, conductivity and mixture-averaged diffusivities in one pass.
+  // Species values are regrouped around shared sqrt(T), 1/sqrt(T), 1/T and
+  // T^1.5 so that each needs about one division; the results differ from the
+  // reference's operation order only by rounding (<= 1e-15 relative).
   HTR_D void Transport(double Tn, double Pn, double MixW, const double *X, double &mu, double &lam,
                        double *D) const {
+    const double PI = 3.1415926535898;
     const double T = Tn * TRef;
     const double P = Pn * PRef;
     const double Tinv = 1.0 / T;
+    const double sT = sqrt(T);
+    const double isT = 1.0 / sT;
     double muk[NS], smu[NS], ismu[NS];
 #pragma unroll
     for (int i = 0; i < NS; i++) {
-      muk[i] = Mu(i, T);
+      double n, d;
+      omega_mu_nd(T * kbOveps[i], n, d);
+      const double om_inv = d / n;  // 1/omega_mu
+      muk[i] = muC[i] * sT * om_inv;
       smu[i] = sqrt(muk[i]);
       ismu[i] = 1.0 / smu[i];
     }
@@ -279,7 +282,7 @@ struct AirDev {
 #pragma unroll
       for (int j = 0; j < NS; j++) {
         double Phi = 1 + smu[i] * ismu[j] * wilkeA[i][j];
-        Phi *= Phi / wilkeB[i][j];
+        Phi *= Phi * wilkeBi[i][j];
         den += X[j] * Phi;
       }
       m += X[i] * muk[i] / den;
@@ -288,20 +291,41 @@ struct AirDev {
     double a = 0.0, b = 0.0;
 #pragma unroll
     for (int i = 0; i < NS; i++) {
-      const double l = Lam(i, T, Tinv, muk[i]);
+      double l;
+      if (geom[i] == 0) {
+        l = 15.0 / 4 * muk[i] * kRGAS * iW[i];
+      } else {
+        const double CvROvR = (geom[i] == 1) ? 1.0 : 1.5;
+        const double CvT = 1.5 * kRGAS;
+        const double CvR = CvROvR * kRGAS;
+        const double CvV = Cp(i, T, Tinv) * W[i] - ((geom[i] == 1) ? 3.5 : 4.0) * kRGAS;
+        double n, d;
+        omega_D_nd(T * kbOveps[i], n, d);
+        const double fV = sdC[i] * sT * d / (n * muk[i]);  // Dkk / mu
+        const double tmp = Tinv / kbOveps[i];
+        const double st = isT * isqKbOveps[i];               // sqrt(tmp)
+        const double fz = 1 + 0.5 * pi15 * st + (2 + 0.25 * PI * PI) * tmp + pi15 * (tmp * st);
+        const double A = 2.5 - fV;
+        const double B = zrot298[i] / fz + 2 / PI * (5. / 3 * CvROvR + fV);
+        const double iB = 1.0 / B;
+        const double fT = 2.5 * (1. - 2 * CvR * A * iB / (PI * CvT));
+        const double fR = fV * (1. + 2 * A * iB / PI);
+        l = muk[i] * iW[i] * (fT * CvT + fR * CvR + fV * CvV);
+      }
       a += X[i] * l;
       b += X[i] / l;
     }
     lam = 0.5 * (a + 1.0 / b) * ilamRef;
-    const double sT3 = sqrt(T * T * T);
+    const double PisT3 = P * Tinv * isT;  // P / T^1.5
 #pragma unroll
     for (int i = 0; i < NS; i++) D[i] = 0.0;
 #pragma unroll
     for (int i = 0; i < NS; i++)
 #pragma unroll
       for (int j = 0; j < i; j++) {
-        const double dij = 3 * sqrt(difNum[i][j]) * sT3 / (difDen[i][j] * P * omega_D(T * difEps[i][j]));
-        const double inv = 1.0 / dij;
+        double n, d;
+        omega_D_nd(T * difEps[i][j], n, d);
+        const double inv = difK[i][j] * PisT3 * n / d;  // 1 / D_ij
         D[i] += X[j] * inv;
         D[j] += X[i] * inv;
       }
@@ -333,13 +357,15 @@ struct AirDev {
 #pragma unroll
     for (int k = 0; k < 5; k++) {
       const AirReac &r = reac[k];
-      double Kf = r.A;
-      if (r.n != 0.0f) Kf *= exp(double(r.n) * logT);
-      if (fabsf(r.EovR) > 1e-5f) Kf *= exp(-double(r.EovR) * Tinv);
+      // A T^n exp(-E/RT) and its backward partner as single exponentials
+      double arg = 0.0;
+      if (r.n != 0.0f) arg += double(r.n) * logT;
+      if (fabsf(r.EovR) > 1e-5f) arg -= double(r.EovR) * Tinv;
+      const double Kf = r.A * exp(arg);
       double a = 1.0;
 #pragma unroll
       for (int i = 0; i < 2; i++)
-        if (i < r.nEd) a *= (r.nuE[i] == 1.0f) ? C[r.ed[i]] : pow(C[r.ed[i]], double(r.nuE[i]));
+        if (i < r.nEd) a *= (r.nuE[i] == 1.0f) ? C[r.ed[i]] : ((r.nuE[i] == 2.0f) ? C[r.ed[i]] * C[r.ed[i]] : pow(C[r.ed[i]], double(r.nuE[i])));
       double Kb = 0.0, b = 1.0;
       if (r.backward) {
         double sumNu = 0.0, sumNuG = 0.0;
@@ -356,10 +382,10 @@ struct AirDev {
             sumNuG += r.nuP[i] * G[r.pd[i]];
           }
         const double lnKc = -sumNuG - sumNu * (logT + lnRP);
-        Kb = Kf * exp(-lnKc);
+        Kb = r.A * exp(arg - lnKc);
 #pragma unroll
         for (int i = 0; i < 2; i++)
-          if (i < r.nPd) b *= (r.nuP[i] == 1.0f) ? C[r.pd[i]] : pow(C[r.pd[i]], double(r.nuP[i]));
+          if (i < r.nPd) b *= (r.nuP[i] == 1.0f) ? C[r.pd[i]] : ((r.nuP[i] == 2.0f) ? C[r.pd[i]] * C[r.pd[i]] : pow(C[r.pd[i]], double(r.nuP[i])));
       }
       double c = 1.0;
       if (r.nTb > 0) {

@@ -218,7 +218,6 @@ bool derive(const htr_airmix_t &s, AirDev &d) {
     if (!(sp.W > 0.0)) return false;
     d.W[i] = sp.W;
     d.rOvW[i] = kRGAS / sp.W;
-    d.RoW[i] = kRGAS / sp.W;
     d.TS1[i] = sp.cpCoeff.TSwitch1;
     d.TS2[i] = sp.cpCoeff.TSwitch2;
     const double *poly[3] = {sp.cpCoeff.cpH, sp.cpCoeff.cpM, sp.cpCoeff.cpL};
@@ -235,6 +234,10 @@ bool derive(const htr_airmix_t &s, AirDev &d) {
     d.kbOveps[i] = sp.DiffCoeff.kbOveps;
     d.geom[i] = sp.DiffCoeff.Geom;
     d.sdDen[i] = 8 * kPI * std::pow(sp.DiffCoeff.sigma, 2);
+    d.muC[i] = 5 * std::sqrt(d.muNum[i]) / d.muDen[i];
+    d.sdC[i] = 3 * std::sqrt(kPI * kKb * sp.W / kNa) / d.sdDen[i];
+    d.isqKbOveps[i] = 1.0 / std::sqrt(sp.DiffCoeff.kbOveps);
+    d.iW[i] = 1.0 / sp.W;
     const double tmp = 1.0 / (sp.DiffCoeff.kbOveps * 298);
     const double fz298 = 1 + 0.5 * std::pow(kPI, 1.5) * std::sqrt(tmp) + (2 + 0.25 * kPI * kPI) * tmp +
                          std::pow(kPI, 1.5) * std::pow(tmp, 1.5);
@@ -246,6 +249,7 @@ bool derive(const htr_airmix_t &s, AirDev &d) {
       const htr_ljdata_t &a = s.species[i].DiffCoeff, &b = s.species[j].DiffCoeff;
       d.wilkeA[i][j] = std::pow(s.species[j].W / s.species[i].W, 0.25);
       d.wilkeB[i][j] = std::sqrt(8 * (1 + s.species[i].W / s.species[j].W));
+      d.wilkeBi[i][j] = 1.0 / d.wilkeB[i][j];
       // Stockmayer collision parameters (Species.inl:152-181)
       double xi = 1.0;
       if ((a.mu * b.mu == 0.0) && (a.mu + b.mu != 0.0)) {
@@ -261,6 +265,7 @@ bool derive(const htr_airmix_t &s, AirDev &d) {
       const double invWij = (Wa + Wb) / (Wa * Wb);
       d.difNum[i][j] = 2 * kPI * std::pow(kKb, 3) * kNa * invWij;
       d.difDen[i][j] = 16 * kPI * sigmaij * sigmaij;
+      d.difK[i][j] = d.difDen[i][j] / (3 * std::sqrt(d.difNum[i][j]));
     }
   auto fill = [&](AirReac &r, const htr_arrhenius_t &A, bool bw, int ne, int np, int nt,
                   const htr_stoich_t *ed, const htr_stoich_t *pd, const htr_collider_t *tb) {

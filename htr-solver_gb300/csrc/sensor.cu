@@ -85,11 +85,12 @@ __global__ void shock_kernel(const SensorArgs a, int dirmask, long long n) {
       double Phi = ld(a.duc.at(q[0]));
 #pragma unroll
       for (int k = 1; k < 6; k++) Phi = smax(Phi, ld(a.duc.at(q[k])));
+      const double cut = sensor_cut(Phi);
       bool s = true;
 #pragma unroll
       for (int h = 0; h < NS; h++)
         s = s && teno_a_sensor(ld(&a.C.at(q[0])[h]), ld(&a.C.at(q[1])[h]), ld(&a.C.at(q[2])[h]),
-                               ld(&a.C.at(q[3])[h]), ld(&a.C.at(q[4])[h]), ld(&a.C.at(q[5])[h]), t, Phi);
+                               ld(&a.C.at(q[3])[h]), ld(&a.C.at(q[4])[h]), ld(&a.C.at(q[5])[h]), t, cut);
       const Fd<bool> &out = e == 0 ? a.sx : (e == 1 ? a.sy : a.sz);
       *out.at(p) = s;
     }

@@ -1,0 +1,93 @@
+// Fused RK-stage pipeline: face-flux buffers and their launchers.
+//
+// htr_rk3_step evaluates one stage as
+//   euler_kg_faces (Z, Y, X)  Kennedy-Gruber faces of every pencil tile from a
+//                             shared-memory window; faces the hybrid sensor
+//                             rejects go to one device-wide TENO queue
+//   euler_teno_faces          the queued (or, for TENO schemes, all) faces,
+//                             load-balanced over the whole GPU
+//   diffusion_faces (Z, Y, X) viscous / heat / species faces
+//   stage_update              per cell: chemistry + flux differences in the
+//                             reference's order, RK update, primitive (Newton)
+//                             and property refresh
+// Face fluxes live in a caller-provided workspace (structure of arrays,
+// component-major); each face is computed once.
+#pragma once
+
+#include "common.cuh"
+
+namespace htr {
+
+// Faces of direction D are indexed by the cell on their right, c in
+// [lo_D, hi_D + 1] x the other two extents of the interior.
+struct FaceGrid {
+  long long lo[3];
+  long long ext[3][3];  // ext[D][axis]
+  long long nf[3];      // faces per direction
+  HTR_HD long long index(int D, const long long *c) const {
+    return (c[0] - lo[0]) + ext[D][0] * ((c[1] - lo[1]) + ext[D][1] * (c[2] - lo[2]));
+  }
+};
+
+inline FaceGrid face_grid(const htr_rect3 &r) {
+  FaceGrid g;
+  long long n[3];
+  for (int i = 0; i < 3; i++) {
+    g.lo[i] = r.lo[i];
+    n[i] = r.hi[i] - r.lo[i] + 1;
+  }
+  for (int D = 0; D < 3; D++) {
+    for (int i = 0; i < 3; i++) g.ext[D][i] = n[i] + (i == D ? 1 : 0);
+    g.nf[D] = g.ext[D][0] * g.ext[D][1] * g.ext[D][2];
+  }
+  return g;
+}
+
+// A queued TENO face: direction and right cell.
+struct TenoEntry {
+  int D, c0, c1, c2;
+};
+
+struct StageWorkspace {
+  double *fe[3];    // Euler face fluxes, [NE][nf[D]]
+  double *fd[3];    // diffusion face fluxes, [NE][nf[D]]
+  TenoEntry *queue; // capacity nf[0]+nf[1]+nf[2]
+  unsigned *count;  // queue length
+  double *prep;     // per-cell prepass values, [kPrepVals][ncell]
+};
+
+// per-cell prepass values: velocity-gradient tensor (9), mixture molar
+// weight (1), total enthalpy H (1)
+constexpr int kPrepVals = 11;
+
+size_t stage_workspace_bytes(const htr_rect3 &interior, int neq);
+bool stage_workspace_carve(void *base, size_t bytes, const htr_rect3 &interior, int neq, StageWorkspace &w);
+
+struct StageParams {
+  int scheme;  // 0 hybrid, 1 skew, 2 TENO-only
+  int kind;    // TENO flavour for scheme 2
+  int chemistry;
+  int stage;   // 1..3
+  double dt;   // full step size
+};
+
+struct ConstPropDev;
+struct AirDev;
+
+// Euler faces of one stage (Z, Y, X KG tiles, then the TENO faces); H is the
+// dense per-cell total enthalpy written by the prepass.
+template <class Mix>
+cudaError_t launch_stage_euler(const htr_fluid_view &v, const htr_rect3 &interior, const htr_rect3 &fb,
+                               const Mix &mix, const StageWorkspace &w, const Fd<double> &H,
+                               const StageParams &p, double rk0, double rk1, double sdt, cudaStream_t s,
+                               cudaEvent_t *ev = nullptr);
+
+template <class Mix>
+cudaError_t launch_stage(const htr_fluid_view &v, const htr_rect3 &interior, const htr_rect3 &fb,
+                         const Mix &mix, const StageWorkspace &w, const StageParams &p, int *status,
+                         cudaStream_t s, cudaEvent_t *ev = nullptr);
+
+// Events of a profiled stage: start, then one after each kernel.
+enum StageKernel { kPrepass, kKgZ, kKgY, kKgX, kTeno, kDiffZ, kDiffY, kDiffX, kUpdate, kStageKernels };
+
+}  // namespace htr

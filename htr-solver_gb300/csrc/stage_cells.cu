@@ -1,0 +1,440 @@
+// Per-cell kernels and orchestration of the fused stage pipeline.
+//
+//   stage_prepass    per cell: velocity-gradient tensor (the reference's
+//                    getDeriv, bit-identical), mixture molar weight and total
+//                    enthalpy H, each computed once and shared by every face
+//                    that needs them
+//   diffusion_faces  viscous / heat / species face fluxes of one direction
+//   stage_update     per cell: chemistry sources, then the face-flux
+//                    differences in the reference's order (Euler Z, Y, X,
+//                    diffusion Z, Y, X), the SSP-RK3 update, the primitive
+//                    recovery (Newton) and the property refresh
+#include "kernels.cuh"
+#include "mixture.cuh"
+#include "stage.cuh"
+#include "stencil.cuh"
+
+namespace htr {
+
+static size_t align256(size_t b) { return (b + 255) & ~size_t(255); }
+
+size_t stage_workspace_bytes(const htr_rect3 &r, int neq) {
+  const FaceGrid g = face_grid(r);
+  const long long ncell = (r.hi[0] - r.lo[0] + 1) * (r.hi[1] - r.lo[1] + 1) * (r.hi[2] - r.lo[2] + 1);
+  size_t b = 0;
+  for (int D = 0; D < 3; D++) b += 2 * align256(sizeof(double) * neq * g.nf[D]);
+  b += align256(sizeof(TenoEntry) * (g.nf[0] + g.nf[1] + g.nf[2]));
+  b += align256(sizeof(unsigned));
+  b += align256(sizeof(double) * kPrepVals * ncell);
+  return b;
+}
+
+bool stage_workspace_carve(void *base, size_t bytes, const htr_rect3 &r, int neq, StageWorkspace &w) {
+  if (base == nullptr || bytes < stage_workspace_bytes(r, neq)) return false;
+  const FaceGrid g = face_grid(r);
+  char *p = static_cast<char *>(base);
+  for (int D = 0; D < 3; D++) {
+    w.fe[D] = reinterpret_cast<double *>(p);
+    p += align256(sizeof(double) * neq * g.nf[D]);
+    w.fd[D] = reinterpret_cast<double *>(p);
+    p += align256(sizeof(double) * neq * g.nf[D]);
+  }
+  w.queue = reinterpret_cast<TenoEntry *>(p);
+  p += align256(sizeof(TenoEntry) * (g.nf[0] + g.nf[1] + g.nf[2]));
+  w.count = reinterpret_cast<unsigned *>(p);
+  p += align256(sizeof(unsigned));
+  w.prep = reinterpret_cast<double *>(p);
+  return true;
+}
+
+struct Dense {  // dense per-cell indexing of the interior
+  long long lo[3], n[3];
+  HTR_HD long long idx(const long long *p) const {
+    return (p[0] - lo[0]) + n[0] * ((p[1] - lo[1]) + n[1] * (p[2] - lo[2]));
+  }
+  HTR_HD long long count() const { return n[0] * n[1] * n[2]; }
+  HTR_HD void point(long long i, long long *p) const {
+    p[0] = lo[0] + i % n[0];
+    p[1] = lo[1] + (i / n[0]) % n[1];
+    p[2] = lo[2] + i / (n[0] * n[1]);
+  }
+};
+static Dense dense(const htr_rect3 &r) {
+  Dense d;
+  for (int i = 0; i < 3; i++) {
+    d.lo[i] = r.lo[i];
+    d.n[i] = r.hi[i] - r.lo[i] + 1;
+  }
+  return d;
+}
+
+static dim3 grid_for(long long n, int threads) {
+  long long b = (n + threads - 1) / threads;
+  if (b > 152LL * 32) b = 152LL * 32;
+  return dim3((unsigned)(b > 0 ? b : 1));
+}
+
+// ---------------------------------------------------------------------------
+struct PrepArgs {
+  Fd<double> u, X, C, P, rho, m[3];
+  Fd<int> nt[3];
+  Box fb;
+  Dense dn;
+  double *prep;
+};
+
+template <class Mix>
+__global__ void stage_prepass(const PrepArgs A, const __grid_constant__ Mix mix) {
+  constexpr int NS = Mix::NS;
+  const long long n = A.dn.count();
+  for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n; i += (long long)gridDim.x * blockDim.x) {
+    long long p[3];
+    A.dn.point(i, p);
+#pragma unroll
+    for (int e = 0; e < 3; e++) {
+      const int t = ld(A.nt[e].at(p));
+      long long pm[3] = {p[0], p[1], p[2]}, pp[3] = {p[0], p[1], p[2]};
+      pm[e] = wrap_minus(p[e], A.fb.lo[e], A.fb.size(e), kNode[t].off[1]);
+      pp[e] = wrap_plus(p[e], A.fb.lo[e], A.fb.size(e), kNode[t].off[2]);
+      const double mm = ld(A.m[e].at(p));
+#pragma unroll
+      for (int c = 0; c < 3; c++)
+        A.prep[(e * 3 + c) * n + i] = deriv(t, ld(&A.u.at(pm)[c]), ld(&A.u.at(p)[c]), ld(&A.u.at(pp)[c]), mm);
+    }
+    double x[NS];
+#pragma unroll
+    for (int k = 0; k < NS; k++) x[k] = ld(&A.X.at(p)[k]);
+    A.prep[9 * n + i] = mix.MolarWeightFromXi(x);
+    A.prep[10 * n + i] = (ld(&A.C.at(p)[NS + 3]) + ld(A.P.at(p))) / ld(A.rho.at(p));
+  }
+}
+
+// ---------------------------------------------------------------------------
+struct DiffFaceArgs {
+  Fd<double> C, T, X, rho, mu, lam, Di, u, ms;
+  Fd<int> nt;
+  Box my, fb;
+  Dense dn;
+  const double *prep;
+  FaceGrid g;
+  double *fd;
+};
+
+template <class Mix, int D>
+__global__ void __launch_bounds__(128) diffusion_faces(const DiffFaceArgs A, const __grid_constant__ Mix mix) {
+  constexpr int NS = Mix::NS, NE = NS + 4, iU = NS, iE = NS + 3;
+  constexpr int T1 = (D == 0) ? 1 : 0, T2 = (D == 2) ? 1 : 2;
+  const long long nf = A.g.nf[D];
+  const long long ncell = A.dn.count();
+  for (long long f = blockIdx.x * (long long)blockDim.x + threadIdx.x; f < nf; f += (long long)gridDim.x * blockDim.x) {
+    long long c[3];
+    const long long e0 = A.g.ext[D][0], e1 = A.g.ext[D][1];
+    c[0] = A.g.lo[0] + f % e0;
+    c[1] = A.g.lo[1] + (f / e0) % e1;
+    c[2] = A.g.lo[2] + f / (e0 * e1);
+    long long p[3] = {c[0], c[1], c[2]};
+    if (c[D] == A.my.lo[D]) {
+      const int t0 = ld(A.nt.at(c));
+      p[D] = wrap_minus(c[D], A.fb.lo[D], A.fb.size(D), kNode[t0].off[1]);
+    } else {
+      p[D] = c[D] - 1;
+    }
+    long long q[3] = {p[0], p[1], p[2]};
+    q[D] = wrap_plus(p[D], A.fb.lo[D], A.fb.size(D), 1);
+    const int t = ld(A.nt.at(p));
+    const double m_s = ld(A.ms.at(p));
+    // interior-dense indices of p and q (periodic interior == bounds)
+    const long long ip = A.dn.idx(p), iq = A.dn.idx(q);
+    double g1p[3], g1q[3], g2p[3], g2q[3];
+#pragma unroll
+    for (int k = 0; k < 3; k++) {
+      g1p[k] = A.prep[(T1 * 3 + k) * ncell + ip];
+      g1q[k] = A.prep[(T1 * 3 + k) * ncell + iq];
+      g2p[k] = A.prep[(T2 * 3 + k) * ncell + ip];
+      g2q[k] = A.prep[(T2 * 3 + k) * ncell + iq];
+    }
+    const double rho_s = interp2(t, ld(A.rho.at(p)), ld(A.rho.at(q)));
+    const double iMixW_s = 1.0 / interp2(t, A.prep[9 * ncell + ip], A.prep[9 * ncell + iq]);
+    const double Tp = ld(A.T.at(p)), Tq = ld(A.T.at(q));
+    const double T_s = interp2(t, Tp, Tq);
+    double heat = interp2(t, ld(A.lam.at(p)), ld(A.lam.at(q))) * m_s * (Tp - Tq);
+    double F[NE];
+    if constexpr (NS > 1) {
+      double h[NS];
+      mix.SpeciesEnthalpies(h, T_s);
+      double ViCorr = 0.0;
+#pragma unroll
+      for (int i = 0; i < NS; i++) {
+        const double YiVi = interp2(t, ld(&A.Di.at(p)[i]), ld(&A.Di.at(q)[i])) * m_s *
+                            (ld(&A.X.at(p)[i]) - ld(&A.X.at(q)[i])) * mix.SpeciesMolarWeight(i) * iMixW_s;
+        F[i] = -rho_s * YiVi;
+        heat += rho_s * YiVi * h[i];
+        ViCorr += YiVi;
+      }
+#pragma unroll
+      for (int i = 0; i < NS; i++) {
+        const double cc = interp2(t, ld(&A.C.at(p)[i]), ld(&A.C.at(q)[i])) * ViCorr;
+        F[i] += cc;
+        heat -= cc * h[i];
+      }
+    } else {
+      const double h0 = mix.SpeciesEnthalpy(0, T_s);
+      const double YiVi = interp2(t, ld(&A.Di.at(p)[0]), ld(&A.Di.at(q)[0])) * m_s *
+                          (ld(&A.X.at(p)[0]) - ld(&A.X.at(q)[0])) * mix.SpeciesMolarWeight(0) * iMixW_s;
+      F[0] = -rho_s * YiVi;
+      heat += rho_s * YiVi * h0;
+      const double cc = interp2(t, ld(&A.C.at(p)[0]), ld(&A.C.at(q)[0])) * YiVi;
+      F[0] += cc;
+      heat -= cc * h0;
+    }
+    const double mu_s = interp2(t, ld(A.mu.at(p)), ld(A.mu.at(q)));
+    double up[3], uq[3];
+#pragma unroll
+    for (int i = 0; i < 3; i++) {
+      up[i] = ld(&A.u.at(p)[i]);
+      uq[i] = ld(&A.u.at(q)[i]);
+    }
+    const double dn_n = m_s * (uq[D] - up[D]);
+    const double dn_t1 = m_s * (uq[T1] - up[T1]);
+    const double dn_t2 = m_s * (uq[T2] - up[T2]);
+    const double d1_n = interp2(t, g1p[D], g1q[D]);
+    const double d1_t1 = interp2(t, g1p[T1], g1q[T1]);
+    const double d2_n = interp2(t, g2p[D], g2q[D]);
+    const double d2_t2 = interp2(t, g2p[T2], g2q[T2]);
+    double sigma[3];
+    sigma[D] = mu_s * (4 * dn_n - 2 * d1_t1 - 2 * d2_t2) / 3;
+    sigma[T1] = mu_s * (dn_t1 + d1_n);
+    sigma[T2] = mu_s * (dn_t2 + d2_n);
+    double uSigma = 0.0;
+#pragma unroll
+    for (int i = 0; i < 3; i++) {
+      F[iU + i] = sigma[i];
+      uSigma += interp2(t, up[i], uq[i]) * sigma[i];
+    }
+    F[iE] = (uSigma - heat);
+#pragma unroll
+    for (int i = 0; i < NE; i++) A.fd[i * nf + f] = F[i];
+  }
+}
+
+// ---------------------------------------------------------------------------
+struct UpdateArgs {
+  Fd<double> C, Cold, Ct, rho, P, T, X, Y, u, mu, lam, Di, SoS, me[3], md[3];
+  Dense dn;
+  FaceGrid g;
+  const double *fe[3], *fd[3];
+  double c1, c2, c3, dt;
+  int chemistry;
+  int *status;
+};
+
+template <class Mix>
+__global__ void __launch_bounds__(128) stage_update(const UpdateArgs A, const __grid_constant__ Mix mix) {
+  constexpr int NS = Mix::NS, NE = NS + 4;
+  const long long n = A.dn.count();
+  for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n; i += (long long)gridDim.x * blockDim.x) {
+    long long p[3];
+    A.dn.point(i, p);
+    double ct[NE];
+#pragma unroll
+    for (int k = 0; k < NE; k++) ct[k] = 0.0;
+    if (A.chemistry) {
+      double y[NS], w[NS];
+#pragma unroll
+      for (int k = 0; k < NS; k++) y[k] = ld(&A.Y.at(p)[k]);
+      mix.ProductionRates(w, ld(A.rho.at(p)), ld(A.P.at(p)), ld(A.T.at(p)), y);
+#pragma unroll
+      for (int k = 0; k < NS; k++) ct[k] = __dadd_rn(ct[k], w[k]);
+    }
+    // flux differences: Euler Z, Y, X then diffusion Z, Y, X
+#pragma unroll
+    for (int pass = 0; pass < 2; pass++) {
+#pragma unroll
+      for (int dd = 2; dd >= 0; dd--) {
+        long long c1[3] = {p[0], p[1], p[2]};
+        c1[dd] += 1;
+        const long long nf = A.g.nf[dd];
+        const long long fm = A.g.index(dd, p), fp = A.g.index(dd, c1);
+        const double *F = pass == 0 ? A.fe[dd] : A.fd[dd];
+        const double m = pass == 0 ? ld(A.me[dd].at(p)) : ld(A.md[dd].at(p));
+#pragma unroll
+        for (int k = 0; k < NE; k++) ct[k] = __dadd_rn(ct[k], __dmul_rn(m, __dsub_rn(F[k * nf + fp], F[k * nf + fm])));
+      }
+    }
+    // SSP-RK3 update (prometeo_rk.rg:88-112)
+    double *cons = A.C.at(p);
+    const double *old = A.Cold.at(p);
+    double *ctp = A.Ct.at(p);
+    double u_[NE];
+#pragma unroll
+    for (int k = 0; k < NE; k++) {
+      ctp[k] = ct[k];
+      u_[k] = __dadd_rn(__dadd_rn(__dmul_rn(A.c1, ld(&old[k])), __dmul_rn(A.c2, cons[k])),
+                        __dmul_rn(__dmul_rn(A.c3, ct[k]), A.dt));
+      cons[k] = u_[k];
+    }
+    // primitive recovery (variables.hpp:163-193)
+    double rhoYi[NS], Yi[NS], x[NS];
+#pragma unroll
+    for (int k = 0; k < NS; k++) rhoYi[k] = u_[k];
+    const double rho = mix.RhoFromRhoYi(rhoYi);
+    mix.YiFromRhoYi(Yi, rho, rhoYi);
+    mix.ClipYi(Yi);
+    const double MixW = mix.MolarWeightFromYi(Yi);
+    mix.MolarFractions(x, MixW, Yi);
+    const double rhoInv = 1.0 / rho;
+    double vel[3];
+#pragma unroll
+    for (int k = 0; k < 3; k++) vel[k] = u_[NS + k] * rhoInv;
+    const double e = u_[NS + 3] * rhoInv - 0.5 * mod2(vel);
+    int its = 0;
+    const double Tn = mix.TFromInternalEnergy(e, *A.T.at(p), Yi, &its);
+    if (its >= 1000 && A.status) atomicMax(A.status, (int)HTR_ERR_ITERATION_CAP);
+    const double Pn = mix.PFromRhoAndT(rho, MixW, Tn);
+    *A.T.at(p) = Tn;
+    *A.P.at(p) = Pn;
+    double *xp = A.X.at(p), *up = A.u.at(p);
+#pragma unroll
+    for (int k = 0; k < NS; k++) xp[k] = x[k];
+#pragma unroll
+    for (int k = 0; k < 3; k++) up[k] = vel[k];
+    // properties (variables.hpp:62-89)
+    const double MixWx = mix.MolarWeightFromXi(x);
+    *A.rho.at(p) = mix.Rho(Pn, Tn, MixWx);
+    double d[NS], y2[NS];
+    if constexpr (NS > 1) {
+      double m_, l_;
+      mix.Transport(Tn, Pn, MixWx, x, m_, l_, d);
+      *A.mu.at(p) = m_;
+      *A.lam.at(p) = l_;
+    } else {
+      *A.mu.at(p) = mix.Viscosity(Tn, x);
+      *A.lam.at(p) = mix.HeatConductivity(Tn, x);
+      mix.Diffusivity(d, Pn, Tn, MixWx, x);
+    }
+    mix.MassFractions(y2, MixWx, x);
+    const double gamma = mix.Gamma(Tn, MixWx, y2);
+    *A.SoS.at(p) = mix.SpeedOfSound(Tn, gamma, MixWx);
+    double *dp = A.Di.at(p), *yp = A.Y.at(p);
+#pragma unroll
+    for (int k = 0; k < NS; k++) {
+      dp[k] = d[k];
+      yp[k] = y2[k];
+    }
+  }
+}
+
+// ---------------------------------------------------------------------------
+template <class Mix>
+cudaError_t launch_stage(const htr_fluid_view &v, const htr_rect3 &my, const htr_rect3 &fb, const Mix &mix,
+                         const StageWorkspace &w, const StageParams &sp, int *status, cudaStream_t s,
+                         cudaEvent_t *ev) {
+  // ev (optional): ev[0] before the first kernel, ev[1 + k] after kernel k (StageKernel)
+  auto mark = [&](int i) { return ev ? cudaEventRecord(ev[i], s) : cudaSuccess; };
+  static const double RK[3][3] = {{1.0, 0.0, 1.0}, {3.0 / 4.0, 1.0 / 4.0, 1.0 / 4.0}, {1.0 / 3.0, 2.0 / 3.0, 2.0 / 3.0}};
+  const double c1 = RK[sp.stage - 1][0], c2 = RK[sp.stage - 1][1], c3 = RK[sp.stage - 1][2];
+  const Dense dn = dense(my);
+  const FaceGrid g = face_grid(my);
+  const long long n = dn.count();
+  double *prep = w.prep;
+  cudaError_t e;
+  if ((e = mark(0)) != cudaSuccess) return e;
+  {
+    PrepArgs A;
+    A.u = fd<double>(v.velocity);
+    A.X = fd<double>(v.MolarFracs);
+    A.C = fd<double>(v.Conserved);
+    A.P = fd<double>(v.pressure);
+    A.rho = fd<double>(v.rho);
+    A.m[0] = fd<double>(v.dcsi_d);
+    A.m[1] = fd<double>(v.deta_d);
+    A.m[2] = fd<double>(v.dzet_d);
+    A.nt[0] = fd<int>(v.nType_x);
+    A.nt[1] = fd<int>(v.nType_y);
+    A.nt[2] = fd<int>(v.nType_z);
+    A.fb = box(fb);
+    A.dn = dn;
+    A.prep = prep;
+    stage_prepass<Mix><<<grid_for(n, 256), 256, 0, s>>>(A, mix);
+    if ((e = cudaGetLastError()) != cudaSuccess || (e = mark(1 + kPrepass)) != cudaSuccess) return e;
+  }
+  Fd<double> H;
+  H.b = reinterpret_cast<char *>(prep + 10 * n);
+  H.s0 = sizeof(double);
+  H.s1 = sizeof(double) * dn.n[0];
+  H.s2 = sizeof(double) * dn.n[0] * dn.n[1];
+  H.b -= (dn.lo[0] * H.s0 + dn.lo[1] * H.s1 + dn.lo[2] * H.s2);
+  if ((e = launch_stage_euler(v, my, fb, mix, w, H, sp, c1, c2, sp.dt * c3, s, ev ? ev + 1 + kKgZ : nullptr)) !=
+      cudaSuccess)
+    return e;
+  const htr_field *ms[3] = {&v.dcsi_s, &v.deta_s, &v.dzet_s};
+  const htr_field *nt[3] = {&v.nType_x, &v.nType_y, &v.nType_z};
+  for (int D = 2; D >= 0; D--) {
+    DiffFaceArgs A;
+    A.C = fd<double>(v.Conserved);
+    A.T = fd<double>(v.temperature);
+    A.X = fd<double>(v.MolarFracs);
+    A.rho = fd<double>(v.rho);
+    A.mu = fd<double>(v.mu);
+    A.lam = fd<double>(v.lam);
+    A.Di = fd<double>(v.Di);
+    A.u = fd<double>(v.velocity);
+    A.ms = fd<double>(*ms[D]);
+    A.nt = fd<int>(*nt[D]);
+    A.my = box(my);
+    A.fb = box(fb);
+    A.dn = dn;
+    A.prep = prep;
+    A.g = g;
+    A.fd = w.fd[D];
+    const dim3 gr = grid_for(g.nf[D], 128);
+    if (D == 0) diffusion_faces<Mix, 0><<<gr, 128, 0, s>>>(A, mix);
+    else if (D == 1) diffusion_faces<Mix, 1><<<gr, 128, 0, s>>>(A, mix);
+    else diffusion_faces<Mix, 2><<<gr, 128, 0, s>>>(A, mix);
+    if ((e = cudaGetLastError()) != cudaSuccess || (e = mark(1 + kDiffZ + (2 - D))) != cudaSuccess) return e;
+  }
+  UpdateArgs U;
+  U.C = fd<double>(v.Conserved);
+  U.Cold = fd<double>(v.Conserved_old);
+  U.Ct = fd<double>(v.Conserved_t);
+  U.rho = fd<double>(v.rho);
+  U.P = fd<double>(v.pressure);
+  U.T = fd<double>(v.temperature);
+  U.X = fd<double>(v.MolarFracs);
+  U.Y = fd<double>(v.MassFracs);
+  U.u = fd<double>(v.velocity);
+  U.mu = fd<double>(v.mu);
+  U.lam = fd<double>(v.lam);
+  U.Di = fd<double>(v.Di);
+  U.SoS = fd<double>(v.SoS);
+  U.me[0] = fd<double>(v.dcsi_e);
+  U.me[1] = fd<double>(v.deta_e);
+  U.me[2] = fd<double>(v.dzet_e);
+  U.md[0] = fd<double>(v.dcsi_d);
+  U.md[1] = fd<double>(v.deta_d);
+  U.md[2] = fd<double>(v.dzet_d);
+  U.dn = dn;
+  U.g = g;
+  for (int D = 0; D < 3; D++) {
+    U.fe[D] = w.fe[D];
+    U.fd[D] = w.fd[D];
+  }
+  U.c1 = c1;
+  U.c2 = c2;
+  U.c3 = c3;
+  U.dt = sp.dt;
+  U.chemistry = sp.chemistry;
+  U.status = status;
+  stage_update<Mix><<<grid_for(n, 128), 128, 0, s>>>(U, mix);
+  if ((e = cudaGetLastError()) != cudaSuccess) return e;
+  return mark(1 + kUpdate);
+}
+
+template cudaError_t launch_stage<ConstPropDev>(const htr_fluid_view &, const htr_rect3 &, const htr_rect3 &,
+                                                const ConstPropDev &, const StageWorkspace &, const StageParams &,
+                                                int *, cudaStream_t, cudaEvent_t *);
+template cudaError_t launch_stage<AirDev>(const htr_fluid_view &, const htr_rect3 &, const htr_rect3 &,
+                                          const AirDev &, const StageWorkspace &, const StageParams &, int *,
+                                          cudaStream_t, cudaEvent_t *);
+
+}  // namespace htr

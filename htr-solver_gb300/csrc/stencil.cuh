@@ -181,7 +181,74 @@ HTR_D Smooth smoothness(double ym2, double ym1, double y, double yp1, double yp2
   return s;
 }
 
-enum TenoKind { kTENO = 0, kTENOA = 1, kTENOLAD = 2 };
+// ---------------------------------------------------------------------------
+// FP32 decision filter for TENO stencil selection.
+//
+// The selection flag of candidate k is  a_k * (1 / sum_j a_j) >= cut  with
+// a_k = (1 + tau6/(s_k + eps))^6.  The weights' values are never used, only
+// the flags.  This filter evaluates q_k = a_k / sum_j a_j in single precision
+// as (x_k/m)^6 / sum_j (x_j/m)^6 (m = max x_j, so nothing overflows) from the
+// exact double-precision smoothness measures.  Every single-precision
+// operation is correctly rounded (u = 2^-24), so |q_k - exact| <= 142 u q_k
+// (conversion, add and divide 5u on x_k, 11u on the ratio, 69u on its sixth
+// power, 72u on the sum, 142u on the quotient).  A flag is taken from the
+// filter only when q_k is further than 1e-4 * cut from cut (70x that bound);
+// otherwise the caller evaluates the exact double-precision expression.  The
+// flags therefore equal the reference's bit for bit while most faces skip
+// the 5 double divisions and 4 double sixth powers.
+// ---------------------------------------------------------------------------
+struct FastX {
+  float x[4];
+  bool ok;
+};
+HTR_D FastX fast_x(const Smooth &s, double eps) {
+  FastX f;
+  const double big = 1e30;
+  f.ok = (s.tau6 < big) && (s.s1 < big) && (s.s2 < big) && (s.s3 < big) && (s.s4 < big);
+  const float t = __double2float_rn(s.tau6);
+  const float e = __double2float_rn(eps);
+  f.x[0] = __fadd_rn(1.0f, __fdiv_rn(t, __fadd_rn(__double2float_rn(s.s1), e)));
+  f.x[1] = __fadd_rn(1.0f, __fdiv_rn(t, __fadd_rn(__double2float_rn(s.s2), e)));
+  f.x[2] = __fadd_rn(1.0f, __fdiv_rn(t, __fadd_rn(__double2float_rn(s.s3), e)));
+  f.x[3] = __fadd_rn(1.0f, __fdiv_rn(t, __fadd_rn(__double2float_rn(s.s4), e)));
+  return f;
+}
+HTR_D float pow6f(float r) {
+  const float r2 = __fmul_rn(r, r);
+  const float r3 = __fmul_rn(r2, r);
+  return __fmul_rn(r3, r3);
+}
+// Flags (bit k = stencil k kept) for the `used` candidates, or -1 when any
+// flag lies inside the safety margin.  Unused candidates get flag 0.
+HTR_D int fast_mask(const FastX &f, unsigned used, double cut) {
+  if (!f.ok || used == 0u) return -1;
+  float m = 0.0f;
+#pragma unroll
+  for (int k = 0; k < 4; k++)
+    if (used & (1u << k)) m = fmaxf(m, f.x[k]);
+  if (!(m >= 1.0f)) return -1;  // NaN guard
+  float q[4], S = 0.0f;
+#pragma unroll
+  for (int k = 0; k < 4; k++) {
+    q[k] = (used & (1u << k)) ? pow6f(__fdiv_rn(f.x[k], m)) : 0.0f;
+    S = __fadd_rn(S, q[k]);
+  }
+  const float c = (float)cut;
+  const float hi = c * 1.0001f, lo = c * 0.9999f;
+  int mask = 0;
+#pragma unroll
+  for (int k = 0; k < 4; k++) {
+    if (!(used & (1u << k))) continue;
+    const float qk = __fdiv_rn(q[k], S);
+    if (qk >= hi)
+      mask |= 1 << k;
+    else if (!(qk <= lo))
+      return -1;
+  }
+  return mask;
+}
+
+
 
 // One TENO reconstruction at face c+1/2 from y = (c-2 .. c+3); MINUS gives
 // the right-biased value (metric.inl:431-1038).  Returns the 4 selection
@@ -196,6 +263,40 @@ HTR_D double teno(double ym2, double ym1, double y, double yp1, double yp2, doub
   const double W3 = MINUS ? kNode[t].cm[3] : kNode[t].cp[3];
   const Smooth s = MINUS ? smoothness(yp3, yp2, yp1, y, ym1, ym2) : smoothness(ym2, ym1, y, yp1, yp2, yp3);
   const double eps = KIND == kTENO ? 1e-10 : (KIND == kTENOA ? 1e-8 : 1e-16);
+  int fmask = -1;
+  if (KIND != kTENOA || t != Std) {
+    // cheap exact-decision filter (see fast_mask); TENO-A on standard nodes
+    // adapts its cut-off to a Ren sensor and always takes the exact path
+    const unsigned used = (W0 < 1e-10 ? 0u : 1u) | (W1 < 1e-10 ? 0u : 2u) | (W2 < 1e-10 ? 0u : 4u) |
+                          (W3 < 1e-10 ? 0u : 8u);
+    const FastX fx = fast_x(s, eps);
+    double fcut = 1e-6;
+    bool cut_ok = true;
+    if (KIND == kTENOA) {
+      fcut = double(kP10[4]);
+    } else if (KIND == kTENOLAD) {
+      const float e = __double2float_rn(eps), tt = __double2float_rn(s.tau6);
+      float cm = __fdiv_rn(tt, __fadd_rn(__double2float_rn(s.s1), e));
+      cm = fmaxf(cm, __fdiv_rn(tt, __fadd_rn(__double2float_rn(s.s2), e)));
+      cm = fmaxf(cm, __fdiv_rn(tt, __fadd_rn(__double2float_rn(s.s3), e)));
+      cm = fmaxf(cm, __fdiv_rn(tt, __fadd_rn(__double2float_rn(s.s4), e)));
+      const float arg = 3.0f + 9.5f / (1.0f + cm * 0.1f);
+      const float fl = floorf(arg);
+      cut_ok = fx.ok && (arg - fl > 1e-3f) && (fl + 1.0f - arg > 1e-3f);
+      fcut = double(kP10[min(max(int(fl), 0), 13)]);
+    }
+    if (cut_ok) fmask = fast_mask(fx, used, fcut);
+  }
+  if (fmask >= 0) {
+    if (mask) *mask = unsigned(fmask);
+  }
+  int b1, b2, b3, b4;
+  if (fmask >= 0) {
+    b1 = fmask & 1;
+    b2 = (fmask >> 1) & 1;
+    b3 = (fmask >> 2) & 1;
+    b4 = (fmask >> 3) & 1;
+  } else {
   const double chi1 = s.tau6 / (s.s1 + eps);
   const double chi2 = s.tau6 / (s.s2 + eps);
   const double chi3 = s.tau6 / (s.s3 + eps);
@@ -240,11 +341,12 @@ HTR_D double teno(double ym2, double ym1, double y, double yp1, double yp2, doub
     if (W3 < 1e-10) a4 = 0.0;
   }
   const double a = 1.0 / (a1 + a2 + a3 + a4);
-  const int b1 = (a1 * a < cut) ? 0 : 1;
-  const int b2 = (a2 * a < cut) ? 0 : 1;
-  const int b3 = (a3 * a < cut) ? 0 : 1;
-  const int b4 = (a4 * a < cut) ? 0 : 1;
+  b1 = (a1 * a < cut) ? 0 : 1;
+  b2 = (a2 * a < cut) ? 0 : 1;
+  b3 = (a3 * a < cut) ? 0 : 1;
+  b4 = (a4 * a < cut) ? 0 : 1;
   if (mask) *mask = unsigned(b1) | (unsigned(b2) << 1) | (unsigned(b3) << 2) | (unsigned(b4) << 3);
+  }
   const double base = MINUS ? yp1 : y;
   double v[4];
   if (t == Std) {
@@ -279,9 +381,18 @@ HTR_D double teno(double ym2, double ym1, double y, double yp1, double yp2, doub
   return base + w1 * v[0] + w2 * v[1] + w3 * v[2] + w4 * v[3];
 }
 
-// Shock sensor of the hybrid scheme on a positive scalar (metric.inl:351-403).
+// Cut-off of the hybrid shock sensor from the Ducros value of the stencil
+// (metric.inl:395-397); shared by every species of a cell and direction.
+HTR_D double sensor_cut(double Phi) {
+  const double decay = pow12_exact(1 - Phi) * (1 + 12 * Phi);
+  const int power = min(max(int(floor(12.5 - 11.5 * (1 - decay))), 0), 13);
+  return double(kP10[power]);
+}
+
+// Shock sensor of the hybrid scheme on a positive scalar (metric.inl:351-403),
+// true = smooth; `cut` from sensor_cut.
 HTR_D bool teno_a_sensor(double ym2, double ym1, double y, double yp1, double yp2, double yp3,
-                         int t, double Phi) {
+                         int t, double cut) {
   const double rc = 0.2;
   const double Ren_eps = 0.9 * rc * 1e-6 / (1.0 - 0.9 * rc);
   const double Ren_irc = 1.0 / rc;
@@ -294,14 +405,15 @@ HTR_D bool teno_a_sensor(double ym2, double ym1, double y, double yp1, double yp
   }
   const Smooth s = smoothness(ym2, ym1, y, yp1, yp2, yp3);
   const double eps = 1e-8;
+  // strict comparison a_k*a > cut: the filter's flag "q >= cut(1+1e-4)"
+  // implies it, "q <= cut(1-1e-4)" refutes it
+  const int fm = fast_mask(fast_x(s, eps), 15u, cut);
+  if (fm >= 0) return fm == 15;
   const double a1 = pow6_exact(1 + s.tau6 / (s.s1 + eps));
   const double a2 = pow6_exact(1 + s.tau6 / (s.s2 + eps));
   const double a3 = pow6_exact(1 + s.tau6 / (s.s3 + eps));
   const double a4 = pow6_exact(1 + s.tau6 / (s.s4 + eps));
   const double a = 1.0 / (a1 + a2 + a3 + a4);
-  const double decay = pow12_exact(1 - Phi) * (1 + 12 * Phi);
-  const int power = min(max(int(floor(12.5 - 11.5 * (1 - decay))), 0), 13);
-  const double cut = double(kP10[power]);
   return ((a1 * a > cut) && (a2 * a > cut) && (a3 * a > cut) && (a4 * a > cut));
 }
 

@@ -37,6 +37,12 @@ def lib():
                                    C.POINTER(htr_step_params), C.c_void_p, C.POINTER(C.c_double),
                                    C.c_void_p, C.c_void_p]
         l.htr_rk3_step.restype = C.c_int
+        l.htr_rk3_workspace_bytes.argtypes = [abi.htr_rect3, C.c_void_p]
+        l.htr_rk3_workspace_bytes.restype = C.c_size_t
+        l.htr_rk3_step_ws.argtypes = [C.POINTER(abi.htr_fluid_view), abi.htr_rect3, abi.htr_rect3,
+                                      C.POINTER(htr_step_params), C.c_void_p, C.c_void_p, C.c_size_t,
+                                      C.POINTER(C.c_double), C.c_void_p, C.c_void_p]
+        l.htr_rk3_step_ws.restype = C.c_int
         for name, args in EXTRA_PROTOTYPES.items():
             fn = getattr(l, name, None)
             if fn is not None:
@@ -61,15 +67,51 @@ def load_mixture(eos, struct):
     return h
 
 
+class Workspace:
+    """Device workspace of the fused step (grown on demand, 256-byte aligned)."""
+
+    def __init__(self):
+        self.buf = None
+        self.nbytes = 0
+
+    def get(self, nbytes, device):
+        import torch
+        if self.buf is None or self.nbytes < nbytes or self.buf.device != torch.device(device):
+            self.buf = torch.empty(nbytes + 256, dtype=torch.uint8, device=device)
+            self.nbytes = nbytes
+        addr = self.buf.data_ptr()
+        return (addr + 255) // 256 * 256
+
+
+_workspace = Workspace()
+
+
+def workspace_bytes(fluid, mixh, interior=None):
+    inner = fluid.interior() if interior is None else interior
+    return lib().htr_rk3_workspace_bytes(inner, mixh)
+
+
 def rk3_step(fluid, mixh, scheme="Hybrid", vorticity_scale=1.0, cfl=0.0, dt=0.0,
-             chemistry=True, stream=None, interior=None, status_dev=None):
-    """One SSP-RK3 step of a periodic device grid; returns the dt used."""
+             chemistry=True, stream=None, interior=None, status_dev=None, fused=True,
+             workspace=None):
+    """One SSP-RK3 step of a device grid; returns the dt used.
+
+    fused=True runs htr_rk3_step_ws (fused stage pipeline, periodic grids) on
+    `workspace` (a Workspace, default: one cached per process); fused=False
+    runs htr_rk3_step, the composition of the per-task entry points."""
     l = lib()
     p = htr_step_params(SCHEMES[scheme], vorticity_scale, cfl, dt, 1 if chemistry else 0)
     v = fluid.view()
     used = C.c_double(0.0)
     inner = fluid.interior() if interior is None else interior
-    st = l.htr_rk3_step(C.byref(v), inner, fluid.bounds(), C.byref(p), mixh, C.byref(used),
-                        status_dev, stream_handle(stream))
-    abi.check(l, st, "htr_rk3_step")
+    if fused:
+        nb = l.htr_rk3_workspace_bytes(inner, mixh)
+        ws = (workspace or _workspace).get(nb, fluid.device)
+        st = l.htr_rk3_step_ws(C.byref(v), inner, fluid.bounds(), C.byref(p), mixh, C.c_void_p(ws), nb,
+                               C.byref(used), status_dev, stream_handle(stream))
+        abi.check(l, st, "htr_rk3_step_ws")
+    else:
+        st = l.htr_rk3_step(C.byref(v), inner, fluid.bounds(), C.byref(p), mixh, C.byref(used),
+                            status_dev, stream_handle(stream))
+        abi.check(l, st, "htr_rk3_step")
     return used.value

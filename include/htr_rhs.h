@@ -236,6 +236,32 @@ int htr_rk3_step(const htr_fluid_view *view, htr_rect3 interior, htr_rect3 fluid
                  const htr_step_params *params, htr_mixture_t mix, double *dt_used,
                  int *status_dev, htr_stream_t stream);
 
+/* --- fused time step on a caller-provided workspace -------------------------
+ * Not a reference task.  The same SSP-RK3 step as htr_rk3_step, computed by
+ * the fused stage pipeline: per stage one per-cell prepass (velocity
+ * gradients, molar weight, total enthalpy), Kennedy-Gruber faces of every
+ * direction from shared-memory tiles with the sensor-rejected faces queued
+ * for one load-balanced TENO kernel, diffusion faces, and one per-cell kernel
+ * (chemistry sources, flux differences in the reference's order, RK update,
+ * primitive recovery, property refresh).  Each face flux is computed once.
+ * Grids periodic in every direction only (interior == fluid_bounds);
+ * otherwise HTR_ERR_UNSUPPORTED.  `workspace` is device memory of at least
+ * htr_rk3_workspace_bytes(interior, mix) bytes, 256-byte aligned, owned by
+ * the caller; the call allocates nothing. */
+size_t htr_rk3_workspace_bytes(htr_rect3 interior, htr_mixture_t mix);
+int htr_rk3_step_ws(const htr_fluid_view *view, htr_rect3 interior, htr_rect3 fluid_bounds,
+                    const htr_step_params *params, htr_mixture_t mix, void *workspace,
+                    size_t workspace_bytes, double *dt_used, int *status_dev, htr_stream_t stream);
+
+/* Profiling aid, no counterpart in the reference: runs stage 1 of the fused
+ * pipeline once (deltaTime, no sensor update) with CUDA events between its
+ * kernels, waits for it, and writes the milliseconds of each kernel to
+ * ms_out[9]: prepass, KG faces Z, Y, X, TENO faces, diffusion faces Z, Y, X,
+ * per-cell update.  The state advances by that stage. */
+int htr_rk3_stage_profile(const htr_fluid_view *view, htr_rect3 interior, htr_rect3 fluid_bounds,
+                          const htr_step_params *params, htr_mixture_t mix, void *workspace,
+                          size_t workspace_bytes, float *ms_out, htr_stream_t stream);
+
 #ifdef __cplusplus
 }
 #endif

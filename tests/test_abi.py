@@ -13,7 +13,7 @@ from htr_gb300 import abi, runtime
 import oracle
 
 ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
-DECL = re.compile(r"^\s*(?:const\s+)?(?:int|char\s*\*|const char\s*\*|void)\s*\**\s*(htr_\w+)\s*\(", re.M)
+DECL = re.compile(r"^\s*(?:const\s+)?(?:int|size_t|char\s*\*|const char\s*\*|void)\s*\**\s*(htr_\w+)\s*\(", re.M)
 
 
 def declared():
@@ -33,7 +33,7 @@ def test_headers_declare_the_task_set():
         assert f"htr_UpdateUsingDiffusionFlux{d}" in names
         assert f"htr_UpdateShockSensor{d}" in names
     for n in ("htr_UpdateDucrosSensor", "htr_AddChemistrySources", "htr_UpdateChemistry",
-              "htr_load_mixture", "htr_rk3_step"):
+              "htr_load_mixture", "htr_rk3_step", "htr_rk3_step_ws", "htr_rk3_workspace_bytes"):
         assert n in names
 
 

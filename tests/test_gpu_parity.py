@@ -155,20 +155,54 @@ def test_spectral_radius(port, gpu, case):
     assert abs(out.item() - r_cpu.value) <= util.RHS_REL_TOL * r_cpu.value
 
 
-def test_rk3_step(port, gpu, case):
-    """One full SSP-RK3 step (fused device driver) against the oracle driver."""
+@pytest.mark.parametrize("fused", [False, True], ids=["tasks", "fused"])
+@pytest.mark.parametrize("scheme", ["Hybrid", "TENO", "TENOA", "TENOLAD", "SkewSymmetric"])
+def test_rk3_step(port, gpu, case, scheme, fused):
+    """One full SSP-RK3 step on the device against the oracle driver: the
+    composition of the task entry points (htr_rk3_step) and the fused stage
+    pipeline (htr_rk3_step_ws), every Euler scheme."""
     import torch
     kind, fl, h, gh = case
     host = fl.copy()
     dev = fl.to_device("cuda")
     chem = kind == "air"
     dt = 1e-9 if chem else 0.05
-    oracle.step(port, host, h, dt=dt, chemistry=chem)
-    runtime.rk3_step(dev, gh, dt=dt, chemistry=chem)
+    oracle.step(port, host, h, scheme=scheme, dt=dt, chemistry=chem)
+    status = torch.zeros(1, dtype=torch.int32, device="cuda")
+    runtime.rk3_step(dev, gh, scheme=scheme, dt=dt, chemistry=chem, fused=fused,
+                     status_dev=C.c_void_p(status.data_ptr()))
     torch.cuda.synchronize()
+    assert status.item() == 0
     out = dev.to_host()
-    for name in ("Conserved", "temperature", "pressure", "Conserved_t"):
+    for name in ("Conserved", "temperature", "pressure", "Conserved_t", "MolarFracs", "velocity",
+                 "rho", "mu", "lam", "Di", "SoS", "MassFracs"):
         err = util.rel_err(out[name], host[name])
-        assert err.max() <= util.RHS_REL_TOL, (name, err)
-    for d in "XYZ":
-        assert np.array_equal(out[f"shockSensor{d}"], host[f"shockSensor{d}"])
+        assert err.max() <= util.RHS_REL_TOL, (name, err.max())
+    if scheme == "Hybrid":
+        for d in "XYZ":
+            assert np.array_equal(out[f"shockSensor{d}"], host[f"shockSensor{d}"])
+
+
+def test_fused_step_rejects_bad_workspace(gpu, case):
+    """htr_rk3_step_ws checks the workspace size and the periodic-grid
+    requirement on the host, before any launch."""
+    kind, fl, h, gh = case
+    dev = fl.to_device("cuda")
+    v = dev.view()
+    p = runtime.htr_step_params(0, 1.0, 0.0, 1e-9, 0)
+    used = C.c_double(0.0)
+    nb = gpu.htr_rk3_workspace_bytes(dev.interior(), gh)
+    assert nb > 0
+    st = gpu.htr_rk3_step_ws(C.byref(v), dev.interior(), dev.bounds(), C.byref(p), gh, None, nb,
+                             C.byref(used), None, runtime.stream_handle())
+    assert st == abi.HTR_ERR_ARGUMENT
+    import torch
+    buf = torch.empty(nb, dtype=torch.uint8, device="cuda")
+    st = gpu.htr_rk3_step_ws(C.byref(v), dev.interior(), dev.bounds(), C.byref(p), gh,
+                             C.c_void_p(buf.data_ptr()), nb - 8, C.byref(used), None, runtime.stream_handle())
+    assert st == abi.HTR_ERR_ARGUMENT
+    inner = dev.interior()
+    inner.hi[0] -= 1
+    st = gpu.htr_rk3_step_ws(C.byref(v), inner, dev.bounds(), C.byref(p), gh,
+                             C.c_void_p(buf.data_ptr()), nb, C.byref(used), None, runtime.stream_handle())
+    assert st == abi.HTR_ERR_UNSUPPORTED
