@@ -51,6 +51,18 @@ def dist_env():
     return ws, rank, local
 
 
+def replica_throughput(ms_local, updates_local, device):
+    """Whole-job throughput of N independent replicas: the cell-updates of all
+    ranks over the slowest rank's time.  Returns (updates/s, max ms)."""
+    import torch
+    t = torch.tensor([ms_local], dtype=torch.float64, device=device)
+    u = torch.tensor([updates_local], dtype=torch.float64, device=device)
+    if torch.distributed.is_available() and torch.distributed.is_initialized():
+        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
+        torch.distributed.all_reduce(u, op=torch.distributed.ReduceOp.SUM)
+    return u.item() / (t.item() * 1e-3), t.item()
+
+
 def hbm_peak():
     try:
         with open(MEASURED_PEAKS) as f:
@@ -227,12 +239,7 @@ def run_gpu(args):
     barrier()
     clk = clocks.stop()
     ms = e0.elapsed_time(e1)
-    t = torch.tensor([ms], dtype=torch.float64, device=device)
-    if ws > 1:
-        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
-    ms_max = t.item()
-    total_updates = 3.0 * ncell * args.steps * ws
-    value = total_updates / (ms_max * 1e-3)
+    value, ms_max = replica_throughput(ms, 3.0 * ncell * args.steps, device)
 
     # end-to-end through the public API with pinned host buffers: per step the
     # time-dependent state goes host -> device, the step runs, Conserved comes back
@@ -257,10 +264,7 @@ def run_gpu(args):
     f1.record(stream)
     barrier()
     e2e_ms = f0.elapsed_time(f1)
-    t = torch.tensor([e2e_ms], dtype=torch.float64, device=device)
-    if ws > 1:
-        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
-    e2e_value = 3.0 * ncell * e2e_steps * ws / (t.item() * 1e-3)
+    e2e_value, _ = replica_throughput(e2e_ms, 3.0 * ncell * e2e_steps, device)
 
     result = None
     if rank == 0:
