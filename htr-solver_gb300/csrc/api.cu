@@ -6,6 +6,7 @@
 // caller's stream.  Nothing is allocated after htr_load_mixture.
 #include <cstdio>
 #include <cstring>
+#include <mutex>
 #include <new>
 #include <string>
 
@@ -135,6 +136,28 @@ int diffusion(const htr_fluid_view *v, htr_rect3 my, htr_rect3 fb, htr_mixture_t
 int neq_of(htr_mixture_t m) { return m->eos == HTR_EOS_AIRMIX ? 9 : 5; }
 int nspec_of(htr_mixture_t m) { return m->eos == HTR_EOS_AIRMIX ? 5 : 1; }
 
+
+// Fixed device scratch of htr_rk3_step_static: module-scope, allocated once
+// when the module loads; its address is looked up once per device.
+constexpr size_t kStaticScratchBytes = size_t(32) << 20;
+static __device__ __align__(256) unsigned char g_static_scratch[kStaticScratchBytes];
+std::mutex g_static_scratch_mu;
+constexpr int kMaxDevices = 64;
+void *g_static_scratch_ptr[kMaxDevices] = {};
+
+int static_scratch(void **out) {
+  int dev = 0;
+  if (int st = cuda_status(cudaGetDevice(&dev), "cudaGetDevice")) return st;
+  if (dev < 0 || dev >= kMaxDevices) return fail(HTR_ERR_UNSUPPORTED, "device ordinal out of range%s");
+  std::lock_guard<std::mutex> lock(g_static_scratch_mu);
+  if (g_static_scratch_ptr[dev] == nullptr) {
+    void *p = nullptr;
+    if (int st = cuda_status(cudaGetSymbolAddress(&p, g_static_scratch), "scratch symbol")) return st;
+    g_static_scratch_ptr[dev] = p;
+  }
+  *out = g_static_scratch_ptr[dev];
+  return HTR_OK;
+}
 
 int check_step_fields(const htr_fluid_view *v, htr_mixture_t m) {
   HTR_REQ_D(*v, rho);
@@ -499,6 +522,26 @@ int htr_rk3_step_ws(const htr_fluid_view *v, htr_rect3 inner, htr_rect3 fb, cons
   if (reinterpret_cast<uintptr_t>(workspace) % 256 != 0) return fail(HTR_ERR_LAYOUT, "workspace not 256-byte aligned%s");
   return fused_step(v, inner, fb, p, m, w, dt_used, status_dev, s);
 }
+
+int htr_rk3_step_static(const htr_fluid_view *v, htr_rect3 inner, htr_rect3 fb, const htr_step_params *p,
+                        htr_mixture_t m, double *dt_used, int *status_dev, htr_stream_t s) {
+  int st;
+  if ((st = check_common(v, m, inner))) return st;
+  if ((st = check_step_fields(v, m))) return st;
+  for (int i = 0; i < 3; i++)
+    if (inner.lo[i] != fb.lo[i] || inner.hi[i] != fb.hi[i])
+      return fail(HTR_ERR_UNSUPPORTED, "the fused step needs a grid periodic in every direction (interior == bounds)%s");
+  const size_t need = htr::stage_workspace_bytes(inner, neq_of(m));
+  if (need > kStaticScratchBytes) return fail(HTR_ERR_UNSUPPORTED, "grid too large for the static scratch%s");
+  void *scratch = nullptr;
+  if ((st = static_scratch(&scratch))) return st;
+  htr::StageWorkspace w;
+  if (!htr::stage_workspace_carve(scratch, kStaticScratchBytes, inner, neq_of(m), w))
+    return fail(HTR_ERR_ARGUMENT, "static scratch carve failed%s");
+  return fused_step(v, inner, fb, p, m, w, dt_used, status_dev, s);
+}
+
+size_t htr_rk3_static_scratch_bytes(void) { return kStaticScratchBytes; }
 
 int htr_rk3_stage_profile(const htr_fluid_view *v, htr_rect3 inner, htr_rect3 fb, const htr_step_params *p,
                           htr_mixture_t m, void *workspace, size_t workspace_bytes, float *ms_out,

@@ -43,6 +43,12 @@ def lib():
                                       C.POINTER(htr_step_params), C.c_void_p, C.c_void_p, C.c_size_t,
                                       C.POINTER(C.c_double), C.c_void_p, C.c_void_p]
         l.htr_rk3_step_ws.restype = C.c_int
+        l.htr_rk3_step_static.argtypes = [C.POINTER(abi.htr_fluid_view), abi.htr_rect3, abi.htr_rect3,
+                                          C.POINTER(htr_step_params), C.c_void_p, C.POINTER(C.c_double),
+                                          C.c_void_p, C.c_void_p]
+        l.htr_rk3_step_static.restype = C.c_int
+        l.htr_rk3_static_scratch_bytes.argtypes = []
+        l.htr_rk3_static_scratch_bytes.restype = C.c_size_t
         for name, args in EXTRA_PROTOTYPES.items():
             fn = getattr(l, name, None)
             if fn is not None:

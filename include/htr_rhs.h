@@ -253,6 +253,19 @@ int htr_rk3_step_ws(const htr_fluid_view *view, htr_rect3 interior, htr_rect3 fl
                     const htr_step_params *params, htr_mixture_t mix, void *workspace,
                     size_t workspace_bytes, double *dt_used, int *status_dev, htr_stream_t stream);
 
+/* No counterpart in the reference.  The fused step of htr_rk3_step_ws on a
+ * fixed scratch that the library owns: a module-scope device array of
+ * htr_rk3_static_scratch_bytes() bytes, reserved when the library's module
+ * loads, whose address is resolved once per device.  The call allocates no
+ * device or host memory.  Grids whose workspace (htr_rk3_workspace_bytes)
+ * exceeds the scratch are rejected with HTR_ERR_UNSUPPORTED before any
+ * launch.  Calls share the scratch of their device: run them on one stream
+ * (or serialise them), never concurrently. */
+int htr_rk3_step_static(const htr_fluid_view *view, htr_rect3 interior, htr_rect3 fluid_bounds,
+                        const htr_step_params *params, htr_mixture_t mix, double *dt_used,
+                        int *status_dev, htr_stream_t stream);
+size_t htr_rk3_static_scratch_bytes(void);
+
 /* Profiling aid, no counterpart in the reference: runs stage 1 of the fused
  * pipeline once (deltaTime, no sensor update) with CUDA events between its
  * kernels, waits for it, and writes the milliseconds of each kernel to
