@@ -65,6 +65,25 @@ enum TenoKind { kTENO = 0, kTENOA = 1, kTENOLAD = 2 };
 HTR_HD double smin(double a, double b) { return (b < a) ? b : a; }
 HTR_HD double smax(double a, double b) { return (a < b) ? b : a; }
 
+// Montgomery's simultaneous inversion: v[k] <- 1 / v[k] for N values with
+// one division and 3 (N - 1) multiplications.  The running products must
+// stay inside the double range (true for the bounded physical quantities it
+// is used on); the relative error is a few ulp.
+template <int N> HTR_D void batch_inverse(double *v) {
+  double pre[N];
+  pre[0] = v[0];
+#pragma unroll
+  for (int k = 1; k < N; k++) pre[k] = pre[k - 1] * v[k];
+  double inv = 1.0 / pre[N - 1];
+#pragma unroll
+  for (int k = N - 1; k > 0; k--) {
+    const double vk = v[k];
+    v[k] = inv * pre[k - 1];
+    inv *= vk;
+  }
+  v[0] = inv;
+}
+
 HTR_HD double mod2(const double *v) {
   double r = 0.0;
   r += v[0] * v[0];

@@ -60,12 +60,16 @@ struct ConstPropDev {
 
 // ---------------------------------------------------------------------------
 struct AirReac {  // one reaction, standard or third-body
-  double A;
-  float n, EovR;
+  // The reference stores n, E/R, the stoichiometric coefficients and the
+  // collider efficiencies as float; they are kept here promoted to double
+  // (exact), so the kernels convert nothing.
+  double A, n, EovR;
+  double nuE[2], nuP[2];
+  double effm1[5];  // efficiency - 1
   int nEd, nPd, nTb;
   int ed[2], pd[2], tb[5];
-  float nuE[2], nuP[2], eff[5];
   bool backward;
+  bool useN, useE;  // n != 0, |E/R| > 1e-5 (the reference's float tests)
 };
 
 struct AirDev {
@@ -74,7 +78,7 @@ struct AirDev {
   static constexpr bool kReactive = true;
   // species
   double W[NS], rOvW[NS];  // rOvW = RGAS/W
-  float TS1[NS], TS2[NS];
+  double TS1[NS], TS2[NS]; // NASA range switches (the reference's floats, promoted)
   double cp[NS][3][7];   // NASA coefficients c0..c6 per range (0 high, 1 mid, 2 low)
   double hc[NS][3][8];   // enthalpy: -c0, c1, c7, c2, c3*0.50, c4/3, c5*0.25, c6/5
   double gc[NS][3][9];   // free enthalpy: -0.5*c0, c1, c2, c7, c8, c3, c4/3, c5/6, c6
@@ -97,6 +101,14 @@ struct AirDev {
   double difDen[NS][NS]; // 16*PI*sigma_ij^2
   double difK[NS][NS];   // difDen/(3*sqrt(difNum)):  1/D_ij = difK * P * omega_D / T^1.5
   double difEps[NS][NS]; // kb/eps_ij
+  // factors of the fused property refresh (TransportFast)
+  double fvK[NS];        // sdC/muC:  Dkk/mu_k = fvK * omega_mu / omega_D
+  double iKbOveps[NS];   // 1/kbOveps
+  double lamMono[NS];    // 15/4 R/W (monatomic conductivity / viscosity)
+  double CvRot[NS];      // CvROvR R
+  double CvVoff[NS];     // 3.5 R (linear) or 4 R (non-linear)
+  double lamB0[NS];      // 2/PI * 5/3 * CvROvR
+  double lamK5[NS];      // 5 CvR / (PI CvT)
   // kinetics (2 standard + 3 third-body)
   AirReac reac[5];
   // reference scales
@@ -339,6 +351,187 @@ struct AirDev {
     }
   }
 
+  // --- fused per-cell refresh (the update kernel of the fused stage) -------
+  // The same physics as TFromInternalEnergy / Transport / HeatCapacity, with
+  // the arithmetic regrouped for fewer FP64 operations: species enthalpies
+  // and heat capacities share 1/T and the range lookup, the Newton loop keeps
+  // the species c_p of its final temperature for the property refresh, and
+  // transport replaces its ~50 divisions by a few batched inversions.
+  // Results differ from the reference's operation order by rounding only.
+
+  // Species enthalpies and heat capacities (mass units) at T (dimensional).
+  HTR_D void EnthalpyCp(double T, double Tinv, double logT, double *h, double *cpk) const {
+#pragma unroll
+    for (int i = 0; i < NS; i++) {
+      const int r = range(i, T);
+      const double *a = hc[i][r];
+      const double *c = cp[i][r];
+      h[i] = (a[0] * Tinv + a[1] * logT + a[2] +
+              T * (a[3] + T * (a[4] + T * (a[5] + T * (a[6] + a[7] * T))))) * rOvW[i];
+      cpk[i] = rOvW[i] * (c[0] * Tinv * Tinv + c[1] * Tinv + c[2] +
+                          T * (c[3] + T * (c[4] + T * (c[5] + T * c[6]))));
+    }
+  }
+  // Newton for T from e (MultiComponent.inl:188-209: same tolerance, cap and
+  // convergence test).  On return cpk holds the species c_p at the returned
+  // temperature, Td = T * TRef and Tinv = 1 / Td.
+  HTR_D double TFromInternalEnergyCp(double e0, double T, const double *Y, int *its, double *cpk,
+                                     double &Td, double &Tinv) const {
+    const int MAXITS = 1000;
+    const double TOL = 1e-8;
+    double dfdT = 1.0, h[NS];
+    int j = 0;
+    for (; j < MAXITS; j++) {
+      Td = T * TRef;
+      Tinv = 1.0 / Td;
+      EnthalpyCp(Td, Tinv, log(Td), h, cpk);
+      double e = 0.0;
+#pragma unroll
+      for (int i = 0; i < NS; i++) e += Y[i] * (h[i] - rOvW[i] * Td);
+      const double f = e0 - e * ieRef;
+      if (fabs(f / dfdT) < TOL) break;
+      double d = 0.0;
+#pragma unroll
+      for (int i = 0; i < NS; i++) d += Y[i] * (cpk[i] - rOvW[i]);
+      dfdT = d * iCpRef;
+      T += f / dfdT;
+    }
+    if (j == MAXITS) {
+      Td = T * TRef;
+      Tinv = 1.0 / Td;
+      EnthalpyCp(Td, Tinv, log(Td), h, cpk);
+    }
+    if (its) *its = j;
+    return T;
+  }
+  // Viscosity, conductivity, diffusivities (Species.inl:145-351,
+  // MultiComponent.inl:231-311) at T = Td with 1/T = Tinv, species c_p given.
+  HTR_D void TransportFast(double Td, double Tinv, double Pn, double MixW, const double *X,
+                           const double *cpk, double &mu, double &lam, double *D) const {
+    const double T = Td;
+    const double P = Pn * PRef;
+    const double isT = rsqrt(T);
+    const double sT = T * isT;
+    double nmu[NS], dmu[NS], nD[NS], dD[NS], inv1[2 * NS];
+#pragma unroll
+    for (int i = 0; i < NS; i++) {
+      omega_mu_nd(T * kbOveps[i], nmu[i], dmu[i]);
+      inv1[i] = nmu[i];
+      if (geom[i] != 0) {
+        omega_D_nd(T * kbOveps[i], nD[i], dD[i]);
+        inv1[NS + i] = nD[i] * dmu[i];
+      } else {
+        nD[i] = dD[i] = 1.0;
+        inv1[NS + i] = 1.0;
+      }
+    }
+    batch_inverse<2 * NS>(inv1);
+    double muk[NS], smu[NS], ismu[NS];
+#pragma unroll
+    for (int i = 0; i < NS; i++) {
+      muk[i] = muC[i] * sT * dmu[i] * inv1[i];
+      ismu[i] = rsqrt(muk[i]);
+      smu[i] = muk[i] * ismu[i];
+    }
+    // Wilke denominators (Phi_ii = 1 exactly) and the rotational relaxation
+    // denominators of the polyatomic species, inverted together
+    double inv2[2 * NS], fV[NS], fz[NS];
+#pragma unroll
+    for (int i = 0; i < NS; i++) {
+      double den = X[i];
+#pragma unroll
+      for (int j = 0; j < NS; j++) {
+        if (j == i) continue;
+        double Phi = 1 + smu[i] * ismu[j] * wilkeA[i][j];
+        Phi *= Phi * wilkeBi[i][j];
+        den += X[j] * Phi;
+      }
+      inv2[i] = den;
+      if (geom[i] != 0) {
+        fV[i] = fvK[i] * dD[i] * nmu[i] * inv1[NS + i];  // Dkk / mu_k
+        const double tmp = Tinv * iKbOveps[i];
+        const double st = isT * isqKbOveps[i];
+        fz[i] = 1 + 0.5 * pi15 * st + (2 + 0.25 * 3.1415926535898 * 3.1415926535898) * tmp + pi15 * (tmp * st);
+        inv2[NS + i] = zrot298[i] + fz[i] * (lamB0[i] + (2 / 3.1415926535898) * fV[i]);
+      } else {
+        fV[i] = fz[i] = 0.0;
+        inv2[NS + i] = 1.0;
+      }
+    }
+    batch_inverse<2 * NS>(inv2);
+    double m = 0.0;
+#pragma unroll
+    for (int i = 0; i < NS; i++) m += X[i] * muk[i] * inv2[i];
+    mu = m * imuRef;
+    // species conductivities; lam = (sum X l + 1 / sum X/l) / 2 with the
+    // second sum taken over a common denominator (one division)
+    double l[NS];
+#pragma unroll
+    for (int i = 0; i < NS; i++) {
+      if (geom[i] == 0) {
+        l[i] = muk[i] * lamMono[i];
+      } else {
+        const double CvT = 1.5 * kRGAS;
+        const double CvV = cpk[i] * W[i] - CvVoff[i];
+        const double AiB = (2.5 - fV[i]) * fz[i] * inv2[NS + i];  // A / B
+        const double fT = 2.5 - lamK5[i] * AiB;
+        const double fR = fV[i] * (1. + (2 / 3.1415926535898) * AiB);
+        l[i] = muk[i] * iW[i] * (fT * CvT + fR * CvRot[i] + fV[i] * CvV);
+      }
+    }
+    double a = 0.0, pre[NS], suf[NS];
+    pre[0] = 1.0;
+#pragma unroll
+    for (int i = 1; i < NS; i++) pre[i] = pre[i - 1] * l[i - 1];
+    suf[NS - 1] = 1.0;
+#pragma unroll
+    for (int i = NS - 2; i >= 0; i--) suf[i] = suf[i + 1] * l[i + 1];
+    double sx = 0.0;
+#pragma unroll
+    for (int i = 0; i < NS; i++) {
+      a += X[i] * l[i];
+      sx += X[i] * (pre[i] * suf[i]);
+    }
+    lam = 0.5 * (a + pre[NS - 1] * l[NS - 1] / sx) * ilamRef;
+    // binary diffusion coefficients, inverted together
+    const double PisT3 = P * Tinv * isT;  // P / T^1.5
+    double nb[NS * (NS - 1) / 2], db[NS * (NS - 1) / 2];
+    {
+      int k = 0;
+#pragma unroll
+      for (int i = 0; i < NS; i++)
+#pragma unroll
+        for (int j = 0; j < i; j++, k++) omega_D_nd(T * difEps[i][j], nb[k], db[k]);
+    }
+    batch_inverse<NS * (NS - 1) / 2>(db);
+    double Ds[NS];
+#pragma unroll
+    for (int i = 0; i < NS; i++) Ds[i] = 0.0;
+    {
+      int k = 0;
+#pragma unroll
+      for (int i = 0; i < NS; i++)
+#pragma unroll
+        for (int j = 0; j < i; j++, k++) {
+          const double inv = difK[i][j] * PisT3 * nb[k] * db[k];  // 1 / D_ij
+          Ds[i] += X[j] * inv;
+          Ds[j] += X[i] * inv;
+        }
+    }
+    double den[NS];
+#pragma unroll
+    for (int i = 0; i < NS; i++) den[i] = MixW * Ds[i];
+    batch_inverse<NS>(den);
+#pragma unroll
+    for (int i = 0; i < NS; i++) {
+      double num = 0.0;
+#pragma unroll
+      for (int j = 0; j < NS; j++)
+        if (j != i) num += X[j] * W[j];
+      D[i] = num * den[i] * iDiRef;
+    }
+  }
+
   // --- kinetics (Reaction.inl, MultiComponent.inl:370-415) ------------------
   HTR_D void ProductionRates(double *w, double rhon, double Pn, double Tn, const double *Y) const {
     const double T = Tn * TRef;
@@ -350,7 +543,7 @@ struct AirDev {
 #pragma unroll
     for (int i = 0; i < NS; i++) {
       w[i] = 0.0;
-      C[i] = Y[i] * rho / W[i];
+      C[i] = Y[i] * rho * iW[i];
       G[i] = FreeEnthalpy(i, T, Tinv, logT);
     }
     const double cM = P / (kRGAS * T);
@@ -359,13 +552,13 @@ struct AirDev {
       const AirReac &r = reac[k];
       // A T^n exp(-E/RT) and its backward partner as single exponentials
       double arg = 0.0;
-      if (r.n != 0.0f) arg += double(r.n) * logT;
-      if (fabsf(r.EovR) > 1e-5f) arg -= double(r.EovR) * Tinv;
+      if (r.useN) arg += r.n * logT;
+      if (r.useE) arg -= r.EovR * Tinv;
       const double Kf = r.A * exp(arg);
       double a = 1.0;
 #pragma unroll
       for (int i = 0; i < 2; i++)
-        if (i < r.nEd) a *= (r.nuE[i] == 1.0f) ? C[r.ed[i]] : ((r.nuE[i] == 2.0f) ? C[r.ed[i]] * C[r.ed[i]] : pow(C[r.ed[i]], double(r.nuE[i])));
+        if (i < r.nEd) a *= (r.nuE[i] == 1.0) ? C[r.ed[i]] : ((r.nuE[i] == 2.0) ? C[r.ed[i]] * C[r.ed[i]] : pow(C[r.ed[i]], r.nuE[i]));
       double Kb = 0.0, b = 1.0;
       if (r.backward) {
         double sumNu = 0.0, sumNuG = 0.0;
@@ -385,14 +578,14 @@ struct AirDev {
         Kb = r.A * exp(arg - lnKc);
 #pragma unroll
         for (int i = 0; i < 2; i++)
-          if (i < r.nPd) b *= (r.nuP[i] == 1.0f) ? C[r.pd[i]] : ((r.nuP[i] == 2.0f) ? C[r.pd[i]] * C[r.pd[i]] : pow(C[r.pd[i]], double(r.nuP[i])));
+          if (i < r.nPd) b *= (r.nuP[i] == 1.0) ? C[r.pd[i]] : ((r.nuP[i] == 2.0) ? C[r.pd[i]] * C[r.pd[i]] : pow(C[r.pd[i]], r.nuP[i]));
       }
       double c = 1.0;
       if (r.nTb > 0) {
         c = cM;
 #pragma unroll
         for (int i = 0; i < 5; i++)
-          if (i < r.nTb) c += C[r.tb[i]] * (r.eff[i] - 1.0);
+          if (i < r.nTb) c += C[r.tb[i]] * r.effm1[i];
       }
       const double R = c * (Kf * a - Kb * b);
 #pragma unroll

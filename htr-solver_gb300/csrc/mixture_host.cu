@@ -242,6 +242,14 @@ bool derive(const htr_airmix_t &s, AirDev &d) {
     const double fz298 = 1 + 0.5 * std::pow(kPI, 1.5) * std::sqrt(tmp) + (2 + 0.25 * kPI * kPI) * tmp +
                          std::pow(kPI, 1.5) * std::pow(tmp, 1.5);
     d.zrot298[i] = sp.DiffCoeff.Z298 * fz298;
+    d.fvK[i] = d.sdC[i] / d.muC[i];
+    d.iKbOveps[i] = 1.0 / sp.DiffCoeff.kbOveps;
+    d.lamMono[i] = 15.0 / 4 * kRGAS / sp.W;
+    const double CvROvR = (sp.DiffCoeff.Geom == 1) ? 1.0 : 1.5;
+    d.CvRot[i] = CvROvR * kRGAS;
+    d.CvVoff[i] = ((sp.DiffCoeff.Geom == 1) ? 3.5 : 4.0) * kRGAS;
+    d.lamB0[i] = 2 / kPI * (5. / 3 * CvROvR);
+    d.lamK5[i] = 5 * d.CvRot[i] / (kPI * 1.5 * kRGAS);
   }
   d.pi15 = std::pow(kPI, 1.5);
   for (int i = 0; i < 5; i++)
@@ -272,6 +280,8 @@ bool derive(const htr_airmix_t &s, AirDev &d) {
     r.A = A.A;
     r.n = A.n;
     r.EovR = A.EovR;
+    r.useN = A.n != 0.0f;
+    r.useE = std::fabs(A.EovR) > 1e-5f;
     r.backward = bw;
     r.nEd = ne;
     r.nPd = np;
@@ -284,7 +294,7 @@ bool derive(const htr_airmix_t &s, AirDev &d) {
     }
     for (int i = 0; i < 5; i++) {
       r.tb[i] = (i < nt) ? tb[i].ind : 0;
-      r.eff[i] = (i < nt) ? tb[i].eff : 1.0f;
+      r.effm1[i] = (i < nt) ? double(tb[i].eff) - 1.0 : 0.0;
     }
   };
   for (int k = 0; k < 2; k++) {

@@ -228,6 +228,96 @@ struct UpdateArgs {
   int *status;
 };
 
+// Primitive recovery and property refresh of one cell from its new
+// conserved vector u_.  Single-species gas: the task kernels' arithmetic.
+// Air: the fused thermo/transport of the mixture (one Newton pass that also
+// yields the species c_p of the final temperature, batched inversions).
+template <class Mix>
+HTR_D void refresh_cell(const UpdateArgs &A, const Mix &mix, const long long *p, const double *u_) {
+  constexpr int NS = Mix::NS;
+  double rhoYi[NS], Yi[NS], x[NS], vel[3], d[NS], y2[NS];
+#pragma unroll
+  for (int k = 0; k < NS; k++) rhoYi[k] = u_[k];
+  const double rho = mix.RhoFromRhoYi(rhoYi);
+  const double rhoInv = 1.0 / rho;
+  int its = 0;
+  if constexpr (NS > 1) {
+#pragma unroll
+    for (int k = 0; k < NS; k++) Yi[k] = rhoInv * rhoYi[k];
+    mix.ClipYi(Yi);
+    double s = 0.0;
+#pragma unroll
+    for (int k = 0; k < NS; k++) s += Yi[k] * mix.iW[k];
+    const double iMixW = 1.0 / s;  // MixW^-1 = sum Y/W
+#pragma unroll
+    for (int k = 0; k < NS; k++) x[k] = Yi[k] * iMixW * mix.iW[k];
+#pragma unroll
+    for (int k = 0; k < 3; k++) vel[k] = u_[NS + k] * rhoInv;
+    const double e = u_[NS + 3] * rhoInv - 0.5 * mod2(vel);
+    double cpk[NS], Td, Tinv;
+    const double Tn = mix.TFromInternalEnergyCp(e, *A.T.at(p), Yi, &its, cpk, Td, Tinv);
+    const double Pn = rho * Tn * iMixW / mix.iMixWRef;
+    *A.T.at(p) = Tn;
+    *A.P.at(p) = Pn;
+    double *xp = A.X.at(p), *up = A.u.at(p);
+#pragma unroll
+    for (int k = 0; k < NS; k++) xp[k] = x[k];
+#pragma unroll
+    for (int k = 0; k < 3; k++) up[k] = vel[k];
+    const double MixWx = mix.MolarWeightFromXi(x);
+    const double Wr = MixWx * mix.iMixWRef;
+    const double iTn = Tinv * mix.TRef;
+    *A.rho.at(p) = Pn * Wr * iTn;
+    double m_, l_;
+    mix.TransportFast(Td, Tinv, Pn, MixWx, x, cpk, m_, l_, d);
+    *A.mu.at(p) = m_;
+    *A.lam.at(p) = l_;
+    const double iMixWx = 1.0 / MixWx;
+    double c = 0.0;
+#pragma unroll
+    for (int k = 0; k < NS; k++) {
+      y2[k] = x[k] * mix.W[k] * iMixWx;
+      c += y2[k] * cpk[k];
+    }
+    c *= mix.iCpRef;
+    const double iWr = 1.0 / Wr;
+    const double gamma = c / (c - iWr);
+    *A.SoS.at(p) = sqrt(gamma * Tn * iWr);
+  } else {
+    mix.YiFromRhoYi(Yi, rho, rhoYi);
+    mix.ClipYi(Yi);
+    const double MixW = mix.MolarWeightFromYi(Yi);
+    mix.MolarFractions(x, MixW, Yi);
+#pragma unroll
+    for (int k = 0; k < 3; k++) vel[k] = u_[NS + k] * rhoInv;
+    const double e = u_[NS + 3] * rhoInv - 0.5 * mod2(vel);
+    const double Tn = mix.TFromInternalEnergy(e, *A.T.at(p), Yi, &its);
+    const double Pn = mix.PFromRhoAndT(rho, MixW, Tn);
+    *A.T.at(p) = Tn;
+    *A.P.at(p) = Pn;
+    double *xp = A.X.at(p), *up = A.u.at(p);
+#pragma unroll
+    for (int k = 0; k < NS; k++) xp[k] = x[k];
+#pragma unroll
+    for (int k = 0; k < 3; k++) up[k] = vel[k];
+    const double MixWx = mix.MolarWeightFromXi(x);
+    *A.rho.at(p) = mix.Rho(Pn, Tn, MixWx);
+    *A.mu.at(p) = mix.Viscosity(Tn, x);
+    *A.lam.at(p) = mix.HeatConductivity(Tn, x);
+    mix.Diffusivity(d, Pn, Tn, MixWx, x);
+    mix.MassFractions(y2, MixWx, x);
+    const double gamma = mix.Gamma(Tn, MixWx, y2);
+    *A.SoS.at(p) = mix.SpeedOfSound(Tn, gamma, MixWx);
+  }
+  if (its >= 1000 && A.status) atomicMax(A.status, (int)HTR_ERR_ITERATION_CAP);
+  double *dp = A.Di.at(p), *yp = A.Y.at(p);
+#pragma unroll
+  for (int k = 0; k < NS; k++) {
+    dp[k] = d[k];
+    yp[k] = y2[k];
+  }
+}
+
 template <class Mix>
 __global__ void __launch_bounds__(128) stage_update(const UpdateArgs A, const __grid_constant__ Mix mix) {
   constexpr int NS = Mix::NS, NE = NS + 4;
@@ -273,54 +363,9 @@ __global__ void __launch_bounds__(128) stage_update(const UpdateArgs A, const __
                         __dmul_rn(__dmul_rn(A.c3, ct[k]), A.dt));
       cons[k] = u_[k];
     }
-    // primitive recovery (variables.hpp:163-193)
-    double rhoYi[NS], Yi[NS], x[NS];
-#pragma unroll
-    for (int k = 0; k < NS; k++) rhoYi[k] = u_[k];
-    const double rho = mix.RhoFromRhoYi(rhoYi);
-    mix.YiFromRhoYi(Yi, rho, rhoYi);
-    mix.ClipYi(Yi);
-    const double MixW = mix.MolarWeightFromYi(Yi);
-    mix.MolarFractions(x, MixW, Yi);
-    const double rhoInv = 1.0 / rho;
-    double vel[3];
-#pragma unroll
-    for (int k = 0; k < 3; k++) vel[k] = u_[NS + k] * rhoInv;
-    const double e = u_[NS + 3] * rhoInv - 0.5 * mod2(vel);
-    int its = 0;
-    const double Tn = mix.TFromInternalEnergy(e, *A.T.at(p), Yi, &its);
-    if (its >= 1000 && A.status) atomicMax(A.status, (int)HTR_ERR_ITERATION_CAP);
-    const double Pn = mix.PFromRhoAndT(rho, MixW, Tn);
-    *A.T.at(p) = Tn;
-    *A.P.at(p) = Pn;
-    double *xp = A.X.at(p), *up = A.u.at(p);
-#pragma unroll
-    for (int k = 0; k < NS; k++) xp[k] = x[k];
-#pragma unroll
-    for (int k = 0; k < 3; k++) up[k] = vel[k];
-    // properties (variables.hpp:62-89)
-    const double MixWx = mix.MolarWeightFromXi(x);
-    *A.rho.at(p) = mix.Rho(Pn, Tn, MixWx);
-    double d[NS], y2[NS];
-    if constexpr (NS > 1) {
-      double m_, l_;
-      mix.Transport(Tn, Pn, MixWx, x, m_, l_, d);
-      *A.mu.at(p) = m_;
-      *A.lam.at(p) = l_;
-    } else {
-      *A.mu.at(p) = mix.Viscosity(Tn, x);
-      *A.lam.at(p) = mix.HeatConductivity(Tn, x);
-      mix.Diffusivity(d, Pn, Tn, MixWx, x);
-    }
-    mix.MassFractions(y2, MixWx, x);
-    const double gamma = mix.Gamma(Tn, MixWx, y2);
-    *A.SoS.at(p) = mix.SpeedOfSound(Tn, gamma, MixWx);
-    double *dp = A.Di.at(p), *yp = A.Y.at(p);
-#pragma unroll
-    for (int k = 0; k < NS; k++) {
-      dp[k] = d[k];
-      yp[k] = y2[k];
-    }
+    // primitive recovery (variables.hpp:163-193) and property refresh
+    // (variables.hpp:62-89) of the new state
+    refresh_cell(A, mix, p, u_);
   }
 }
 
