@@ -248,15 +248,15 @@ HTR_D void refresh_cell(const UpdateArgs &A, const Mix &mix, const long long *p,
     double s = 0.0;
 #pragma unroll
     for (int k = 0; k < NS; k++) s += Yi[k] * mix.iW[k];
-    const double iMixW = 1.0 / s;  // MixW^-1 = sum Y/W
+    const double MixW = 1.0 / s;  // 1 / MixW = sum Y/W
 #pragma unroll
-    for (int k = 0; k < NS; k++) x[k] = Yi[k] * iMixW * mix.iW[k];
+    for (int k = 0; k < NS; k++) x[k] = Yi[k] * MixW * mix.iW[k];
 #pragma unroll
     for (int k = 0; k < 3; k++) vel[k] = u_[NS + k] * rhoInv;
     const double e = u_[NS + 3] * rhoInv - 0.5 * mod2(vel);
     double cpk[NS], Td, Tinv;
     const double Tn = mix.TFromInternalEnergyCp(e, *A.T.at(p), Yi, &its, cpk, Td, Tinv);
-    const double Pn = rho * Tn * iMixW / mix.iMixWRef;
+    const double Pn = rho * Tn * s / mix.iMixWRef;
     *A.T.at(p) = Tn;
     *A.P.at(p) = Pn;
     double *xp = A.X.at(p), *up = A.u.at(p);
