@@ -98,7 +98,8 @@ def _run(lib, fl, mixh, device, chem_dt=None):
         if device:
             import torch
             st = torch.zeros(1, dtype=torch.int32, device=device)
-            util.call(lib, "htr_UpdateChemistry", C.byref(v), r, chem_dt, mixh, C.c_void_p(st.data_ptr()), s)
+            util.call(lib, "htr_UpdateChemistry", C.byref(v), r, chem_dt, mixh,
+                      C.cast(C.c_void_p(st.data_ptr()), C.POINTER(C.c_int)), s)
             torch.cuda.synchronize()
             assert st.item() == 0
             out["chem"] = f.to_host()
