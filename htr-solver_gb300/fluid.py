@@ -104,11 +104,14 @@ class Fluid:
         return out
 
     def copy(self):
-        if self.device is not None:
-            raise NotImplementedError
-        out = Fluid(self.shape, self.nspec, device=None, fields=list(self.arrays))
+        """Deep copy on the same device (host arrays or device tensors)."""
+        out = Fluid(self.shape, self.nspec, device=self.device, fields=list(self.arrays))
         for name, a in self.arrays.items():
-            out.arrays[name][...] = a
+            if self.device is None:
+                out.arrays[name][...] = a
+            else:
+                out.arrays[name].copy_(a)
+        out.meta = dict(self.meta)
         return out
 
     def interior(self, bnum=(0, 0, 0)):
