@@ -85,7 +85,7 @@ __global__ void shock_kernel(const SensorArgs a, int dirmask, long long n) {
       double Phi = ld(a.duc.at(q[0]));
 #pragma unroll
       for (int k = 1; k < 6; k++) Phi = smax(Phi, ld(a.duc.at(q[k])));
-      const double cut = sensor_cut(Phi);
+      const double cut = sensor_cut_fast(Phi);
       bool s = true;
 #pragma unroll
       for (int h = 0; h < NS; h++)

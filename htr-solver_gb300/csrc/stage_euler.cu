@@ -1,227 +1,16 @@
-// Euler faces of the fused stage pipeline (compiled with -fmad=false).
+// Characteristic TENO faces of the fused stage pipeline (compiled with
+// -fmad=false) and the Euler orchestration of one stage.
 //
-// euler_kg_faces<D>: a block owns L pencils x S faces along D.  The cell data
-// of its window (S + 6 points per pencil: the faces' 6-point stencils) is
-// staged in shared memory once — rho, p, H = (rhoE + p)/rho (precomputed per
-// cell by the stage prepass), mass fractions, velocity, sensor flag, node
-// type — and each face is reconstructed from it.  Kennedy-Gruber faces are
-// written to the face buffer directly; faces the hybrid sensor rejects are
-// appended to a device-wide queue (warp-aggregated atomics).
-//
-// euler_teno_faces: characteristic TENO faces of the queue (hybrid) or of
-// the whole grid (TENO schemes), spread over every SM with a grid-stride
-// loop, so the expensive reconstruction is load-balanced independently of
-// where the shocks are.
-//
+// euler_teno_faces: the faces the hybrid sensor rejected (queued by the
+// Kennedy-Gruber kernel, stage_kg.cu), or every face for the TENO schemes,
+// spread over every SM with a grid-stride loop, so the expensive
+// reconstruction is load-balanced independently of where the shocks are.
 // The arithmetic per face is the one of the per-direction task kernels
-// (euler_face.cuh), so the face fluxes are bit-identical to theirs.
-#include "euler_face.cuh"
-#include "stage.cuh"
+// (euler_face.cuh), so selection flags and face fluxes are bit-identical to
+// theirs.
+#include "stage_euler.cuh"
 
 namespace htr {
-
-struct StageEulerArgs {
-  EulerArgs e;       // fields, bounds, RK coefficients (e.my = interior)
-  Fd<double> H;      // per-cell total enthalpy from the prepass (dense)
-  FaceGrid g;
-  double *fe;        // face buffer of this direction, [NE][nf]
-  TenoEntry *queue;
-  unsigned *count;
-};
-
-template <int D> struct KGTile {
-  static constexpr int L = (D == 0) ? 1 : 32;
-  static constexpr int S = (D == 0) ? 128 : 8;
-  static constexpr int WS = S + 6;
-  static constexpr int THREADS = (D == 0) ? 128 : 256;
-};
-
-HTR_D long long wrap_in(long long v, long long lo, long long size) {
-  return ((v - lo) % size + size) % size + lo;
-}
-
-template <class Mix, int D, bool HYBRID>
-__global__ void __launch_bounds__(KGTile<D>::THREADS) euler_kg_faces(const StageEulerArgs A, const __grid_constant__ Mix mix) {
-  constexpr int NS = Mix::NS, NE = NS + 4, iU = NS, iE = NS + 3;
-  constexpr int L = KGTile<D>::L, S = KGTile<D>::S, WS = KGTile<D>::WS;
-  extern __shared__ double win[];  // [NV][L*WS]
-  __shared__ unsigned char sflag[L * WS];
-  __shared__ signed char stype[L * WS];
-  const EulerArgs &a = A.e;
-  (void)iE;
-
-  long long o[3];
-  if (D == 0) {
-    o[0] = a.my.lo[0] + (long long)blockIdx.x * S;
-    o[1] = a.my.lo[1] + blockIdx.y;
-    o[2] = a.my.lo[2] + blockIdx.z;
-  } else if (D == 1) {
-    o[0] = a.my.lo[0] + (long long)blockIdx.x * L;
-    o[1] = a.my.lo[1] + (long long)blockIdx.y * S;
-    o[2] = a.my.lo[2] + blockIdx.z;
-  } else {
-    o[0] = a.my.lo[0] + (long long)blockIdx.x * L;
-    o[1] = a.my.lo[1] + blockIdx.y;
-    o[2] = a.my.lo[2] + (long long)blockIdx.z * S;
-  }
-  const int nlines = (D == 0) ? 1 : (int)min((long long)L, a.my.hi[0] - o[0] + 1);
-  const long long ncell = min((long long)S, a.my.hi[D] - o[D] + 1);
-  // faces of this tile: right cells o..o+ncell-1, plus hi+1 on the last tile
-  const int nfl = (int)ncell + ((o[D] + ncell - 1 == a.my.hi[D]) ? 1 : 0);
-  const long long base_d = o[D] - 3;
-
-  // --- stage the window ----------------------------------------------------
-  const long long fbsz = a.fb.size(D);
-  for (int idx = threadIdx.x; idx < L * WS; idx += blockDim.x) {
-    const int l = idx % L, w = idx / L;
-    if (l >= nlines) continue;
-    long long p[3] = {o[0], o[1], o[2]};
-    if (D != 0) p[0] += l;
-    p[D] = wrap_in(base_d + w, a.fb.lo[D], fbsz);
-    const int k = w * L + l;
-    win[0 * L * WS + k] = ld(a.rho.at(p));
-    win[1 * L * WS + k] = ld(a.P.at(p));
-    win[2 * L * WS + k] = ld(A.H.at(p));
-#pragma unroll
-    for (int i = 0; i < NS; i++) win[(3 + i) * L * WS + k] = ld(&a.Y.at(p)[i]);
-#pragma unroll
-    for (int i = 0; i < 3; i++) win[(3 + NS + i) * L * WS + k] = ld(&a.u.at(p)[i]);
-    sflag[k] = HYBRID ? (unsigned char)ld(a.sen.at(p)) : 1;
-    stype[k] = (signed char)ld(a.nt.at(p));
-  }
-  __syncthreads();
-
-  const long long nf = A.g.nf[D];
-  const int lane = threadIdx.x & 31;
-  const int nface = nlines * nfl;
-  const int nround = (nface + blockDim.x - 1) / blockDim.x;
-  for (int r = 0; r < nround; r++) {
-    const int f = r * blockDim.x + threadIdx.x;
-    bool active = f < nface;
-    bool teno = false;
-    long long c[3] = {o[0], o[1], o[2]};
-    if (active) {
-      const int l = (D == 0) ? 0 : f % nlines;
-      const int j = (D == 0) ? f : f / nlines;
-      if (D != 0) c[0] += l;
-      c[D] += j;
-      // left point p and right point q of the face, as window indices
-      int wp, wq, t;
-      if (c[D] == a.my.lo[D]) {
-        const int w0 = (int)(c[D] - base_d);
-        wp = w0 + kNode[stype[w0 * L + l]].off[1];
-        wq = w0;
-        t = stype[wp * L + l];
-      } else {
-        wp = (int)(c[D] - 1 - base_d);
-        t = stype[wp * L + l];
-        wq = wp + kNode[t].off[2];
-      }
-      const int wm = wp + kNode[t].off[1];
-      const bool smooth = !HYBRID || (sflag[wm * L + l] && sflag[wp * L + l] && sflag[wq * L + l]);
-      if (smooth) {
-        double F[NE];
-        const long long fi = A.g.index(D, c);
-        auto V = [&](int q, int w) { return win[q * L * WS + w * L + l]; };
-        if (t == L_S || t == Rm1_S) {
-          // staggered boundary node: the flux is the physical flux at the face node
-          const int wn = (t == L_S) ? wp : wp + kNode[t].off[2];
-          long long pn[3] = {c[0], c[1], c[2]};
-          pn[D] = wrap_in(base_d + wn, a.fb.lo[D], fbsz);
-          const double un = V(3 + NS + D, wn), pq = V(1, wn);
-          const double *Cq = a.C.at(pn);
-#pragma unroll
-          for (int i = 0; i < NE; i++) F[i] = -(ld(&Cq[i]) * un);
-          F[iU + D] -= pq;
-          F[NS + 3] -= pq * un;
-        } else {
-          int wk[6];
-          wk[0] = wp + kNode[t].off[0];
-          wk[1] = wm;
-          wk[2] = wp;
-          wk[3] = wp + kNode[t].off[2];
-          wk[4] = wp + kNode[t].off[3];
-          wk[5] = wp + kNode[t].off[4];
-          double r_[6], v_[6], pr[6], h[6];
-#pragma unroll
-          for (int k = 0; k < 6; k++) {
-            r_[k] = V(0, wk[k]);
-            pr[k] = V(1, wk[k]);
-            h[k] = V(2, wk[k]);
-            v_[k] = -V(3 + NS + D, wk[k]);
-          }
-          const int order = kNode[t].kgOrder;
-          const double kgc[3] = {kNode[t].kg[0], kNode[t].kg[1], kNode[t].kg[2]};
-          double rv[3][3];
-#pragma unroll
-          for (int l2 = 0; l2 < 3; l2++)
-#pragma unroll
-            for (int m = 0; m < 3; m++)
-              if (m <= l2 && l2 < order)
-                rv[l2][m] = (r_[2 - m] + r_[2 - m + l2 + 1]) * (v_[2 - m] + v_[2 - m + l2 + 1]);
-          auto triple = [&](int q) {
-            double flux = 0.0;
-#pragma unroll
-            for (int l2 = 0; l2 < 3; l2++) {
-              if (l2 < order) {
-                double acc = 0.0;
-#pragma unroll
-                for (int m = 0; m <= l2; m++) acc += rv[l2][m] * (V(q, wk[2 - m]) + V(q, wk[2 - m + l2 + 1]));
-                flux += kgc[l2] * acc;
-              }
-            }
-            return flux * 0.25;
-          };
-#pragma unroll
-          for (int i = 0; i < NS; i++) F[i] = triple(3 + i);
-#pragma unroll
-          for (int cc = 0; cc < 3; cc++) F[iU + cc] = triple(3 + NS + cc);
-          double pflux = 0.0;
-#pragma unroll
-          for (int l2 = 0; l2 < 3; l2++) {
-            if (l2 < order) {
-              double acc = 0.0;
-#pragma unroll
-              for (int m = 0; m <= l2; m++) acc += (pr[2 - m] + pr[2 - m + l2 + 1]);
-              pflux += kgc[l2] * acc;
-            }
-          }
-          F[iU + D] -= pflux;
-          // energy: the same triple product with phi = H
-          {
-            double flux = 0.0;
-#pragma unroll
-            for (int l2 = 0; l2 < 3; l2++) {
-              if (l2 < order) {
-                double acc = 0.0;
-#pragma unroll
-                for (int m = 0; m <= l2; m++) acc += rv[l2][m] * (h[2 - m] + h[2 - m + l2 + 1]);
-                flux += kgc[l2] * acc;
-              }
-            }
-            F[NS + 3] = flux * 0.25;
-          }
-        }
-#pragma unroll
-        for (int i = 0; i < NE; i++) A.fe[i * nf + fi] = F[i];
-      } else {
-        teno = true;
-      }
-    }
-    // warp-aggregated append of the rejected faces to the TENO queue
-    const unsigned m = __ballot_sync(0xffffffffu, teno);
-    if (m) {
-      unsigned base = 0;
-      const int leader = __ffs(m) - 1;
-      if (lane == leader) base = atomicAdd(A.count, (unsigned)__popc(m));
-      base = __shfl_sync(0xffffffffu, base, leader);
-      if (teno) {
-        const unsigned slot = base + __popc(m & ((1u << lane) - 1u));
-        A.queue[slot] = TenoEntry{D, (int)c[0], (int)c[1], (int)c[2]};
-      }
-    }
-  }
-}
 
 // --- characteristic TENO faces -------------------------------------------
 struct StageTenoArgs {
@@ -321,21 +110,6 @@ static EulerArgs euler_args(const htr_fluid_view &v, const htr_rect3 &my, const 
   return a;
 }
 
-template <class Mix, int D, bool HYBRID>
-static cudaError_t kg_dir(const StageEulerArgs &A, const Mix &mix, cudaStream_t s) {
-  using TL = KGTile<D>;
-  const long long n[3] = {A.e.my.size(0), A.e.my.size(1), A.e.my.size(2)};
-  dim3 grid;
-  if (D == 0) grid = dim3((unsigned)((n[0] + TL::S - 1) / TL::S), (unsigned)n[1], (unsigned)n[2]);
-  else if (D == 1) grid = dim3((unsigned)((n[0] + TL::L - 1) / TL::L), (unsigned)((n[1] + TL::S - 1) / TL::S), (unsigned)n[2]);
-  else grid = dim3((unsigned)((n[0] + TL::L - 1) / TL::L), (unsigned)n[1], (unsigned)((n[2] + TL::S - 1) / TL::S));
-  const size_t sm = sizeof(double) * (Mix::NS + 6) * TL::L * TL::WS;
-  auto k = euler_kg_faces<Mix, D, HYBRID>;
-  cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm);
-  k<<<grid, TL::THREADS, sm, s>>>(A, mix);
-  return cudaGetLastError();
-}
-
 template <class Mix>
 cudaError_t launch_stage_euler(const htr_fluid_view &v, const htr_rect3 &my, const htr_rect3 &fb, const Mix &mix,
                                const StageWorkspace &w, const Fd<double> &H, const StageParams &p,
@@ -356,10 +130,7 @@ cudaError_t launch_stage_euler(const htr_fluid_view &v, const htr_rect3 &my, con
       A.fe = w.fe[D];
       A.queue = w.queue;
       A.count = w.count;
-      const bool hyb = p.scheme == 0;
-      if (D == 0) e = hyb ? kg_dir<Mix, 0, true>(A, mix, s) : kg_dir<Mix, 0, false>(A, mix, s);
-      else if (D == 1) e = hyb ? kg_dir<Mix, 1, true>(A, mix, s) : kg_dir<Mix, 1, false>(A, mix, s);
-      else e = hyb ? kg_dir<Mix, 2, true>(A, mix, s) : kg_dir<Mix, 2, false>(A, mix, s);
+      e = launch_kg_faces(A, mix, D, p.scheme == 0, s);
       if (e != cudaSuccess || (e = mark(k)) != cudaSuccess) return e;
     }
     if (p.scheme == 1) return mark(3);  // skew-symmetric: KG everywhere

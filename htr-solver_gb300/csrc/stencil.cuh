@@ -22,7 +22,7 @@ struct NodeDev {
   int8_t kgOrder;
   double rp[4][6], rm[4][6];
   double cp[4], cm[4];
-  float interp[2], grad[2];
+  double interp[2], grad[2];  // the reference's float tables (metric_coeffs.h:85-88), promoted
   double kg[3];
 };
 
@@ -102,11 +102,11 @@ static __constant__ float kP10[14] = {1,    1e-1, 1e-2, 1e-3,  1e-4,  1e-5,  1e-
                                       1e-7, 1e-8, 1e-9, 1e-10, 1e-11, 1e-12, 1e-13};
 
 HTR_D double interp2(int t, double a, double b) {
-  return __dadd_rn(__dmul_rn(double(kNode[t].interp[0]), a), __dmul_rn(double(kNode[t].interp[1]), b));
+  return __dadd_rn(__dmul_rn(kNode[t].interp[0], a), __dmul_rn(kNode[t].interp[1], b));
 }
 HTR_D double deriv(int t, double xm1, double x, double xp1, double m) {
-  return __dmul_rn(__dadd_rn(__dmul_rn(double(kNode[t].grad[0]), __dsub_rn(x, xm1)),
-                             __dmul_rn(double(kNode[t].grad[1]), __dsub_rn(xp1, x))),
+  return __dmul_rn(__dadd_rn(__dmul_rn(kNode[t].grad[0], __dsub_rn(x, xm1)),
+                             __dmul_rn(kNode[t].grad[1], __dsub_rn(xp1, x))),
                    m);
 }
 
@@ -389,6 +389,119 @@ HTR_D double sensor_cut(double Phi) {
   return double(kP10[power]);
 }
 
+// ---------------------------------------------------------------------------
+// FP32 pre-decision of the shock sensor with rigorous error bounds.
+//
+// The sensor of a node is true iff a_k / sum_j a_j > cut for its four
+// candidates, a_k = (1 + tau6 / (s_k + eps))^6, with the smoothness measures
+// s_k and tau6 of six point values.  sensor_prefilter evaluates s_k and tau6
+// in single precision together with an upper bound on the absolute error of
+// each: every stencil difference with integer coefficients c_i and k
+// rounded operations is within (k + 2) u C M of its exact value (C = sum
+// |c_i|, M = max |y_i|, u = 2^-24; the +2 covers the conversion of the
+// inputs), squares and sums add at most a few u relative to the (positive)
+// terms.  From those bounds it forms intervals for x_k = 1 + tau6/(s_k+eps)
+// and for q_k = x_k^6 / sum_j x_j^6, and returns a decision only when every
+// interval lies on one side of cut by more than 1e-3 cut, far above the
+// relative rounding of the interval arithmetic itself (below 1e-5).  It
+// returns -1 otherwise (and for large or non-finite inputs); the caller then
+// evaluates the sensor exactly in double precision.  Decisions therefore equal
+// the double-precision ones.
+// ---------------------------------------------------------------------------
+HTR_D int sensor_prefilter(double ym2, double ym1, double y0, double yp1, double yp2, double yp3,
+                           double cut) {
+  const float u = 5.9604645e-08f;
+  const float v0 = __double2float_rn(ym2), v1 = __double2float_rn(ym1), v2 = __double2float_rn(y0),
+              v3 = __double2float_rn(yp1), v4 = __double2float_rn(yp2), v5 = __double2float_rn(yp3);
+  float M = fmaxf(fmaxf(fmaxf(fabsf(v0), fabsf(v1)), fmaxf(fabsf(v2), fabsf(v3))), fmaxf(fabsf(v4), fabsf(v5)));
+  if (!(M < 1e6f)) return -1;
+  const float uM = u * M;
+  // s = A a^2 + B b^2 (+ C c^2) and the bound on its error
+  auto sq2 = [&](float A, float a, float ea, float B, float b, float eb, float &e) {
+    const float t = __fadd_rn(__fmul_rn(__fmul_rn(A, a), a), __fmul_rn(__fmul_rn(B, b), b));
+    e = A * ea * (2.0f * fabsf(a) + ea) + B * eb * (2.0f * fabsf(b) + eb) + 8.0f * u * t;
+    return t;
+  };
+  const float C13 = 13.0f / 12.0f, C23 = 3.0f / 12.0f, C14 = 1.0f / 36.0f, C24 = 13.0f / 12.0f,
+              C34 = 781.0f / 720.0f;
+  float e1, e2, e3, e4;
+  // s1: a = ym1 - 2y + yp1 (C 4, 2 ops), b = ym1 - yp1 (C 2, 1 op)
+  const float s1 = sq2(C13, __fadd_rn(__fsub_rn(v1, 2.0f * v2), v3), 4.0f * 4.0f * uM, C23, __fsub_rn(v1, v3),
+                       3.0f * 2.0f * uM, e1);
+  // s2: a = y - 2yp1 + yp2 (C 4, 2), b = 3y - 4yp1 + yp2 (C 8, 3)
+  const float s2 = sq2(C13, __fadd_rn(__fsub_rn(v2, 2.0f * v3), v4), 4.0f * 4.0f * uM, C23,
+                       __fadd_rn(__fsub_rn(__fmul_rn(3.0f, v2), 4.0f * v3), v4), 5.0f * 8.0f * uM, e2);
+  // s3: a = ym2 - 2ym1 + y (C 4, 2), b = 3y - 4ym1 + ym2 (C 8, 3)
+  const float s3 = sq2(C13, __fadd_rn(__fsub_rn(v0, 2.0f * v1), v2), 4.0f * 4.0f * uM, C23,
+                       __fadd_rn(__fsub_rn(__fmul_rn(3.0f, v2), 4.0f * v1), v0), 5.0f * 8.0f * uM, e3);
+  // s4: a = -11y + 18yp1 - 9yp2 + 2yp3 (C 40, 6), b = 2y - 5yp1 + 4yp2 - yp3 (C 12, 4),
+  //     c = -y + 3yp1 - 3yp2 + yp3 (C 8, 5)
+  const float a4 = __fadd_rn(__fsub_rn(__fadd_rn(__fmul_rn(-11.0f, v2), __fmul_rn(18.0f, v3)), __fmul_rn(9.0f, v4)),
+                             2.0f * v5);
+  const float b4 = __fsub_rn(__fadd_rn(__fsub_rn(2.0f * v2, __fmul_rn(5.0f, v3)), 4.0f * v4), v5);
+  const float c4 = __fadd_rn(__fsub_rn(__fadd_rn(-v2, __fmul_rn(3.0f, v3)), __fmul_rn(3.0f, v4)), v5);
+  const float ea4 = 8.0f * 40.0f * uM, eb4 = 6.0f * 12.0f * uM, ec4 = 7.0f * 8.0f * uM;
+  const float s4 = __fadd_rn(__fadd_rn(__fmul_rn(__fmul_rn(C14, a4), a4), __fmul_rn(__fmul_rn(C24, b4), b4)),
+                             __fmul_rn(__fmul_rn(C34, c4), c4));
+  e4 = C14 * ea4 * (2.0f * fabsf(a4) + ea4) + C24 * eb4 * (2.0f * fabsf(b4) + eb4) +
+       C34 * ec4 * (2.0f * fabsf(c4) + ec4) + 10.0f * u * s4;
+  const float comb = __fdiv_rn(__fadd_rn(__fadd_rn(s3, s2), 4.0f * s1), 6.0f);
+  const float tau = fabsf(__fsub_rn(s4, comb));
+  const float et = e4 + (e3 + e2 + 4.0f * e1) / 6.0f + 6.0f * u * (s4 + comb);
+  const float eps = 1e-8f;
+  const float tlo = fmaxf(tau - et, 0.0f), thi = tau + et;
+  const float sv[4] = {s1, s2, s3, s4}, ev[4] = {e1, e2, e3, e4};
+  float xl[4], xh[4], m = 1.0f;
+#pragma unroll
+  for (int k = 0; k < 4; k++) {
+    xl[k] = 1.0f + tlo / (sv[k] + ev[k] + eps);
+    xh[k] = 1.0f + thi / (fmaxf(sv[k] - ev[k], 0.0f) + eps);
+    m = fmaxf(m, xh[k]);
+  }
+  float pl[4], ph[4];
+#pragma unroll
+  for (int k = 0; k < 4; k++) {
+    pl[k] = pow6f(xl[k] / m);
+    ph[k] = pow6f(xh[k] / m);
+  }
+  const float cf = (float)cut;
+  bool all_smooth = true, any_shock = false;
+#pragma unroll
+  for (int k = 0; k < 4; k++) {
+    float ol = 0.0f, oh = 0.0f;
+#pragma unroll
+    for (int j = 0; j < 4; j++)
+      if (j != k) {
+        ol += pl[j];
+        oh += ph[j];
+      }
+    const float qlo = pl[k] / (pl[k] + oh);
+    const float qhi = ph[k] / (ph[k] + ol);
+    all_smooth = all_smooth && (qlo > cf * 1.001f);
+    any_shock = any_shock || (qhi < cf * 0.999f);
+  }
+  if (all_smooth) return 1;
+  if (any_shock) return 0;
+  return -1;
+}
+
+// sensor_cut with an FP32 pre-decision: decay and the exponent argument in
+// single precision (absolute error of the argument below 3e-4 for Phi in
+// [0, 1]); the integer part is taken from it when the argument is further
+// than 1e-3 from an integer, otherwise the exact double-precision path runs.
+HTR_D double sensor_cut_fast(double Phi) {
+  if (Phi >= 0.0 && Phi <= 1.0) {
+    const float P = __double2float_rn(Phi);
+    const float w = __fsub_rn(1.0f, P);
+    const float w2 = __fmul_rn(w, w), w3 = __fmul_rn(w2, w), w6 = __fmul_rn(w3, w3), w12 = __fmul_rn(w6, w6);
+    const float d = __fmul_rn(w12, __fadd_rn(1.0f, __fmul_rn(12.0f, P)));
+    const float z = __fsub_rn(12.5f, __fmul_rn(11.5f, __fsub_rn(1.0f, d)));
+    const float fl = floorf(z), fr = z - fl;
+    if (fr > 1e-3f && fr < 1.0f - 1e-3f) return double(kP10[min(max(int(fl), 0), 13)]);
+  }
+  return sensor_cut(Phi);
+}
+
 // Shock sensor of the hybrid scheme on a positive scalar (metric.inl:351-403),
 // true = smooth; `cut` from sensor_cut.
 HTR_D bool teno_a_sensor(double ym2, double ym1, double y, double yp1, double yp2, double yp3,
@@ -403,6 +516,8 @@ HTR_D bool teno_a_sensor(double ym2, double ym1, double y, double yp1, double yp
     const double eta = (fabs(2.0 * v1 * v2) + Ren_eps) / (v1 * v1 + v2 * v2 + Ren_eps);
     return ((1.0 - smin(1.0, Ren_irc * eta)) < 0.5);
   }
+  const int pre = sensor_prefilter(ym2, ym1, y, yp1, yp2, yp3, cut);
+  if (pre >= 0) return pre == 1;
   const Smooth s = smoothness(ym2, ym1, y, yp1, yp2, yp3);
   const double eps = 1e-8;
   // strict comparison a_k*a > cut: the filter's flag "q >= cut(1+1e-4)"

@@ -107,6 +107,38 @@ def test_sensors_bit_exact(port, gpu, case):
         assert np.array_equal(a, b), f"{(a != b).sum()} of {a.size} sensor{d} flags differ"
 
 
+@pytest.mark.parametrize("kind,n,mach", [("air", 40, (0.5, 3.0)), ("air", 32, (2.0, 6.0)), ("tg", 40, None)])
+def test_sensors_bit_exact_large(port, gpu, kind, n, mach):
+    """Shock sensors on larger seeded grids (tens of thousands of cells per
+    direction, strong compressions for the Mach 2-6 case): every boolean and
+    the Ducros value equal the oracle's."""
+    import torch
+    if kind == "air":
+        fl = workloads.air_box(n, seed=21, mach=mach)
+    else:
+        fl = workloads.taylor_green(n, seed=21)
+    m = workloads.make_mixture_struct(port, fl.meta["eos"], fl.meta["mix"])
+    h = oracle.load_mixture(port, fl.meta["eos"], m)
+    workloads.derive_state(port, fl, h)
+    gh = runtime.load_mixture(fl.meta["eos"], m)
+    host = fl.copy()
+    dev = fl.to_device("cuda")
+    oracle.update_sensors(port, host, h, 1.0)
+    vd = dev.view()
+    r = dev.bounds()
+    s = runtime.stream_handle()
+    util.call(gpu, "htr_UpdateDucrosSensor", C.byref(vd), r, r, 1.0, s)
+    for d in "XYZ":
+        util.call(gpu, f"htr_UpdateShockSensor{d}", C.byref(vd), r, r, gh, s)
+    torch.cuda.synchronize()
+    out = dev.to_host()
+    assert np.array_equal(out["DucrosSensor"], host["DucrosSensor"])
+    for d in "XYZ":
+        a, b = out[f"shockSensor{d}"], host[f"shockSensor{d}"]
+        assert np.array_equal(a, b), f"{(a != b).sum()} of {a.size} sensor{d} flags differ"
+        assert 0 < b.sum() <= b.size
+
+
 def test_chemistry_sources(port, gpu, case):
     kind, fl, h, gh = case
     host, dev = _run_both(port, gpu, fl, h, gh, "htr_AddChemistrySources",
