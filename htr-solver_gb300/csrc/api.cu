@@ -159,6 +159,15 @@ int static_scratch(void **out) {
   return HTR_OK;
 }
 
+// Directions with more than one cell (a one-cell direction is periodic and
+// contributes nothing to the RHS).
+unsigned active_dirs(const htr_rect3 &r) {
+  unsigned a = 0;
+  for (int d = 0; d < 3; d++)
+    if (r.hi[d] > r.lo[d]) a |= 1u << d;
+  return a;
+}
+
 int check_step_fields(const htr_fluid_view *v, htr_mixture_t m) {
   HTR_REQ_D(*v, rho);
   HTR_REQ_D(*v, mu);
@@ -193,7 +202,7 @@ namespace {
 
 // Step size, sensors (once per step) and Conserved_old (src/prometeo.rg:1342-1380).
 int step_prologue(const htr_fluid_view *v, htr_rect3 inner, htr_rect3 fb, const htr_step_params *p,
-                  htr_mixture_t m, double *dt_out, htr_stream_t s) {
+                  htr_mixture_t m, double *dt_out, htr_stream_t s, unsigned sensor_dirs = 7u) {
   if (p == nullptr) return fail(HTR_ERR_ARGUMENT, "null step parameters%s");
   if (int st = check_common(v, m, inner)) return st;
   if (p->scheme < HTR_SCHEME_HYBRID || p->scheme > HTR_SCHEME_SKEW) return fail(HTR_ERR_ARGUMENT, "unknown scheme%s");
@@ -220,7 +229,9 @@ int step_prologue(const htr_fluid_view *v, htr_rect3 inner, htr_rect3 fb, const 
     if ((st = check_field(v->shockSensorX, 1, "shockSensorX")) || (st = check_field(v->shockSensorY, 1, "shockSensorY")) ||
         (st = check_field(v->shockSensorZ, 1, "shockSensorZ")))
       return st;
-    if ((st = cuda_status(htr::launch_shock_sensor(*v, fb, fb, nspec_of(m), 7, cs), "shock sensors"))) return st;
+    if ((st = cuda_status(htr::launch_shock_sensor(*v, fb, fb, nspec_of(m), (int)sensor_dirs, cs),
+                          "shock sensors")))
+      return st;
   }
   return htr_InitializeTemporaries(v, fb, m, s);
 }
@@ -230,13 +241,15 @@ int step_prologue(const htr_fluid_view *v, htr_rect3 inner, htr_rect3 fb, const 
 int fused_step(const htr_fluid_view *v, htr_rect3 inner, htr_rect3 fb, const htr_step_params *p,
                htr_mixture_t m, const htr::StageWorkspace &w, double *dt_used, int *status_dev, htr_stream_t s) {
   double dt = 0.0;
-  if (int st = step_prologue(v, inner, fb, p, m, &dt, s)) return st;
+  // the fused stages read the sensors of the active directions only
+  if (int st = step_prologue(v, inner, fb, p, m, &dt, s, active_dirs(inner))) return st;
   if (dt_used) *dt_used = dt;
   htr::StageParams sp;
   sp.scheme = p->scheme == HTR_SCHEME_HYBRID ? 0 : (p->scheme == HTR_SCHEME_SKEW ? 1 : 2);
   sp.kind = p->scheme == HTR_SCHEME_TENOA ? htr::kTENOA : (p->scheme == HTR_SCHEME_TENOLAD ? htr::kTENOLAD : htr::kTENO);
   sp.chemistry = p->explicitChemistry ? 1 : 0;
   sp.dt = dt;
+  sp.active = active_dirs(inner);
   for (int stage = 1; stage <= 3; stage++) {
     sp.stage = stage;
     if (int st = with_mix(m, [&](const auto &mix) {
@@ -491,7 +504,9 @@ int htr_rk3_step(const htr_fluid_view *v, htr_rect3 inner, htr_rect3 fb, const h
     }
     for (int d = 2; d >= 0; d--)
       if ((st = diffusion(v, inner, fb, m, d, s))) return st;
-    if ((st = htr_UpdateVars(v, fb, stage, dt, 0, m, s))) return st;
+    // ghost cells keep their imposed state (the reference restores them
+    // from their primitives after the update)
+    if ((st = htr_UpdateVars(v, inner, stage, dt, 0, m, s))) return st;
     if ((st = check_common(v, m, inner))) return st;
     if ((st = with_mix(m, [&](const auto &mix) {
            return cuda_status(htr::launch_primitive(*v, inner, mix, status_dev, cs), "primitive");
@@ -563,6 +578,7 @@ int htr_rk3_stage_profile(const htr_fluid_view *v, htr_rect3 inner, htr_rect3 fb
   sp.chemistry = p->explicitChemistry ? 1 : 0;
   sp.dt = p->deltaTime;
   sp.stage = 1;
+  sp.active = active_dirs(inner);
   cudaEvent_t ev[htr::kStageKernels + 1];
   int made = 0;
   cudaError_t e = cudaSuccess;

@@ -69,6 +69,10 @@ struct StageParams {
   int chemistry;
   int stage;   // 1..3
   double dt;   // full step size
+  // bit D set: direction D has more than one cell.  A one-cell periodic
+  // direction contributes exactly zero to every flux difference (both faces
+  // see the same cell), so its faces are not computed.
+  unsigned active;
 };
 
 struct ConstPropDev;

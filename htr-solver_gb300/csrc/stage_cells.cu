@@ -142,6 +142,11 @@ __global__ void __launch_bounds__(128) diffusion_faces(const DiffFaceArgs A, con
     long long q[3] = {p[0], p[1], p[2]};
     q[D] = wrap_plus(p[D], A.fb.lo[D], A.fb.size(D), 1);
     const int t = ld(A.nt.at(p));
+    if (outside_face(t)) {
+#pragma unroll
+      for (int i = 0; i < NE; i++) A.fd[i * nf + f] = 0.0;
+      continue;
+    }
     const double m_s = ld(A.ms.at(p));
     // interior-dense indices of p and q (periodic interior == bounds)
     const long long ip = A.dn.idx(p), iq = A.dn.idx(q);
@@ -220,6 +225,8 @@ __global__ void __launch_bounds__(128) diffusion_faces(const DiffFaceArgs A, con
 // ---------------------------------------------------------------------------
 struct UpdateArgs {
   Fd<double> C, Cold, Ct, rho, P, T, X, Y, u, mu, lam, Di, SoS, me[3], md[3];
+  Fd<int> nt[3];
+  unsigned active;
   Dense dn;
   FaceGrid g;
   const double *fe[3], *fd[3];
@@ -328,6 +335,17 @@ __global__ void __launch_bounds__(128) stage_update(const UpdateArgs A, const __
     double ct[NE];
 #pragma unroll
     for (int k = 0; k < NE; k++) ct[k] = 0.0;
+    // boundary ghosts keep their imposed state; their RHS is zero
+    bool ghost = false;
+#pragma unroll
+    for (int D = 0; D < 3; D++)
+      if (A.active & (1u << D)) ghost = ghost || ghost_node(ld(A.nt[D].at(p)));
+    if (ghost) {
+      double *ctp = A.Ct.at(p);
+#pragma unroll
+      for (int k = 0; k < NE; k++) ctp[k] = 0.0;
+      continue;
+    }
     if (A.chemistry) {
       double y[NS], w[NS];
 #pragma unroll
@@ -341,6 +359,7 @@ __global__ void __launch_bounds__(128) stage_update(const UpdateArgs A, const __
     for (int pass = 0; pass < 2; pass++) {
 #pragma unroll
       for (int dd = 2; dd >= 0; dd--) {
+        if (!(A.active & (1u << dd))) continue;
         long long c1[3] = {p[0], p[1], p[2]};
         c1[dd] += 1;
         const long long nf = A.g.nf[dd];
@@ -415,6 +434,10 @@ cudaError_t launch_stage(const htr_fluid_view &v, const htr_rect3 &my, const htr
   const htr_field *ms[3] = {&v.dcsi_s, &v.deta_s, &v.dzet_s};
   const htr_field *nt[3] = {&v.nType_x, &v.nType_y, &v.nType_z};
   for (int D = 2; D >= 0; D--) {
+    if (!(sp.active & (1u << D))) {
+      if ((e = mark(1 + kDiffZ + (2 - D))) != cudaSuccess) return e;
+      continue;
+    }
     DiffFaceArgs A;
     A.C = fd<double>(v.Conserved);
     A.T = fd<double>(v.temperature);
@@ -458,6 +481,10 @@ cudaError_t launch_stage(const htr_fluid_view &v, const htr_rect3 &my, const htr
   U.md[0] = fd<double>(v.dcsi_d);
   U.md[1] = fd<double>(v.deta_d);
   U.md[2] = fd<double>(v.dzet_d);
+  U.nt[0] = fd<int>(v.nType_x);
+  U.nt[1] = fd<int>(v.nType_y);
+  U.nt[2] = fd<int>(v.nType_z);
+  U.active = sp.active;
   U.dn = dn;
   U.g = g;
   for (int D = 0; D < 3; D++) {

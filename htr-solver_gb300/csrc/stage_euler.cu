@@ -20,6 +20,7 @@ struct StageTenoArgs {
   const TenoEntry *queue;
   const unsigned *count;
   long long nall;  // > 0: every face of the three directions (no queue)
+  unsigned active; // directions whose faces are computed
 };
 
 template <class Mix, int D, int KIND>
@@ -45,8 +46,13 @@ HTR_D void teno_face_at(const StageTenoArgs &A, const Mix &mix, const long long 
     ef.shift(q, p, kNode[t].off[2], true);
   }
   double F[NE];
-  const double lim_f = a.dt * (ld(a.me.at(p)) + ld(a.me.at(q)));
-  ef.template teno_flux<KIND>(F, p, t, lim_f);
+  if (outside_face(t)) {
+#pragma unroll
+    for (int i = 0; i < NE; i++) F[i] = 0.0;
+  } else {
+    const double lim_f = a.dt * (ld(a.me.at(p)) + ld(a.me.at(q)));
+    ef.template teno_flux<KIND>(F, p, t, lim_f);
+  }
   const long long nf = A.g.nf[D];
   const long long fi = A.g.index(D, c);
   double *out = A.fe[D];
@@ -64,6 +70,7 @@ __global__ void __launch_bounds__(128) euler_teno_faces(const StageTenoArgs A, c
       long long f = k;
       D = 0;
       while (D < 2 && f >= A.g.nf[D]) f -= A.g.nf[D++];
+      if (!(A.active & (1u << D))) continue;
       const long long e0 = A.g.ext[D][0], e1 = A.g.ext[D][1];
       c[0] = A.g.lo[0] + f % e0;
       c[1] = A.g.lo[1] + (f / e0) % e1;
@@ -123,6 +130,10 @@ cudaError_t launch_stage_euler(const htr_fluid_view &v, const htr_rect3 &my, con
     if ((e = cudaMemsetAsync(w.count, 0, sizeof(unsigned), s)) != cudaSuccess) return e;
     for (int k = 0; k < 3; k++) {
       const int D = order[k];
+      if (!(p.active & (1u << D))) {
+        if ((e = mark(k)) != cudaSuccess) return e;
+        continue;
+      }
       StageEulerArgs A;
       A.e = euler_args(v, my, fb, D, rk0, rk1, sdt);
       A.H = H;
@@ -147,6 +158,7 @@ cudaError_t launch_stage_euler(const htr_fluid_view &v, const htr_rect3 &my, con
   T.queue = w.queue;
   T.count = w.count;
   T.nall = (p.scheme == 2) ? (g.nf[0] + g.nf[1] + g.nf[2]) : 0;
+  T.active = p.active;
   int dev = 0, sms = 152;
   cudaGetDevice(&dev);
   cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);

@@ -105,8 +105,13 @@ __global__ void __launch_bounds__(KGTile<D>::THREADS) euler_kg_faces(const Stage
         wq = wp + kNode[t].off[2];
       }
       const int wm = wp + kNode[t].off[1];
-      const bool smooth = !HYBRID || (sflag[wm * L + l] && sflag[wp * L + l] && sflag[wq * L + l]);
-      if (smooth) {
+      const bool outside = outside_face(t);
+      const bool smooth = outside || !HYBRID || (sflag[wm * L + l] && sflag[wp * L + l] && sflag[wq * L + l]);
+      if (outside) {
+        const long long fi = A.g.index(D, c);
+#pragma unroll
+        for (int i = 0; i < NE; i++) A.fe[i * nf + fi] = 0.0;
+      } else if (smooth) {
         double F[NE];
         const long long fi = A.g.index(D, c);
         auto V = [&](int q, int w) { return win[q * L * WS + w * L + l]; };

@@ -17,6 +17,12 @@ namespace htr {
 
 enum NodeType { Std = 0, L_S, Lp1_S, Lp2_S, Rm3_S, Rm2_S, Rm1_S, R_S, L_C, Lp1_C, Rm2_C, Rm1_C, R_C };
 
+// Boundary (ghost) nodes: their state is imposed by the boundary condition,
+// never advanced by the RHS.
+HTR_HD bool ghost_node(int t) { return t == L_S || t == R_S || t == L_C || t == R_C; }
+// A face whose left node is a right-boundary ghost lies outside the domain.
+HTR_HD bool outside_face(int t) { return t == R_S || t == R_C; }
+
 struct NodeDev {
   int8_t off[5];
   int8_t kgOrder;

@@ -93,12 +93,12 @@ def spectral_dt(lib, fl, mixh, cfl):
     return cfl / r.value
 
 
-def update_derivatives(lib, fl, mixh, stage, dt, scheme="Hybrid", chemistry=True):
+def update_derivatives(lib, fl, mixh, stage, dt, scheme="Hybrid", chemistry=True, bnum=(0, 0, 0)):
     """One explicit RHS evaluation in the reference's order (prometeo.rg:480-606)."""
     A = _abi()
     v = fl.view()
     allr = fl.bounds()
-    inner = fl.interior()
+    inner = fl.interior(bnum)
     fb = fl.bounds()
     A.check(lib, lib.htr_InitializeTimeDerivatives(C.byref(v), allr, 0, mixh, None), "init_t")
     if chemistry:
@@ -128,19 +128,23 @@ def update_sensors(lib, fl, mixh, vorticity_scale):
         A.check(lib, fn(C.byref(v), r, r, mixh, None), f"shock {d}")
 
 
-def refresh(lib, fl, mixh):
-    """UpdatePrimitivesAndBCsFromConserved for a fully periodic grid."""
+def refresh(lib, fl, mixh, bnum=(0, 0, 0)):
+    """UpdatePrimitivesAndBCsFromConserved (prometeo.rg:429-478) for periodic
+    grids and constant (Dirichlet) ghost nodes, whose state stays imposed."""
     A = _abi()
     v = fl.view()
-    A.check(lib, lib.htr_UpdatePrimitiveFromConserved(C.byref(v), fl.interior(), mixh, None),
+    A.check(lib, lib.htr_UpdatePrimitiveFromConserved(C.byref(v), fl.interior(bnum), mixh, None),
             "prim")
     A.check(lib, lib.htr_UpdatePropertiesFromPrimitive(C.byref(v), fl.bounds(), mixh, None),
             "props")
 
 
 def step(lib, fl, mixh, scheme="Hybrid", vorticity_scale=1.0, cfl=0.8, dt=None, chemistry=True,
-         stages=3, hook=None):
-    """One SSP-RK3 time step of a periodic grid; returns the dt used."""
+         stages=3, hook=None, bnum=(0, 0, 0)):
+    """One SSP-RK3 time step; returns the dt used.  `bnum` ghost layers per
+    side hold Dirichlet states: the RHS, the RK update and the primitive
+    recovery run on the interior only (the reference restores ghost
+    conserved variables from their imposed primitives after each update)."""
     A = _abi()
     if dt is None:
         dt = spectral_dt(lib, fl, mixh, cfl)
@@ -149,9 +153,9 @@ def step(lib, fl, mixh, scheme="Hybrid", vorticity_scale=1.0, cfl=0.8, dt=None, 
     v = fl.view()
     A.check(lib, lib.htr_InitializeTemporaries(C.byref(v), fl.bounds(), mixh, None), "tmp")
     for s in range(1, stages + 1):
-        update_derivatives(lib, fl, mixh, s, dt, scheme, chemistry)
+        update_derivatives(lib, fl, mixh, s, dt, scheme, chemistry, bnum)
         if hook is not None:
             hook(s, fl)
-        A.check(lib, lib.htr_UpdateVars(C.byref(v), fl.bounds(), s, dt, 0, mixh, None), "rk")
-        refresh(lib, fl, mixh)
+        A.check(lib, lib.htr_UpdateVars(C.byref(v), fl.interior(bnum), s, dt, 0, mixh, None), "rk")
+        refresh(lib, fl, mixh, bnum)
     return dt

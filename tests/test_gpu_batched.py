@@ -1,0 +1,116 @@
+"""Batched 1-D shock tubes on the GPU against per-tube oracle steps.
+
+Tubes of both mixtures (staggered Dirichlet ghosts, one-cell periodic y/z)
+are packed end to end into one strip per mixture; one fused RK3 step of the
+strip (htr_rk3_step_ws) must reproduce, tube by tube, one oracle step of
+each tube on its own (RHS, update and primitive recovery on the interior,
+ghosts imposed).  The per-tube task path (htr_rk3_step on each tube, the
+plain drop-in) is checked against the same oracle steps.  Bar: every state
+field within 1e-11 relative per component; x shock sensors bit-exact.
+"""
+import ctypes as C
+
+import numpy as np
+import pytest
+
+from htr_gb300 import abi, runtime, tubes, workloads
+
+import oracle
+from tests import util
+
+FIELDS = ("Conserved", "temperature", "pressure", "Conserved_t", "MolarFracs", "MassFracs", "velocity",
+          "rho", "mu", "lam", "Di", "SoS")
+
+
+def _groups(seed=31, n=8):
+    insts = tubes.instances(n, seed=seed, length=(12, 40))
+    groups = {}
+    for inst in insts:
+        groups.setdefault(inst["eos"], []).append(inst)
+    return groups
+
+
+def _oracle_tubes(port, insts, chem):
+    """Host tubes derived by the oracle, the common dt, and their oracle step."""
+    eos = insts[0]["eos"]
+    fls = [tubes.tube_fluid(i) for i in insts]
+    m = workloads.make_mixture_struct(port, eos, fls[0].meta["mix"])
+    h = oracle.load_mixture(port, eos, m)
+    for f in fls:
+        workloads.derive_state(port, f, h)
+    dt = 0.1 * min(oracle.spectral_dt(port, f, h, 0.8) for f in fls)
+    start = [f.copy() for f in fls]
+    for f in fls:
+        oracle.step(port, f, h, dt=dt, chemistry=chem, bnum=(1, 0, 0))
+    return start, fls, m, dt
+
+
+def _check(out, ref, name_prefix, sensors=("X",)):
+    for name in FIELDS:
+        err = util.rel_err(out[name], ref[name])
+        assert err.max() <= util.RHS_REL_TOL, (name_prefix, name, err.max())
+    for d in sensors:
+        assert np.array_equal(out[f"shockSensor{d}"], ref[f"shockSensor{d}"]), (name_prefix, d)
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("eos", [abi.HTR_EOS_CONSTPROPMIX, abi.HTR_EOS_AIRMIX])
+def test_batched_strip_equals_per_tube_oracle(eos):
+    import torch
+    port = oracle.port_lib()
+    insts = _groups()[eos]
+    chem = eos == abi.HTR_EOS_AIRMIX
+    start, ref, m, dt = _oracle_tubes(port, insts, chem)
+    strip, offs = tubes.pack(start)
+    gh = runtime.load_mixture(eos, m)
+    dev = strip.to_device("cuda")
+    status = torch.zeros(1, dtype=torch.int32, device="cuda")
+    runtime.rk3_step(dev, gh, dt=dt, chemistry=chem, fused=True, status_dev=C.c_void_p(status.data_ptr()))
+    torch.cuda.synchronize()
+    assert status.item() == 0
+    out = dev.to_host()
+    for k, (o, f) in enumerate(zip(offs, ref)):
+        tube = {name: a[:, :, o:o + f.nx] for name, a in out.arrays.items()}
+        _check(tube, f.arrays, f"tube {k}")
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("eos", [abi.HTR_EOS_CONSTPROPMIX, abi.HTR_EOS_AIRMIX])
+def test_plain_per_tube_task_path(eos):
+    import torch
+    port = oracle.port_lib()
+    insts = _groups()[eos]
+    chem = eos == abi.HTR_EOS_AIRMIX
+    start, ref, m, dt = _oracle_tubes(port, insts, chem)
+    gh = runtime.load_mixture(eos, m)
+    for k, (s, f) in enumerate(zip(start, ref)):
+        dev = s.to_device("cuda")
+        runtime.rk3_step(dev, gh, dt=dt, chemistry=chem, fused=False, interior=dev.interior((1, 0, 0)))
+        torch.cuda.synchronize()
+        _check(dev.to_host().arrays, f.arrays, f"tube {k}", sensors=("X", "Y", "Z"))
+
+
+@pytest.mark.parametrize("eos", [abi.HTR_EOS_CONSTPROPMIX, abi.HTR_EOS_AIRMIX])
+def test_oracle_tube_step_keeps_ghosts(eos):
+    """CPU: one oracle step of a tube leaves its Dirichlet ghosts untouched and
+    changes the interior."""
+    port = oracle.port_lib()
+    insts = _groups()[eos]
+    start, ref, m, dt = _oracle_tubes(port, insts, eos == abi.HTR_EOS_AIRMIX)
+    for s, f in zip(start, ref):
+        for name in ("Conserved", "temperature", "pressure", "rho"):
+            a, b = s[name], f[name]
+            assert np.array_equal(a[:, :, [0, -1]], b[:, :, [0, -1]]), name
+        assert not np.array_equal(s["Conserved"], f["Conserved"])
+        assert np.isfinite(f["Conserved"]).all()
+
+
+def test_strip_layout():
+    insts = tubes.instances(5, seed=2, length=(10, 20))
+    fls = [tubes.tube_fluid(i) for i in insts if i["eos"] == insts[0]["eos"]]
+    strip, offs = tubes.pack(fls)
+    assert strip.nx == sum(f.nx for f in fls) and strip.ny == strip.nz == 1
+    for o, f in zip(offs, fls):
+        t = strip["nType_x"][0, 0, o:o + f.nx]
+        assert t[0] == tubes.L_S and t[-1] == tubes.R_S
+        assert np.array_equal(t, tubes.node_types(f.nx - 2))
