@@ -34,7 +34,7 @@ sys.path.insert(0, ROOT)
 import __graft_entry__  # noqa: E402
 
 __graft_entry__.load_package()
-from htr_gb300 import abi, workloads  # noqa: E402
+from htr_gb300 import abi, tubes, workloads  # noqa: E402
 
 METRIC = "FP64 RHS cell-updates/s"
 UNIT = "cell-updates/s"
@@ -252,6 +252,99 @@ def e2e_pipelined(dev, gh, dt, steps, runtime, barrier, device):
     return value, h2d, d2h, n
 
 
+def run_batched(args, device, runtime, lib, steps=3):
+    """Batched 1-D shock tubes: every tube of one mixture packed into one strip,
+    both strips advanced by one CUDA graph per SSP-RK3 step (fused stages);
+    against the plain drop-in looped over the tubes (htr_rk3_step, one task
+    kernel per reference task, on each tube in place).  A solve is one RK3
+    step of one tube; both forms use the same per-mixture dt."""
+    import torch
+    insts = tubes.instances(args.tubes, seed=4242)
+    stream = torch.cuda.current_stream()
+    strips = []
+    for eos in (abi.HTR_EOS_CONSTPROPMIX, abi.HTR_EOS_AIRMIX):
+        group = [i for i in insts if i["eos"] == eos]
+        if not group:
+            continue
+        host, offs = tubes.build_strip(group)
+        m = workloads.make_mixture_struct(lib, eos, host.meta["mix"])
+        gh = runtime.load_mixture(eos, m)
+        dev = host.to_device(device)
+        del host
+        workloads.derive_state(lib, dev, gh, runtime.stream_handle())
+        air = eos == abi.HTR_EOS_AIRMIX
+        if air:
+            dt = choose_dt(dev, gh, lib, runtime)
+        else:
+            out = torch.zeros(1, dtype=torch.float64, device=device)
+            v = dev.view()
+            abi.check(lib, lib.htr_CalculateMaxSpectralRadius(
+                C.byref(v), dev.interior(), gh, C.cast(C.c_void_p(out.data_ptr()), C.POINTER(C.c_double)),
+                runtime.stream_handle()), "cfl")
+            dt = 0.8 / out.item()
+        strips.append(dict(dev=dev, gh=gh, dt=dt, offs=offs, L=[i["L"] for i in group], chem=air))
+    cells = sum(s["dev"].ncells for s in strips)
+    ws = runtime.Workspace()
+    ws.get(max(runtime.workspace_bytes(s["dev"], s["gh"]) for s in strips), device)
+
+    def step_all(st):
+        for s in strips:
+            runtime.rk3_step(s["dev"], s["gh"], dt=s["dt"], chemistry=s["chem"], stream=st, workspace=ws)
+
+    side = torch.cuda.Stream()
+    side.wait_stream(stream)
+    with torch.cuda.stream(side):
+        step_all(side)
+    stream.wait_stream(side)
+    graph = torch.cuda.CUDAGraph()
+    with torch.cuda.graph(graph, stream=side, capture_error_mode="relaxed"):
+        step_all(side)
+    graph.replay()
+    torch.cuda.synchronize()
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    e0.record(stream)
+    for _ in range(steps):
+        graph.replay()
+    e1.record(stream)
+    e1.synchronize()
+    t_batched = e0.elapsed_time(e1) / steps
+    # plain drop-in: htr_rk3_step on each tube, in place inside the strips
+    p = runtime.htr_step_params
+    used = C.c_double(0.0)
+    sh = runtime.stream_handle()
+
+    def loop_all():
+        for s in strips:
+            prm = p(runtime.SCHEMES["Hybrid"], 1.0, 0.0, s["dt"], 1 if s["chem"] else 0)
+            sv = s["dev"].view()
+            for off, L in zip(s["offs"], s["L"]):
+                v, fb, inner = tubes.tube_view(sv, int(off), L)
+                st = lib.htr_rk3_step(C.byref(v), inner, fb, C.byref(prm), s["gh"], C.byref(used), None, sh)
+                if st:
+                    abi.check(lib, st, "htr_rk3_step")
+
+    loop_all()
+    torch.cuda.synchronize()
+    f0, f1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    f0.record(stream)
+    loop_all()
+    f1.record(stream)
+    f1.synchronize()
+    t_plain = f0.elapsed_time(f1)
+    n = len(insts)
+    return {"metric": "batched solves/s", "unit": "tube RK3 steps/s", "tubes": n, "cells": int(cells),
+            "value": n / (t_batched * 1e-3), "ms_per_step": t_batched,
+            "cell_updates_per_s": 3.0 * cells / (t_batched * 1e-3),
+            "plain": {"value": n / (t_plain * 1e-3), "ms_per_step": t_plain,
+                      "cell_updates_per_s": 3.0 * cells / (t_plain * 1e-3),
+                      "form": "htr_rk3_step looped over the tubes (task kernels, one tube per call)"},
+            "speedup_vs_plain": t_plain / t_batched,
+            "config": {"workload": f"{n} 1-D shock tubes, 128-8192 cells, gamma-1.4 gas or 5-species air "
+                                   f"(1/2 each), staggered Dirichlet ends, hybrid scheme, SSP-RK3",
+                       "form": "two strips (one per mixture), one CUDA graph per RK3 step",
+                       "dt": {("air" if s["chem"] else "gas"): s["dt"] for s in strips}}}
+
+
 def fp64_peak(lib):
     lib.htr_probe_fp64_tflops.argtypes = [C.c_int, C.POINTER(C.c_double)]
     lib.htr_probe_fp64_tflops.restype = C.c_int
@@ -337,6 +430,11 @@ def run_gpu(args):
             "gpu_launches": args.steps * (3 + 3 * 9),
             "clocks": clk,
         }
+        if args.tubes > 0:
+            try:
+                result["batched"] = run_batched(args, device, runtime, lib)
+            except Exception as exc:  # the headline line must still print
+                result["batched"] = {"error": f"{type(exc).__name__}: {exc}"}
         if args.cpu_baseline:
             result["cpu_baseline"] = cpu_baseline(args.cpu_seconds)
     if ws > 1:
@@ -408,6 +506,7 @@ def main():
     p.add_argument("--n", type=int, default=256)
     p.add_argument("--cpu-seconds", type=float, default=20.0)
     p.add_argument("--no-cpu-baseline", dest="cpu_baseline", action="store_false")
+    p.add_argument("--tubes", type=int, default=4096, help="batched shock tubes (0: skip)")
     args = p.parse_args()
     res = run_reference(args) if args.impl == "reference" else run_gpu(args)
     if res is not None:

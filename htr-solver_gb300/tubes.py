@@ -80,20 +80,28 @@ def metric_1d(L, width=1.0):
                x[min(max(p + o[2], 0), n - 1)], x[min(max(p + o[3], 0), n - 1)], x[min(max(p + o[4], 0), n - 1)]]
         return sum(pts[j] * sum(nd["rp"][k][j] * nd["cp"][k] for k in range(4)) for j in range(6))
 
-    m_e = np.empty(n)
+    # face coordinates x_{p+1/2}: standard nodes vectorised, boundary nodes one by one
+    xf = np.empty(n)
+    w = np.array([sum(NODE[STD]["rp"][k][j] * NODE[STD]["cp"][k] for k in range(4)) for j in range(6)])
+    i = np.arange(3, n - 4)
+    xf[i] = (x[i - 2] * w[0] + x[i - 1] * w[1] + x[i] * w[2] + x[i + 1] * w[3] + x[i + 2] * w[4] +
+             x[i + 3] * w[5])
+    for p in list(range(0, 3)) + list(range(n - 4, n)):
+        xf[p] = recon(p)
+    xm0 = recon(0 + NODE[int(t[0])]["off"][1])
+    dxf = np.diff(np.concatenate([[xm0], xf]))
+    m_e = np.divide(1.0, dxf, out=np.zeros(n), where=dxf != 0)
+    # collocated (getDeriv) and staggered metrics
     m_d = np.empty(n)
-    m_s = np.empty(n)
-    xm = recon(0 + NODE[int(t[0])]["off"][1])
-    for p in range(n):
-        xp = recon(p)
-        m_e[p] = 1.0 / (xp - xm) if xp != xm else 0.0
-        xm = xp
+    m_d[i] = 1.0 / (0.5 * (x[i] - x[i - 1]) + 0.5 * (x[i + 1] - x[i]))
+    for p in list(range(0, 3)) + list(range(n - 4, n)):
         nd = NODE[int(t[p])]
         pm1 = min(max(p + nd["off"][1], 0), n - 1)
         pp1 = min(max(p + nd["off"][2], 0), n - 1)
-        g = nd["grad"][0] * (x[p] - x[pm1]) + nd["grad"][1] * (x[pp1] - x[p])
-        m_d[p] = 1.0 / g
-        m_s[p] = 1.0 / (x[p + 1] - x[p]) if p + 1 < n else 1.0 / dx
+        m_d[p] = 1.0 / (nd["grad"][0] * (x[p] - x[pm1]) + nd["grad"][1] * (x[pp1] - x[p]))
+    m_s = np.empty(n)
+    m_s[:-1] = 1.0 / np.diff(x)
+    m_s[-1] = 1.0 / dx
     m_e[0] = 1.0 / (-8.0 / 3.0 * x[0] + 3.0 * x[1] - 1.0 / 3.0 * x[2])
     m_e[-1] = 1.0 / (8.0 / 3.0 * x[-1] - 3.0 * x[-2] + 1.0 / 3.0 * x[-3])
     return m_e, m_d, m_s
@@ -147,6 +155,60 @@ def tube_fluid(inst):
     fl.meta = dict(workload="shock_tube", eos=inst["eos"], L=L, bnum=(1, 0, 0),
                    mix=(AIR_REF if nspec == 5 else GAS_PARAMS), vorticityScale=1.0)
     return fl
+
+
+def _tube_arrays(inst):
+    """Per-cell x arrays of one tube: node type, metrics, p, T (model units)."""
+    L = inst["L"]
+    m_e, m_d, m_s = metric_1d(L)
+    xs = np.concatenate([[0.0], (np.arange(L) + 0.5) / L, [1.0]])
+    left = xs < 0.5
+    (pL, TL), (pR, TR) = inst["left"], inst["right"]
+    p = np.where(left, pL, pR)
+    T = np.where(left, TL, TR)
+    if inst["eos"] == abi.HTR_EOS_AIRMIX:
+        p = p / AIR_REF["PRef"]
+        T = T / AIR_REF["TRef"]
+    return node_types(L), m_e, m_d, m_s, p, T
+
+
+def build_strip(insts):
+    """The strip of `insts` (one mixture) built directly; equals
+    pack([tube_fluid(i) for i in insts]).  Returns (strip, x offsets)."""
+    assert len({i["eos"] for i in insts}) == 1
+    air = insts[0]["eos"] == abi.HTR_EOS_AIRMIX
+    parts = [_tube_arrays(i) for i in insts]
+    offs = np.cumsum([0] + [len(pt[0]) for pt in parts])
+    n = int(offs[-1])
+    strip = Fluid((n, 1, 1), 5 if air else 1)
+    cat = lambda k: np.concatenate([pt[k] for pt in parts]).reshape(1, 1, -1)
+    strip["nType_x"] = cat(0)
+    strip["dcsi_e"], strip["dcsi_d"], strip["dcsi_s"] = cat(1), cat(2), cat(3)
+    strip["pressure"], strip["temperature"] = cat(4), cat(5)
+    if air:
+        strip["MolarFracs"] = np.broadcast_to(X_AIR, strip["MolarFracs"].shape)
+    else:
+        strip["MolarFracs"] = 1.0
+    strip["velocity"] = 0.0
+    for name in ("deta", "dzet"):
+        for suf in ("_e", "_d", "_s"):
+            strip[name + suf] = 1.0
+    strip.meta = dict(workload="shock_tube_strip", eos=insts[0]["eos"], bnum=(0, 0, 0), tubes=len(insts),
+                      mix=(AIR_REF if air else GAS_PARAMS), vorticityScale=1.0)
+    return strip, offs[:-1]
+
+
+def tube_view(strip_view, off, L):
+    """htr_fluid_view of one tube inside a strip (bases shifted by `off` cells),
+    with its bounds and interior rectangles in tube coordinates."""
+    import ctypes as C
+    v = abi.htr_fluid_view()
+    C.memmove(C.byref(v), C.byref(strip_view), C.sizeof(v))
+    for name, _ in abi.htr_fluid_view._fields_:
+        f = getattr(v, name)
+        if f.base:
+            f.base = f.base + off * f.stride[0]
+    return v, abi.rect((0, 0, 0), (L + 1, 0, 0)), abi.rect((1, 0, 0), (L, 0, 0))
 
 
 def pack(fluids):
