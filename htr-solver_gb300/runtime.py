@@ -82,8 +82,11 @@ class Workspace:
 
     def get(self, nbytes, device):
         import torch
-        if self.buf is None or self.nbytes < nbytes or self.buf.device != torch.device(device):
-            self.buf = torch.empty(nbytes + 256, dtype=torch.uint8, device=device)
+        dev = torch.device(device)
+        if dev.type == "cuda" and dev.index is None:
+            dev = torch.device("cuda", torch.cuda.current_device())
+        if self.buf is None or self.nbytes < nbytes or self.buf.device != dev:
+            self.buf = torch.empty(nbytes + 256, dtype=torch.uint8, device=dev)
             self.nbytes = nbytes
         addr = self.buf.data_ptr()
         return (addr + 255) // 256 * 256
@@ -121,3 +124,32 @@ def rk3_step(fluid, mixh, scheme="Hybrid", vorticity_scale=1.0, cfl=0.0, dt=0.0,
                             status_dev, stream_handle(stream))
         abi.check(l, st, "htr_rk3_step")
     return used.value
+
+
+def stable_dt(fluid, mixh, cfl=0.8, chemistry=True, stream=None):
+    """Step size of a device grid: cfl / max spectral radius
+    (src/prometeo_cfl.hpp:55-190), and with chemistry at most half the fastest
+    chemical time scale rho_i / |w_i| of the species that carry at least 0.1 %
+    of the mass (explicit chemistry stays stable)."""
+    import torch
+    l = lib()
+    v = fluid.view()
+    s = stream_handle(stream)
+    out = torch.zeros(1, dtype=torch.float64, device=fluid.device)
+    abi.check(l, l.htr_CalculateMaxSpectralRadius(C.byref(v), fluid.interior(), mixh,
+                                                  C.cast(C.c_void_p(out.data_ptr()), C.POINTER(C.c_double)), s),
+              "htr_CalculateMaxSpectralRadius")
+    torch.cuda.synchronize()
+    dt = cfl / out.item()
+    if chemistry and fluid.nspec > 1:
+        abi.check(l, l.htr_InitializeTimeDerivatives(C.byref(v), fluid.bounds(), 0, mixh, s), "init")
+        abi.check(l, l.htr_AddChemistrySources(C.byref(v), fluid.interior(), mixh, s), "chem")
+        torch.cuda.synchronize()
+        ns = fluid.nspec
+        w = fluid["Conserved_t"][..., :ns].abs()
+        rhoi = fluid["Conserved"][..., :ns]
+        rho = fluid["rho"][..., None]
+        sig = rhoi > 1e-3 * rho
+        tau = torch.where(sig, rhoi / w.clamp_min(1e-300), torch.full_like(rhoi, float("inf"))).min().item()
+        dt = min(dt, 0.5 * tau)
+    return dt

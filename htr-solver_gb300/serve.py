@@ -1,0 +1,249 @@
+"""Serving: simulation requests admitted as they arrive, stepped together.
+
+A request asks for a number of SSP-RK3 steps of one seeded grid: a 1-D shock
+tube, a 2-D vortex-advection box or a 3-D reacting-air box.  The server
+keeps every admitted request's state resident on the device and advances
+all of them round by round: each round issues one step of every active
+request, each as the replay of that request's CUDA graph of one fused step
+(htr_rk3_step_ws on the request's own workspace) on a stream of a small
+pool, so the steps of different requests overlap on the GPU.  Requests are
+admitted in arrival order while their device memory (state + workspace) fits
+the HBM budget; a finished request's result (Conserved) is copied to the host
+and its memory released, which lets the next request in.  At most two rounds
+are in flight, so the host never runs far ahead of the device.
+
+`run_plain` is the reference point: the plain drop-in per request, one
+request at a time in arrival order (htr_rk3_step, one task kernel per
+reference task).
+
+Times are seconds from the start of a session; time-to-solution is the
+completion time minus the arrival time.
+"""
+import time
+from dataclasses import dataclass
+
+import numpy as np
+
+from . import abi, runtime, tubes, workloads
+
+
+@dataclass
+class Request:
+    rid: int
+    kind: str          # "tube" | "vortex" | "box"
+    size: int          # cells per side (tube: interior length)
+    seed: int
+    steps: int
+    arrival: float     # s after the start of the session
+    admitted: float = None
+    done: float = None
+    result: object = None   # host copy of Conserved after the last step
+
+    @property
+    def tts(self):
+        return None if self.done is None else self.done - self.arrival
+
+
+def request_mix(n, rate, seed=0, steps=(100, 2000), tube=(256, 8192), vortex=(64, 512), box=(32, 96)):
+    """n requests with Poisson arrivals of `rate` per second: tubes, 2-D
+    vortex boxes and 3-D reacting boxes in equal proportion."""
+    rng = np.random.Generator(np.random.PCG64(seed))
+    t = 0.0
+    out = []
+    for i in range(n):
+        t += rng.exponential(1.0 / rate)
+        kind = ("tube", "vortex", "box")[int(rng.integers(0, 3))]
+        lo, hi = {"tube": tube, "vortex": vortex, "box": box}[kind]
+        out.append(Request(i, kind, int(rng.integers(lo, hi + 1)), int(rng.integers(0, 2 ** 31)),
+                           int(rng.integers(steps[0], steps[1] + 1)), t))
+    return out
+
+
+def host_fluid(req):
+    """Seeded host state of a request (primitives, node types, metrics)."""
+    if req.kind == "tube":
+        inst = tubes.instances(1, seed=req.seed, length=(req.size, req.size))[0]
+        return tubes.tube_fluid(inst)
+    if req.kind == "vortex":
+        return workloads.vortex2d(req.size, seed=req.seed)
+    return workloads.air_box(shape=(req.size,) * 3, seed=req.seed)
+
+
+class Instance:
+    """Device state of one admitted request."""
+
+    def __init__(self, req, device, stream, graphs=True):
+        import torch
+        self.req = req
+        self.stream = stream
+        host = host_fluid(req)
+        eos = host.meta["eos"]
+        self.bnum = host.meta.get("bnum", (0, 0, 0))
+        self.chem = eos == abi.HTR_EOS_AIRMIX
+        l = runtime.lib()
+        m = workloads.make_mixture_struct(l, eos, host.meta["mix"])
+        self.gh = runtime.load_mixture(eos, m)
+        with torch.cuda.stream(stream):
+            self.dev = host.to_device(device)
+            workloads.derive_state(l, self.dev, self.gh, runtime.stream_handle(stream))
+            self.dt = runtime.stable_dt(self.dev, self.gh, chemistry=self.chem, stream=stream)
+            self.ws = runtime.Workspace()
+            self.ws.get(runtime.workspace_bytes(self.dev, self.gh), device)
+        self.bytes = sum(a.numel() * a.element_size() for a in self.dev.arrays.values()) + self.ws.nbytes
+        self.remaining = req.steps
+        self.graph = None
+        if graphs:
+            g = torch.cuda.CUDAGraph()
+            stream.synchronize()
+            with torch.cuda.stream(stream):
+                g.capture_begin(capture_error_mode="relaxed")
+                self._step(stream)
+                g.capture_end()
+            self.graph = g
+        self.done_event = None
+
+    def _step(self, stream):
+        runtime.rk3_step(self.dev, self.gh, dt=self.dt, chemistry=self.chem, stream=stream, workspace=self.ws)
+
+    def step(self):
+        import torch
+        with torch.cuda.stream(self.stream):
+            if self.graph is not None:
+                self.graph.replay()
+            else:
+                self._step(self.stream)
+        self.remaining -= 1
+
+    def finish(self):
+        """Host copy of the result; releases the device state."""
+        self.req.result = self.dev["Conserved"].cpu().numpy()
+        self.dev = None
+        self.ws = None
+        self.graph = None
+
+
+def estimate_bytes(req):
+    """Device bytes of a request before admission (state + workspace)."""
+    if req.kind == "tube":
+        cells, neq = req.size + 2, 9
+    elif req.kind == "vortex":
+        cells, neq = req.size ** 2, 5
+    else:
+        cells, neq = req.size ** 3, 9
+    nsp = neq - 4
+    state = cells * 8 * (12 + 3 * 3 + 3 * neq + 3 * nsp + 4 + 1) + cells * (3 * 4 + 3)
+    faces = 3 * (cells + cells ** (2 / 3 if req.kind == "box" else 0.5))
+    work = int(2 * faces * neq * 8 + faces * 16 + 11 * cells * 8)
+    return int(state + work)
+
+
+def admissible(queue, now, used, budget, size=estimate_bytes):
+    """How many requests at the head of the arrival-ordered queue can be
+    admitted at time `now` with `used` bytes in use (first come, first served:
+    a request that does not fit blocks the ones behind it)."""
+    k = 0
+    for req in queue:
+        if req.arrival > now or used + size(req) > budget:
+            break
+        used += size(req)
+        k += 1
+    return k
+
+
+class Server:
+    """Continuous batching under an HBM budget (bytes)."""
+
+    def __init__(self, device="cuda", hbm_budget=150e9, streams=8, graphs=True):
+        import torch
+        self.device = device
+        self.budget = hbm_budget
+        self.pool = [torch.cuda.Stream() for _ in range(streams)]
+        self.graphs = graphs
+        self.used = 0          # bytes reserved by admitted requests
+        self.peak = 0
+        self.rounds = 0
+        self.over_estimate = 0.0  # max actual / reserved bytes of a request
+
+    def run(self, requests, clock=time.perf_counter):
+        import torch
+        queue = sorted(requests, key=lambda r: r.arrival)
+        active, finishing = [], []
+        t0 = clock()
+        prev_round, next_stream = [], 0
+        while queue or active or finishing:
+            now = clock() - t0
+            # admission in arrival order while the budget allows
+            while queue and admissible(queue[:1], now, self.used, self.budget):
+                req = queue.pop(0)
+                inst = Instance(req, self.device, self.pool[next_stream % len(self.pool)], self.graphs)
+                next_stream += 1
+                req.admitted = clock() - t0
+                inst.reserved = estimate_bytes(req)
+                self.over_estimate = max(self.over_estimate, inst.bytes / inst.reserved)
+                self.used += inst.reserved
+                self.peak = max(self.peak, self.used)
+                active.append(inst)
+            # retire requests whose last step completed
+            for inst in list(finishing):
+                if inst.done_event.query():
+                    inst.finish()
+                    inst.req.done = clock() - t0
+                    self.used -= inst.reserved
+                    finishing.remove(inst)
+            if not active:
+                if finishing:
+                    time.sleep(1e-4)
+                elif queue:
+                    time.sleep(max(0.0, min(queue[0].arrival - (clock() - t0), 0.01)))
+                continue
+            # one round: a step of every active request
+            for ev in prev_round:
+                ev.synchronize()
+            cur = []
+            for inst in active:
+                inst.step()
+                ev = torch.cuda.Event()
+                ev.record(inst.stream)
+                cur.append(ev)
+                if inst.remaining == 0:
+                    inst.done_event = ev
+                    finishing.append(inst)
+            active = [i for i in active if i.remaining > 0]
+            prev_round = cur
+            self.rounds += 1
+        torch.cuda.synchronize()
+        return requests
+
+
+def run_plain(requests, device="cuda", clock=time.perf_counter):
+    """The plain drop-in per request, in arrival order, one at a time."""
+    import torch
+    t0 = clock()
+    for req in sorted(requests, key=lambda r: r.arrival):
+        now = clock() - t0
+        if req.arrival > now:
+            time.sleep(req.arrival - now)
+        host = host_fluid(req)
+        eos = host.meta["eos"]
+        chem = eos == abi.HTR_EOS_AIRMIX
+        l = runtime.lib()
+        m = workloads.make_mixture_struct(l, eos, host.meta["mix"])
+        gh = runtime.load_mixture(eos, m)
+        dev = host.to_device(device)
+        workloads.derive_state(l, dev, gh, runtime.stream_handle())
+        dt = runtime.stable_dt(dev, gh, chemistry=chem)
+        req.admitted = clock() - t0
+        inner = dev.interior(host.meta.get("bnum", (0, 0, 0)))
+        for _ in range(req.steps):
+            runtime.rk3_step(dev, gh, dt=dt, chemistry=chem, fused=False, interior=inner)
+        req.result = dev["Conserved"].cpu().numpy()
+        req.done = clock() - t0
+        del dev
+    torch.cuda.synchronize()
+    return requests
+
+
+def summary(requests, elapsed):
+    tts = np.array([r.tts for r in requests])
+    return {"solves_per_s": len(requests) / elapsed, "tts_p50_s": float(np.percentile(tts, 50)),
+            "tts_p99_s": float(np.percentile(tts, 99)), "elapsed_s": elapsed, "requests": len(requests)}

@@ -18,6 +18,8 @@ Workloads:
                  Dirichlet(1)-distributed mass fractions varying smoothly in
                  space, velocities of local Mach 0.5-3 built from random
                  solenoidal plus compressive modes.
+  vortex2d       2-D periodic isentropic vortex on a uniform stream.
+(1-D shock tubes: see tubes.py.)
 """
 import math
 
@@ -154,6 +156,40 @@ def air_box(n=256, seed=0, shape=None, mach=(0.5, 3.0), T=(300.0, 8000.0), p_bar
     _uniform_metrics(fl, dx, dy, dz)
     fl.meta = dict(workload="air_box", eos=abi.HTR_EOS_AIRMIX, seed=seed, mix=dict(ref),
                    periodic=(True, True, True), bnum=(0, 0, 0), vorticityScale=1.0, cfl=0.8)
+    return fl
+
+
+def vortex2d(n=128, seed=0, shape=None, strength=None, mach=None, width=10.0):
+    """2-D periodic isentropic vortex advected by a uniform stream (single-
+    species gas, gamma 1.4, R 1, Pr 0.71, constant viscosity 1e-4): the
+    vortex-advection case of the served mix (seeded strength in 0.1-5 and
+    stream Mach number in 0.3-2 unless given).  nz = 1."""
+    nx, ny = shape if shape is not None else (n, n)
+    rng = np.random.Generator(np.random.PCG64(seed))
+    beta = strength if strength is not None else rng.uniform(0.1, 5.0)
+    M = mach if mach is not None else rng.uniform(0.3, 2.0)
+    gamma = 1.4
+    xc, dx = _centers(nx, width)
+    yc, dy = _centers(ny, width)
+    Y, X = np.meshgrid(yc, xc, indexing="ij")
+    r2 = (X - 0.5 * width) ** 2 + (Y - 0.5 * width) ** 2
+    f = np.exp(0.5 * (1.0 - r2))
+    u = M + beta / (2 * math.pi) * -(Y - 0.5 * width) * f
+    v = beta / (2 * math.pi) * (X - 0.5 * width) * f
+    T = 1.0 - (gamma - 1.0) * beta * beta / (8.0 * gamma * math.pi ** 2) * f * f
+    rho = T ** (1.0 / (gamma - 1.0))
+    p = rho * T / gamma  # free stream: rho 1, a 1
+    fl = Fluid((nx, ny, 1), 1)
+    fl["pressure"] = p[None]
+    fl["temperature"] = (p / rho)[None]
+    fl["MolarFracs"] = 1.0
+    fl["velocity"] = np.stack([u, v, np.zeros_like(u)], axis=-1)[None]
+    _uniform_metrics(fl, dx, dy, 1.0)
+    fl.meta = dict(workload="vortex2d", eos=abi.HTR_EOS_CONSTPROPMIX, seed=seed,
+                   mix=dict(gasConstant=1.0, gamma=gamma, prandtl=0.71, viscosityModel=abi.HTR_VISC_CONSTANT,
+                            p0=1e-4, p1=0.0, p2=0.0),
+                   periodic=(True, True, True), bnum=(0, 0, 0), vorticityScale=1.0, cfl=0.8,
+                   strength=beta, mach=M)
     return fl
 
 
