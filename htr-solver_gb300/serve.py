@@ -122,19 +122,33 @@ class Instance:
         self.graph = None
 
 
-def estimate_bytes(req):
-    """Device bytes of a request before admission (state + workspace)."""
+def _grid(req):
+    """(nx, ny, nz, nspec) of a request's grid."""
     if req.kind == "tube":
-        cells, neq = req.size + 2, 9
-    elif req.kind == "vortex":
-        cells, neq = req.size ** 2, 5
-    else:
-        cells, neq = req.size ** 3, 9
-    nsp = neq - 4
-    state = cells * 8 * (12 + 3 * 3 + 3 * neq + 3 * nsp + 4 + 1) + cells * (3 * 4 + 3)
-    faces = 3 * (cells + cells ** (2 / 3 if req.kind == "box" else 0.5))
-    work = int(2 * faces * neq * 8 + faces * 16 + 11 * cells * 8)
-    return int(state + work)
+        return req.size + 2, 1, 1, (5 if tubes.instances(1, seed=req.seed, length=(req.size, req.size))[0]["eos"]
+                                    == abi.HTR_EOS_AIRMIX else 1)
+    if req.kind == "vortex":
+        return req.size, req.size, 1, 1
+    return req.size, req.size, req.size, 5
+
+
+def estimate_bytes(req):
+    """Device bytes a request holds while admitted: every field of its grid
+    plus the fused-step workspace (the layout of stage_workspace_bytes) and
+    the workspace's alignment slack."""
+    nx, ny, nz, nsp = _grid(req)
+    cells = nx * ny * nz
+    neq = nsp + 4
+    size = {"int32": 4, "float64": 8, "bool": 1}
+    state = 0
+    for _name, dt, comp in abi.FIELD_SPECS:
+        c = {"nSpec": nsp, "nEq": neq}.get(comp, comp)
+        state += cells * int(c) * size[dt]
+    a256 = lambda b: (b + 255) // 256 * 256
+    n = (nx, ny, nz)
+    nf = [(n[0] + (d == 0)) * (n[1] + (d == 1)) * (n[2] + (d == 2)) for d in range(3)]
+    work = sum(2 * a256(8 * neq * f) for f in nf) + a256(16 * sum(nf)) + a256(4) + a256(8 * 11 * cells)
+    return int(state + work + 256)
 
 
 def admissible(queue, now, used, budget, size=estimate_bytes):
