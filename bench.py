@@ -347,13 +347,14 @@ def run_batched(args, device, runtime, lib, steps=3):
 
 def run_served(args, device):
     """Served mix: Poisson arrivals (200/s) of 1-D tubes (256-8192 cells), 2-D
-    vortex boxes (64^2-256^2) and 3-D reacting-air boxes (32^3-64^3); each asks
-    for 20-100 RK3 steps (the served configuration's 100-2000 scaled by 1/20
-    so the run stays bounded).  The server (continuous batching, per-request
-    CUDA graphs on 8 streams, 150 GB budget) against the plain per-request
-    path (one request at a time, task kernels)."""
-    mix = serve.request_mix(args.serve, rate=200.0, seed=777, steps=(20, 100), tube=(256, 8192),
-                            vortex=(64, 256), box=(32, 64))
+    vortex boxes (64^2-512^2) and 3-D reacting-air boxes (32^3-96^3), each
+    submitted with its initial state (generated before the session) and
+    asking for 20-100 RK3 steps (the served configuration's 100-2000 scaled by
+    1/20 so the run stays bounded).  The server (continuous batching,
+    per-request CUDA graphs on 8 streams, 150 GB budget) against the plain
+    per-request path (one request at a time, task kernels)."""
+    mix = serve.prepare(serve.request_mix(args.serve, rate=200.0, seed=777, steps=(20, 100), tube=(256, 8192),
+                                          vortex=(64, 512), box=(32, 96)))
     # warm the library, the allocator and the host-state generators
     warm = serve.request_mix(3, rate=1e6, seed=1, steps=(1, 1), tube=(64, 64), vortex=(16, 16), box=(8, 8))
     serve.Server(device=device, streams=2).run(warm)
@@ -362,7 +363,7 @@ def run_served(args, device):
     t0 = time.perf_counter()
     server.run(mix)
     t_srv = time.perf_counter() - t0
-    plain = [serve.Request(r.rid, r.kind, r.size, r.seed, r.steps, r.arrival) for r in mix]
+    plain = [serve.Request(r.rid, r.kind, r.size, r.seed, r.steps, r.arrival, state=r.state) for r in mix]
     t0 = time.perf_counter()
     serve.run_plain(plain, device=device)
     t_plain = time.perf_counter() - t0
@@ -376,10 +377,10 @@ def run_served(args, device):
             "speedup_vs_plain": t_plain / t_srv,
             "config": {"requests": len(mix), "arrival_rate_per_s": 200.0, "steps": [20, 100],
                        "kinds": {k: sum(r.kind == k for r in mix) for k in ("tube", "vortex", "box")},
-                       "sizes": {"tube": [256, 8192], "vortex": [64, 256], "box": [32, 64]},
-                       "note": "steps and the largest 2-D/3-D sizes scaled down from the served "
-                               "configuration to bound the run; state generation on the host is "
-                               "inside both timings"}}
+                       "sizes": {"tube": [256, 8192], "vortex": [64, 512], "box": [32, 96]},
+                       "note": "steps scaled by 1/20 from the served configuration to bound the run; "
+                               "each request carries its host initial state; both timings include "
+                               "H2D, state derivation, dt, the steps and the D2H of the result"}}
 
 
 def fp64_peak(lib):

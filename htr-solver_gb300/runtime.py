@@ -139,12 +139,13 @@ def stable_dt(fluid, mixh, cfl=0.8, chemistry=True, stream=None):
     abi.check(l, l.htr_CalculateMaxSpectralRadius(C.byref(v), fluid.interior(), mixh,
                                                   C.cast(C.c_void_p(out.data_ptr()), C.POINTER(C.c_double)), s),
               "htr_CalculateMaxSpectralRadius")
-    torch.cuda.synchronize()
+    st = stream if stream is not None else torch.cuda.current_stream()
+    st.synchronize()
     dt = cfl / out.item()
     if chemistry and fluid.nspec > 1:
         abi.check(l, l.htr_InitializeTimeDerivatives(C.byref(v), fluid.bounds(), 0, mixh, s), "init")
         abi.check(l, l.htr_AddChemistrySources(C.byref(v), fluid.interior(), mixh, s), "chem")
-        torch.cuda.synchronize()
+        st.synchronize()
         ns = fluid.nspec
         w = fluid["Conserved_t"][..., :ns].abs()
         rhoi = fluid["Conserved"][..., :ns]

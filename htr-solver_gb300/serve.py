@@ -38,6 +38,7 @@ class Request:
     admitted: float = None
     done: float = None
     result: object = None   # host copy of Conserved after the last step
+    state: object = None    # host Fluid submitted with the request (prepare())
 
     @property
     def tts(self):
@@ -60,7 +61,10 @@ def request_mix(n, rate, seed=0, steps=(100, 2000), tube=(256, 8192), vortex=(64
 
 
 def host_fluid(req):
-    """Seeded host state of a request (primitives, node types, metrics)."""
+    """Host state of a request (primitives, node types, metrics): the one it
+    was submitted with, else generated from its seed."""
+    if req.state is not None:
+        return req.state
     if req.kind == "tube":
         inst = tubes.instances(1, seed=req.seed, length=(req.size, req.size))[0]
         return tubes.tube_fluid(inst)
@@ -132,6 +136,15 @@ def _grid(req):
     return req.size, req.size, req.size, 5
 
 
+def prepare(requests):
+    """Generate every request's seeded initial state on the host, as a client
+    would submit it (outside any timed session)."""
+    for r in requests:
+        r.state = None
+        r.state = host_fluid(r)
+    return requests
+
+
 def estimate_bytes(req):
     """Device bytes a request holds while admitted: every field of its grid
     plus the fused-step workspace (the layout of stage_workspace_bytes) and
@@ -167,9 +180,10 @@ def admissible(queue, now, used, budget, size=estimate_bytes):
 class Server:
     """Continuous batching under an HBM budget (bytes)."""
 
-    def __init__(self, device="cuda", hbm_budget=150e9, streams=8, graphs=True):
+    def __init__(self, device="cuda", hbm_budget=150e9, streams=8, graphs=True, admit_per_round=2):
         import torch
         self.device = device
+        self.admit_per_round = admit_per_round  # admissions between rounds (keeps the device busy)
         self.budget = hbm_budget
         self.pool = [torch.cuda.Stream() for _ in range(streams)]
         self.graphs = graphs
@@ -187,7 +201,10 @@ class Server:
         while queue or active or finishing:
             now = clock() - t0
             # admission in arrival order while the budget allows
-            while queue and admissible(queue[:1], now, self.used, self.budget):
+            admitted_now = 0
+            while queue and admissible(queue[:1], now, self.used, self.budget) and \
+                    (admitted_now < self.admit_per_round or not active):
+                admitted_now += 1
                 req = queue.pop(0)
                 inst = Instance(req, self.device, self.pool[next_stream % len(self.pool)], self.graphs)
                 next_stream += 1
