@@ -63,6 +63,7 @@ FIELD_SPECS = [
     ("Conserved_t", "float64", "nEq"), ("Conserved_t_old", "float64", "nEq"),
     ("shockSensorX", "bool", 1), ("shockSensorY", "bool", 1), ("shockSensorZ", "bool", 1),
     ("DucrosSensor", "float64", 1),
+    ("dudtBoundary", "float64", 3), ("dTdtBoundary", "float64", 1),
 ]
 FIELD_NAMES = [f[0] for f in FIELD_SPECS]
 
@@ -170,6 +171,12 @@ for _d in "XYZ":
     PROTOTYPES[f"htr_UpdateUsingSkewSymmetricEulerFlux{_d}"] = [_V, _R, _R, _M, _S]
     PROTOTYPES[f"htr_UpdateUsingDiffusionFlux{_d}"] = [_V, _R, _R, _M, _S]
     PROTOTYPES[f"htr_UpdateShockSensor{_d}"] = [_V, _R, _R, _M, _S]
+
+
+for _side in ("XNeg", "XPos", "YNeg", "YPos", "ZNeg", "ZPos"):
+    PROTOTYPES[f"htr_UpdateUsingFluxNSCBCInflow{_side}"] = [_V, _R, _M, _S]
+    PROTOTYPES[f"htr_UpdateUsingFluxNSCBCOutflow{_side}"] = [_V, _R, _R, _M, C.c_double, C.c_double, C.c_double, _S]
+PROTOTYPES["htr_CalculateMaxMachNumber"] = [_V, _R, C.c_int, _P(C.c_double), _S]
 
 
 def bind(lib, extra=None):

@@ -479,6 +479,80 @@ int htr_UpdateVars(const htr_fluid_view *v, htr_rect3 my, int stage, double dt, 
 }
 
 // One SSP-RK3 time step of a periodic grid in the reference's driver order.
+}  // extern "C"
+
+namespace {
+
+int nscbc_common(const htr_fluid_view *v, htr_mixture_t m, const htr_rect3 &bc, int dir) {
+  if (int st = check_common(v, m, bc)) return st;
+  if (bc.lo[dir] != bc.hi[dir]) return fail(HTR_ERR_ARGUMENT, "the boundary region must be one plane thick%s");
+  HTR_REQ_D(*v, MassFracs);
+  HTR_REQ_D(*v, pressure);
+  HTR_REQ_D(*v, velocity);
+  HTR_REQ_D(*v, rho);
+  HTR_REQ_D(*v, SoS);
+  HTR_REQ_D(*v, temperature);
+  HTR_REQ_D(*v, Conserved_t);
+  if (int st = check_field(dirf(*v, dir, 0), 4, "nType")) return st;
+  if (int st = check_field(dirf(*v, dir, 2), 8, "m_d")) return st;
+  return HTR_OK;
+}
+
+int nscbc_inflow(const htr_fluid_view *v, htr_rect3 bc, htr_mixture_t m, int dir, bool minus, htr_stream_t s) {
+  if (int st = nscbc_common(v, m, bc, dir)) return st;
+  HTR_REQ_D(*v, dudtBoundary);
+  HTR_REQ_D(*v, dTdtBoundary);
+  return with_mix(m, [&](const auto &mix) {
+    return cuda_status(htr::launch_nscbc_inflow(*v, bc, mix, dir, minus, (cudaStream_t)s), "nscbc inflow");
+  });
+}
+
+int nscbc_outflow(const htr_fluid_view *v, htr_rect3 bc, htr_rect3 fb, htr_mixture_t m, int dir, bool minus,
+                  double MaxMach, double LengthScale, double PInf, htr_stream_t s) {
+  if (int st = nscbc_common(v, m, bc, dir)) return st;
+  if (!rect_ok(fb) || !inside(bc, fb)) return fail(HTR_ERR_ARGUMENT, "boundary plane outside the grid bounds%s");
+  HTR_REQ_D(*v, mu);
+  HTR_REQ_D(*v, Conserved);
+  for (int e = 0; e < 3; e++) {
+    if (int st = check_field(dirf(*v, e, 0), 4, "nType")) return st;
+    if (int st = check_field(dirf(*v, e, 2), 8, "m_d")) return st;
+  }
+  return with_mix(m, [&](const auto &mix) {
+    return cuda_status(htr::launch_nscbc_outflow(*v, bc, fb, mix, dir, minus, MaxMach, LengthScale, PInf,
+                                                 (cudaStream_t)s),
+                       "nscbc outflow");
+  });
+}
+
+}  // namespace
+
+extern "C" {
+
+#define HTR_NSCBC(SIDE, DIR, MINUS)                                                                           \
+  int htr_UpdateUsingFluxNSCBCInflow##SIDE(const htr_fluid_view *v, htr_rect3 bc, htr_mixture_t m,            \
+                                           htr_stream_t s) {                                                  \
+    return nscbc_inflow(v, bc, m, DIR, MINUS, s);                                                             \
+  }                                                                                                           \
+  int htr_UpdateUsingFluxNSCBCOutflow##SIDE(const htr_fluid_view *v, htr_rect3 bc, htr_rect3 fb, htr_mixture_t m, \
+                                            double MaxMach, double LengthScale, double PInf, htr_stream_t s) {  \
+    return nscbc_outflow(v, bc, fb, m, DIR, MINUS, MaxMach, LengthScale, PInf, s);                          \
+  }
+HTR_NSCBC(XNeg, 0, true)
+HTR_NSCBC(XPos, 0, false)
+HTR_NSCBC(YNeg, 1, true)
+HTR_NSCBC(YPos, 1, false)
+HTR_NSCBC(ZNeg, 2, true)
+HTR_NSCBC(ZPos, 2, false)
+#undef HTR_NSCBC
+
+int htr_CalculateMaxMachNumber(const htr_fluid_view *v, htr_rect3 my, int dir, double *result, htr_stream_t s) {
+  if (v == nullptr || result == nullptr || dir < 0 || dir > 2) return fail(HTR_ERR_ARGUMENT, "null argument or bad direction%s");
+  if (!rect_ok(my)) return fail(HTR_ERR_ARGUMENT, "inverted rectangle%s");
+  HTR_REQ_D(*v, velocity);
+  HTR_REQ_D(*v, SoS);
+  return cuda_status(htr::launch_max_mach(*v, my, dir, result, (cudaStream_t)s), "max mach");
+}
+
 int htr_rk3_step(const htr_fluid_view *v, htr_rect3 inner, htr_rect3 fb, const htr_step_params *p,
                  htr_mixture_t m, double *dt_used, int *status_dev, htr_stream_t s) {
   static const double RK[3][3] = {{1.0, 0.0, 1.0}, {3.0 / 4.0, 1.0 / 4.0, 1.0 / 4.0}, {1.0 / 3.0, 2.0 / 3.0, 2.0 / 3.0}};

@@ -43,6 +43,16 @@ template <class Mix>
 cudaError_t launch_update_chemistry(const htr_fluid_view &v, const htr_rect3 &my, double dt,
                                     const Mix &mix, int *status, cudaStream_t s);
 
+// NSCBC boundary terms on the plane `bc` (dir 0..2, minus = the "Neg" side)
+template <class Mix>
+cudaError_t launch_nscbc_inflow(const htr_fluid_view &v, const htr_rect3 &bc, const Mix &mix, int dir, bool minus,
+                                cudaStream_t s);
+template <class Mix>
+cudaError_t launch_nscbc_outflow(const htr_fluid_view &v, const htr_rect3 &bc, const htr_rect3 &fb, const Mix &mix,
+                                 int dir, bool minus, double MaxMach, double LengthScale, double PInf,
+                                 cudaStream_t s);
+cudaError_t launch_max_mach(const htr_fluid_view &v, const htr_rect3 &my, int dir, double *result, cudaStream_t s);
+
 // SSP-RK3 bookkeeping; neq = number of conserved components
 cudaError_t launch_copy_conserved(const htr_fluid_view &v, const htr_rect3 &my, int neq, cudaStream_t s);
 cudaError_t launch_init_rhs(const htr_fluid_view &v, const htr_rect3 &my, int neq, int implicit,

@@ -79,6 +79,7 @@ typedef struct {
   htr_field Conserved, Conserved_old, Conserved_t, Conserved_t_old; /* VecNEq */
   htr_field shockSensorX, shockSensorY, shockSensorZ;               /* bool */
   htr_field DucrosSensor;
+  htr_field dudtBoundary, dTdtBoundary;  /* Vec3, double: NSCBC inflow data */
 } htr_fluid_view;
 
 typedef struct htr_mixture_s *htr_mixture_t;
@@ -207,6 +208,45 @@ int htr_InitializeTimeDerivatives(const htr_fluid_view *view, htr_rect3 my_fluid
 /* stage in {1,2,3}: Conserved = C1*Conserved_old + C2*Conserved + C3*Conserved_t*dt. */
 int htr_UpdateVars(const htr_fluid_view *view, htr_rect3 my_fluid, int stage, double deltaTime,
                    int implicitChemistry, htr_mixture_t mix, htr_stream_t stream);
+
+/* --- NSCBC boundary terms (src/prometeo_rhs.hpp:476-719,
+ * src/prometeo_rhs.inl:1284-1629, src/prometeo_rhs.cc:531-900) -------------
+ * Add the LODI terms of a characteristic boundary to Conserved_t on the
+ * boundary plane `bc` (the task's BC region).  Inflow: species terms of a
+ * subsonic inlet whose velocity and temperature are imposed (dudtBoundary,
+ * dTdtBoundary); the RHS is zeroed at a supersonic inlet.  Outflow: partially
+ * non-reflecting outlet relaxed towards PInf with the maximum Mach number
+ * MaxMach of the normal velocity (htr_CalculateMaxMachNumber) and
+ * LengthScale; fluid_bounds bounds the tangential stencils. */
+int htr_UpdateUsingFluxNSCBCInflowXNeg(const htr_fluid_view *view, htr_rect3 bc, htr_mixture_t mix, htr_stream_t stream);
+int htr_UpdateUsingFluxNSCBCInflowXPos(const htr_fluid_view *view, htr_rect3 bc, htr_mixture_t mix, htr_stream_t stream);
+int htr_UpdateUsingFluxNSCBCInflowYNeg(const htr_fluid_view *view, htr_rect3 bc, htr_mixture_t mix, htr_stream_t stream);
+int htr_UpdateUsingFluxNSCBCInflowYPos(const htr_fluid_view *view, htr_rect3 bc, htr_mixture_t mix, htr_stream_t stream);
+int htr_UpdateUsingFluxNSCBCInflowZNeg(const htr_fluid_view *view, htr_rect3 bc, htr_mixture_t mix, htr_stream_t stream);
+int htr_UpdateUsingFluxNSCBCInflowZPos(const htr_fluid_view *view, htr_rect3 bc, htr_mixture_t mix, htr_stream_t stream);
+int htr_UpdateUsingFluxNSCBCOutflowXNeg(const htr_fluid_view *view, htr_rect3 bc, htr_rect3 fluid_bounds,
+                                        htr_mixture_t mix, double MaxMach, double LengthScale, double PInf,
+                                        htr_stream_t stream);
+int htr_UpdateUsingFluxNSCBCOutflowXPos(const htr_fluid_view *view, htr_rect3 bc, htr_rect3 fluid_bounds,
+                                        htr_mixture_t mix, double MaxMach, double LengthScale, double PInf,
+                                        htr_stream_t stream);
+int htr_UpdateUsingFluxNSCBCOutflowYNeg(const htr_fluid_view *view, htr_rect3 bc, htr_rect3 fluid_bounds,
+                                        htr_mixture_t mix, double MaxMach, double LengthScale, double PInf,
+                                        htr_stream_t stream);
+int htr_UpdateUsingFluxNSCBCOutflowYPos(const htr_fluid_view *view, htr_rect3 bc, htr_rect3 fluid_bounds,
+                                        htr_mixture_t mix, double MaxMach, double LengthScale, double PInf,
+                                        htr_stream_t stream);
+int htr_UpdateUsingFluxNSCBCOutflowZNeg(const htr_fluid_view *view, htr_rect3 bc, htr_rect3 fluid_bounds,
+                                        htr_mixture_t mix, double MaxMach, double LengthScale, double PInf,
+                                        htr_stream_t stream);
+int htr_UpdateUsingFluxNSCBCOutflowZPos(const htr_fluid_view *view, htr_rect3 bc, htr_rect3 fluid_bounds,
+                                        htr_mixture_t mix, double MaxMach, double LengthScale, double PInf,
+                                        htr_stream_t stream);
+/* max |velocity[dir]| / SoS over my_fluid (CalculateMaxMachNumber,
+ * src/prometeo_stat.rg:223-234); the result is written to *result (device
+ * pointer for the CUDA library, host pointer for the CPU oracle). */
+int htr_CalculateMaxMachNumber(const htr_fluid_view *view, htr_rect3 my_fluid, int dir, double *result,
+                               htr_stream_t stream);
 
 /* --- fused time step (the driver of src/prometeo.rg:1153-1172, 1342-1486) --
  * Not a reference task: one whole SSP-RK3 step of a periodic grid

@@ -95,3 +95,50 @@ HTR_REF_SKEW(htr_UpdateUsingSkewSymmetricEulerFluxZ, Zdir)
 HTR_REF_DIFF(htr_UpdateUsingDiffusionFluxX, Xdir)
 HTR_REF_DIFF(htr_UpdateUsingDiffusionFluxY, Ydir)
 HTR_REF_DIFF(htr_UpdateUsingDiffusionFluxZ, Zdir)
+
+// NSCBC boundary terms: the BC region (the boundary plane) is the index
+// space every region of the task is built on (the tasks iterate over it).
+namespace {
+template <class Task> int run_inflow(const htr_fluid_view *v, htr_rect3 bc, htr_mixture_t mix) {
+  if (!valid(v, mix, HTR_REF_EOS_ID)) return HTR_ERR_ARGUMENT;
+  const Rect<3> exec = to_rect(bc);
+  ArgsBuf<typename Task::Args> a(mix);
+  std::vector<Future> fut;
+  Runtime rt;
+  Task::cpu_base_impl(a.get(), regions(v, &exec, 3), fut, nullptr, &rt);
+  return HTR_OK;
+}
+template <class Task>
+int run_outflow(const htr_fluid_view *v, htr_rect3 bc, htr_rect3 fb, htr_mixture_t mix, double MaxMach,
+                double LengthScale, double PInf) {
+  if (!valid(v, mix, HTR_REF_EOS_ID)) return HTR_ERR_ARGUMENT;
+  const Rect<3> exec = to_rect(bc);
+  ArgsBuf<typename Task::Args> a(mix);
+  a.get().Fluid_bounds = to_rect(fb);
+  a.get().MaxMach = MaxMach;
+  a.get().LengthScale = LengthScale;
+  a.get().PInf = PInf;
+  std::vector<Future> fut{Future(MaxMach)};
+  Runtime rt;
+  Task::cpu_base_impl(a.get(), regions(v, &exec, 4), fut, nullptr, &rt);
+  return HTR_OK;
+}
+}  // namespace
+
+#define HTR_REF_NSCBC(SIDE, DIR, PM)                                                                      \
+  extern "C" int htr_UpdateUsingFluxNSCBCInflow##SIDE(const htr_fluid_view *v, htr_rect3 bc, htr_mixture_t m, \
+                                                      htr_stream_t) {                                     \
+    return run_inflow<UpdateUsingFluxNSCBCInflow##PM##SideTask<DIR>>(v, bc, m);                          \
+  }                                                                                                       \
+  extern "C" int htr_UpdateUsingFluxNSCBCOutflow##SIDE(const htr_fluid_view *v, htr_rect3 bc, htr_rect3 fb, \
+                                                       htr_mixture_t m, double MaxMach, double LS, double PInf, \
+                                                       htr_stream_t) {                                     \
+    return run_outflow<UpdateUsingFluxNSCBCOutflow##PM##SideTask<DIR>>(v, bc, fb, m, MaxMach, LS, PInf);  \
+  }
+HTR_REF_NSCBC(XNeg, Xdir, Minus)
+HTR_REF_NSCBC(XPos, Xdir, Plus)
+HTR_REF_NSCBC(YNeg, Ydir, Minus)
+HTR_REF_NSCBC(YPos, Ydir, Plus)
+HTR_REF_NSCBC(ZNeg, Zdir, Minus)
+HTR_REF_NSCBC(ZPos, Zdir, Plus)
+#undef HTR_REF_NSCBC

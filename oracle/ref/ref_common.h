@@ -71,6 +71,8 @@ inline Legion::PhysicalRegion make_region(const htr_fluid_view *v, const Legion:
   bind(r, FID_shockSensorY, v->shockSensorY);
   bind(r, FID_shockSensorZ, v->shockSensorZ);
   bind(r, FID_DucrosSensor, v->DucrosSensor);
+  bind(r, FID_dudtBoundary, v->dudtBoundary);
+  bind(r, FID_dTdtBoundary, v->dTdtBoundary);
   return r;
 }
 
