@@ -64,6 +64,9 @@ FIELD_SPECS = [
     ("shockSensorX", "bool", 1), ("shockSensorY", "bool", 1), ("shockSensorZ", "bool", 1),
     ("DucrosSensor", "float64", 1),
     ("dudtBoundary", "float64", 3), ("dTdtBoundary", "float64", 1),
+    ("velocity_old_NSCBC", "float64", 3), ("temperature_old_NSCBC", "float64", 1),
+    ("MolarFracs_profile", "float64", "nSpec"), ("velocity_profile", "float64", 3),
+    ("temperature_profile", "float64", 1),
 ]
 FIELD_NAMES = [f[0] for f in FIELD_SPECS]
 
@@ -177,6 +180,12 @@ for _side in ("XNeg", "XPos", "YNeg", "YPos", "ZNeg", "ZPos"):
     PROTOTYPES[f"htr_UpdateUsingFluxNSCBCInflow{_side}"] = [_V, _R, _M, _S]
     PROTOTYPES[f"htr_UpdateUsingFluxNSCBCOutflow{_side}"] = [_V, _R, _R, _M, C.c_double, C.c_double, C.c_double, _S]
 PROTOTYPES["htr_CalculateMaxMachNumber"] = [_V, _R, C.c_int, _P(C.c_double), _S]
+for _d in "XYZ":
+    PROTOTYPES[f"htr_SetNSCBC_InflowBC{_d}"] = [_V, _R, _M, C.c_double, _S]
+PROTOTYPES["htr_SetNSCBC_OutflowBC"] = [_V, _R, _M, _P(C.c_int), _S]
+PROTOTYPES["htr_SetIsothermalWallBC"] = [_V, _R, C.c_int, _M, _S]
+PROTOTYPES["htr_SetAdiabaticWallBC"] = [_V, _R, C.c_int, _M, _S]
+PROTOTYPES["htr_UpdateNSCBCGhostCellTimeDerivatives"] = [_V, _R, C.c_double, _S]
 
 
 def bind(lib, extra=None):

@@ -545,6 +545,71 @@ HTR_NSCBC(ZNeg, 2, true)
 HTR_NSCBC(ZPos, 2, false)
 #undef HTR_NSCBC
 
+static int inflow_state(const htr_fluid_view *v, htr_rect3 bc, htr_mixture_t m, double Pbc, int dir,
+                        htr_stream_t s) {
+  if (int st = check_common(v, m, bc)) return st;
+  HTR_REQ_D(*v, Conserved);
+  HTR_REQ_D(*v, SoS);
+  HTR_REQ_D(*v, MolarFracs_profile);
+  HTR_REQ_D(*v, temperature_profile);
+  HTR_REQ_D(*v, velocity_profile);
+  HTR_REQ_D(*v, pressure);
+  HTR_REQ_D(*v, temperature);
+  HTR_REQ_D(*v, MolarFracs);
+  HTR_REQ_D(*v, velocity);
+  return with_mix(m, [&](const auto &mix) {
+    return cuda_status(htr::launch_inflow_state(*v, bc, mix, Pbc, dir, (cudaStream_t)s), "nscbc inflow state");
+  });
+}
+int htr_SetNSCBC_InflowBCX(const htr_fluid_view *v, htr_rect3 bc, htr_mixture_t m, double Pbc, htr_stream_t s) {
+  return inflow_state(v, bc, m, Pbc, 0, s);
+}
+int htr_SetNSCBC_InflowBCY(const htr_fluid_view *v, htr_rect3 bc, htr_mixture_t m, double Pbc, htr_stream_t s) {
+  return inflow_state(v, bc, m, Pbc, 1, s);
+}
+int htr_SetNSCBC_InflowBCZ(const htr_fluid_view *v, htr_rect3 bc, htr_mixture_t m, double Pbc, htr_stream_t s) {
+  return inflow_state(v, bc, m, Pbc, 2, s);
+}
+int htr_SetNSCBC_OutflowBC(const htr_fluid_view *v, htr_rect3 bc, htr_mixture_t m, int *status_dev, htr_stream_t s) {
+  if (int st = check_common(v, m, bc)) return st;
+  HTR_REQ_D(*v, Conserved);
+  HTR_REQ_D(*v, temperature);
+  HTR_REQ_D(*v, pressure);
+  HTR_REQ_D(*v, MolarFracs);
+  HTR_REQ_D(*v, velocity);
+  return with_mix(m, [&](const auto &mix) {
+    return cuda_status(htr::launch_primitive(*v, bc, mix, status_dev, (cudaStream_t)s), "nscbc outflow state");
+  });
+}
+static int wall_state(const htr_fluid_view *v, htr_rect3 bc, int side, htr_mixture_t m, bool iso, htr_stream_t s) {
+  if (int st = check_common(v, m, bc)) return st;
+  if (side < 0 || side > 5) return fail(HTR_ERR_ARGUMENT, "side must be 0..5%s");
+  if (bc.lo[side / 2] != bc.hi[side / 2]) return fail(HTR_ERR_ARGUMENT, "the boundary region must be one plane thick%s");
+  HTR_REQ_D(*v, MolarFracs);
+  HTR_REQ_D(*v, pressure);
+  HTR_REQ_D(*v, temperature);
+  HTR_REQ_D(*v, velocity);
+  if (iso) HTR_REQ_D(*v, temperature_profile);
+  return cuda_status(htr::launch_wall_state(*v, bc, nspec_of(m), side, iso, (cudaStream_t)s), "wall state");
+}
+int htr_SetIsothermalWallBC(const htr_fluid_view *v, htr_rect3 bc, int side, htr_mixture_t m, htr_stream_t s) {
+  return wall_state(v, bc, side, m, true, s);
+}
+int htr_SetAdiabaticWallBC(const htr_fluid_view *v, htr_rect3 bc, int side, htr_mixture_t m, htr_stream_t s) {
+  return wall_state(v, bc, side, m, false, s);
+}
+int htr_UpdateNSCBCGhostCellTimeDerivatives(const htr_fluid_view *v, htr_rect3 bc, double dt, htr_stream_t s) {
+  if (v == nullptr || !rect_ok(bc)) return fail(HTR_ERR_ARGUMENT, "null view or inverted rectangle%s");
+  if (!(dt > 0.0)) return fail(HTR_ERR_ARGUMENT, "non-positive time step%s");
+  HTR_REQ_D(*v, velocity);
+  HTR_REQ_D(*v, temperature);
+  HTR_REQ_D(*v, dudtBoundary);
+  HTR_REQ_D(*v, dTdtBoundary);
+  HTR_REQ_D(*v, velocity_old_NSCBC);
+  HTR_REQ_D(*v, temperature_old_NSCBC);
+  return cuda_status(htr::launch_nscbc_time_derivatives(*v, bc, dt, (cudaStream_t)s), "nscbc time derivatives");
+}
+
 int htr_CalculateMaxMachNumber(const htr_fluid_view *v, htr_rect3 my, int dir, double *result, htr_stream_t s) {
   if (v == nullptr || result == nullptr || dir < 0 || dir > 2) return fail(HTR_ERR_ARGUMENT, "null argument or bad direction%s");
   if (!rect_ok(my)) return fail(HTR_ERR_ARGUMENT, "inverted rectangle%s");

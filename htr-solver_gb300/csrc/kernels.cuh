@@ -53,6 +53,14 @@ cudaError_t launch_nscbc_outflow(const htr_fluid_view &v, const htr_rect3 &bc, c
                                  cudaStream_t s);
 cudaError_t launch_max_mach(const htr_fluid_view &v, const htr_rect3 &my, int dir, double *result, cudaStream_t s);
 
+// boundary-point state updates (side: 0 XNeg .. 5 ZPos)
+template <class Mix>
+cudaError_t launch_inflow_state(const htr_fluid_view &v, const htr_rect3 &bc, const Mix &mix, double Pbc, int dir,
+                                cudaStream_t s);
+cudaError_t launch_wall_state(const htr_fluid_view &v, const htr_rect3 &bc, int nspec, int side, bool isothermal,
+                              cudaStream_t s);
+cudaError_t launch_nscbc_time_derivatives(const htr_fluid_view &v, const htr_rect3 &bc, double dt, cudaStream_t s);
+
 // SSP-RK3 bookkeeping; neq = number of conserved components
 cudaError_t launch_copy_conserved(const htr_fluid_view &v, const htr_rect3 &my, int neq, cudaStream_t s);
 cudaError_t launch_init_rhs(const htr_fluid_view &v, const htr_rect3 &my, int neq, int implicit,

@@ -80,6 +80,8 @@ typedef struct {
   htr_field shockSensorX, shockSensorY, shockSensorZ;               /* bool */
   htr_field DucrosSensor;
   htr_field dudtBoundary, dTdtBoundary;  /* Vec3, double: NSCBC inflow data */
+  htr_field velocity_old_NSCBC, temperature_old_NSCBC;  /* Vec3, double */
+  htr_field MolarFracs_profile, velocity_profile, temperature_profile; /* VecNSp, Vec3, double */
 } htr_fluid_view;
 
 typedef struct htr_mixture_s *htr_mixture_t;
@@ -242,6 +244,32 @@ int htr_UpdateUsingFluxNSCBCOutflowZNeg(const htr_fluid_view *view, htr_rect3 bc
 int htr_UpdateUsingFluxNSCBCOutflowZPos(const htr_fluid_view *view, htr_rect3 bc, htr_rect3 fluid_bounds,
                                         htr_mixture_t mix, double MaxMach, double LengthScale, double PInf,
                                         htr_stream_t stream);
+/* --- boundary-condition state updates --------------------------------------
+ * Primitive variables of the boundary points after each RK stage
+ * (UpdateGhostPrimitives, src/prometeo_bc.rg:1160-1279):
+ *   NSCBC inflow   SetNSCBC_InflowBCTask<dir> (src/prometeo_bc.hpp:108-150,
+ *                  src/prometeo_bc.cc:84-135): imposed profile; pressure from
+ *                  the advanced density unless the inflow is supersonic (Pbc)
+ *   NSCBC outflow  SetNSCBC_OutflowBCTask (src/prometeo_bc.cc:160-197):
+ *                  primitive recovery of the advanced boundary point
+ *   isothermal wall / adiabatic wall (src/prometeo_bc.rg:1207-1263): wall
+ *                  ghost at rest with the first interior point's pressure and
+ *                  composition, temperature from the wall profile / interior
+ * and the NSCBC time derivatives of the imposed inflow after a time step
+ * (UpdateNSCBCGhostCellTimeDerivatives, src/prometeo_bc.rg:1794-1810). */
+int htr_SetNSCBC_InflowBCX(const htr_fluid_view *view, htr_rect3 bc, htr_mixture_t mix, double Pbc, htr_stream_t stream);
+int htr_SetNSCBC_InflowBCY(const htr_fluid_view *view, htr_rect3 bc, htr_mixture_t mix, double Pbc, htr_stream_t stream);
+int htr_SetNSCBC_InflowBCZ(const htr_fluid_view *view, htr_rect3 bc, htr_mixture_t mix, double Pbc, htr_stream_t stream);
+int htr_SetNSCBC_OutflowBC(const htr_fluid_view *view, htr_rect3 bc, htr_mixture_t mix, int *status_dev,
+                           htr_stream_t stream);
+/* side: 0 XNeg, 1 XPos, 2 YNeg, 3 YPos, 4 ZNeg, 5 ZPos */
+int htr_SetIsothermalWallBC(const htr_fluid_view *view, htr_rect3 bc, int side, htr_mixture_t mix,
+                            htr_stream_t stream);
+int htr_SetAdiabaticWallBC(const htr_fluid_view *view, htr_rect3 bc, int side, htr_mixture_t mix,
+                           htr_stream_t stream);
+int htr_UpdateNSCBCGhostCellTimeDerivatives(const htr_fluid_view *view, htr_rect3 bc, double deltaTime,
+                                            htr_stream_t stream);
+
 /* max |velocity[dir]| / SoS over my_fluid (CalculateMaxMachNumber,
  * src/prometeo_stat.rg:223-234); the result is written to *result (device
  * pointer for the CUDA library, host pointer for the CPU oracle). */

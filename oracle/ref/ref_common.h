@@ -73,6 +73,11 @@ inline Legion::PhysicalRegion make_region(const htr_fluid_view *v, const Legion:
   bind(r, FID_DucrosSensor, v->DucrosSensor);
   bind(r, FID_dudtBoundary, v->dudtBoundary);
   bind(r, FID_dTdtBoundary, v->dTdtBoundary);
+  bind(r, FID_velocity_old_NSCBC, v->velocity_old_NSCBC);
+  bind(r, FID_temperature_old_NSCBC, v->temperature_old_NSCBC);
+  bind(r, FID_MolarFracs_profile, v->MolarFracs_profile);
+  bind(r, FID_velocity_profile, v->velocity_profile);
+  bind(r, FID_temperature_profile, v->temperature_profile);
   return r;
 }
 

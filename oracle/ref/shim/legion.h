@@ -18,6 +18,7 @@
 #include <map>
 #include <vector>
 #include <algorithm>
+#include <type_traits>
 
 namespace Realm {
 template <typename FT, int N, typename T> struct AffineAccessor {};
@@ -99,7 +100,12 @@ struct Future {
   double value = 0.0;
   Future() {}
   Future(double v) : value(v) {}
-  template <typename T> T get_result() const { return T(value); }
+  template <typename T> T get_result() const {
+    if constexpr (std::is_constructible_v<T, double>)
+      return T(value);
+    else
+      return T();  // results the harness never reads (e.g. averages)
+  }
 };
 
 template <typename T> struct DeferredValue {
@@ -173,9 +179,39 @@ template <typename T> class MinReduction {};
 template <typename REDOP, bool EXCLUSIVE, int N, typename T, typename A>
 class ReductionAccessor {
  public:
+  // reductions are never executed by the harness: folding into the proxy is a no-op
+  struct Ref {
+    template <typename V> const Ref &operator<<=(const V &) const { return *this; }
+  };
   ReductionAccessor() {}
   ReductionAccessor(const PhysicalRegion &, FieldID, int) {}
+  template <typename P> Ref operator[](const P &) const { return Ref(); }
 };
+static const int LEGION_REDOP_SUM_FLOAT64 = 0;
+
+// Compare-and-swap helpers named by the reference's reduction operators
+// (never executed by the harness: its tasks do not reduce).
+namespace TypePunning {
+template <typename T> struct Pointer {
+  void *p;
+  explicit Pointer(void *q) : p(q) {}
+  operator T *() const { return static_cast<T *>(p); }
+};
+template <typename A, typename B> struct Alias {
+  A a;
+  void load(const Pointer<A> &q) { a = *static_cast<A *>(q.p); }
+  A as_one() const { return a; }
+  B as_two() const {
+    B b;
+    std::memcpy(&b, &a, sizeof(b));
+    return b;
+  }
+  Alias &operator=(B b) {
+    std::memcpy(&a, &b, sizeof(a));
+    return *this;
+  }
+};
+}  // namespace TypePunning
 
 }  // namespace Legion
 
