@@ -286,6 +286,11 @@ def run_batched(args, device, runtime, lib, steps=3):
     cells = sum(s["dev"].ncells for s in strips)
     ws = runtime.Workspace()
     ws.get(max(runtime.workspace_bytes(s["dev"], s["gh"]) for s in strips), device)
+    # launch shapes for these strips (the arithmetic does not depend on them)
+    from htr_gb300 import autotune
+    default = autotune.get_tuning()
+    tuned, t_tuned, t_default, _ = autotune.autotune([(s["dev"], s["gh"], s["dt"], s["chem"]) for s in strips],
+                                                     workspace=ws)
 
     def step_all(st):
         for s in strips:
@@ -332,17 +337,20 @@ def run_batched(args, device, runtime, lib, steps=3):
     f1.synchronize()
     t_plain = f0.elapsed_time(f1)
     n = len(insts)
-    return {"metric": "batched solves/s", "unit": "tube RK3 steps/s", "tubes": n, "cells": int(cells),
+    out = {"metric": "batched solves/s", "unit": "tube RK3 steps/s", "tubes": n, "cells": int(cells),
             "value": n / (t_batched * 1e-3), "ms_per_step": t_batched,
             "cell_updates_per_s": 3.0 * cells / (t_batched * 1e-3),
             "plain": {"value": n / (t_plain * 1e-3), "ms_per_step": t_plain,
                       "cell_updates_per_s": 3.0 * cells / (t_plain * 1e-3),
                       "form": "htr_rk3_step looped over the tubes (task kernels, one tube per call)"},
             "speedup_vs_plain": t_plain / t_batched,
+            "autotune": {"tuning": tuned, "stage_ms_tuned": t_tuned, "stage_ms_default": t_default},
             "config": {"workload": f"{n} 1-D shock tubes, 128-8192 cells, gamma-1.4 gas or 5-species air "
                                    f"(1/2 each), staggered Dirichlet ends, hybrid scheme, SSP-RK3",
                        "form": "two strips (one per mixture), one CUDA graph per RK3 step",
                        "dt": {("air" if s["chem"] else "gas"): s["dt"] for s in strips}}}
+    autotune.set_tuning(default)
+    return out
 
 
 def run_served(args, device):

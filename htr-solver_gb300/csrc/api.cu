@@ -610,6 +610,33 @@ int htr_UpdateNSCBCGhostCellTimeDerivatives(const htr_fluid_view *v, htr_rect3 b
   return cuda_status(htr::launch_nscbc_time_derivatives(*v, bc, dt, (cudaStream_t)s), "nscbc time derivatives");
 }
 
+int htr_rk3_set_tuning(const htr_stage_tuning *t) {
+  if (t == nullptr) return fail(HTR_ERR_ARGUMENT, "null tuning%s");
+  auto pow2_in = [](int v, int lo, int hi) { return v >= lo && v <= hi && (v & (v - 1)) == 0; };
+  if (!pow2_in(t->prepass_block, 64, 256) || !pow2_in(t->diffusion_block, 32, 128) ||
+      !pow2_in(t->update_block, 32, 128) || t->teno_blocks_per_sm < 1 || t->teno_blocks_per_sm > 32 ||
+      !(t->kg_x_tile == 64 || t->kg_x_tile == 128 || t->kg_x_tile == 256))
+    return fail(HTR_ERR_ARGUMENT, "tuning value outside the supported set%s");
+  htr::StageTuning &g = htr::stage_tuning();
+  g.prepass_block = t->prepass_block;
+  g.diffusion_block = t->diffusion_block;
+  g.update_block = t->update_block;
+  g.teno_blocks_per_sm = t->teno_blocks_per_sm;
+  g.kg_x_tile = t->kg_x_tile;
+  return HTR_OK;
+}
+
+int htr_rk3_get_tuning(htr_stage_tuning *t) {
+  if (t == nullptr) return fail(HTR_ERR_ARGUMENT, "null tuning%s");
+  const htr::StageTuning &g = htr::stage_tuning();
+  t->prepass_block = g.prepass_block;
+  t->diffusion_block = g.diffusion_block;
+  t->update_block = g.update_block;
+  t->teno_blocks_per_sm = g.teno_blocks_per_sm;
+  t->kg_x_tile = g.kg_x_tile;
+  return HTR_OK;
+}
+
 int htr_CalculateMaxMachNumber(const htr_fluid_view *v, htr_rect3 my, int dir, double *result, htr_stream_t s) {
   if (v == nullptr || result == nullptr || dir < 0 || dir > 2) return fail(HTR_ERR_ARGUMENT, "null argument or bad direction%s");
   if (!rect_ok(my)) return fail(HTR_ERR_ARGUMENT, "inverted rectangle%s");

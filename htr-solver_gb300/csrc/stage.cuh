@@ -75,6 +75,17 @@ struct StageParams {
   unsigned active;
 };
 
+// Launch shapes of the fused stage (process-wide; set before launches or
+// graph captures that should use them).
+struct StageTuning {
+  int prepass_block = 256;      // threads per block, per-cell prepass (64..256)
+  int diffusion_block = 128;    // threads per block, diffusion faces (32..128)
+  int update_block = 128;       // threads per block, per-cell update (32..128)
+  int teno_blocks_per_sm = 8;   // grid of the TENO kernel
+  int kg_x_tile = 128;          // faces per x tile of the KG kernel (64, 128, 256)
+};
+StageTuning &stage_tuning();
+
 struct ConstPropDev;
 struct AirDev;
 

@@ -18,6 +18,11 @@ namespace htr {
 
 static size_t align256(size_t b) { return (b + 255) & ~size_t(255); }
 
+StageTuning &stage_tuning() {
+  static StageTuning t;
+  return t;
+}
+
 size_t stage_workspace_bytes(const htr_rect3 &r, int neq) {
   const FaceGrid g = face_grid(r);
   const long long ncell = (r.hi[0] - r.lo[0] + 1) * (r.hi[1] - r.lo[1] + 1) * (r.hi[2] - r.lo[2] + 1);
@@ -419,7 +424,8 @@ cudaError_t launch_stage(const htr_fluid_view &v, const htr_rect3 &my, const htr
     A.fb = box(fb);
     A.dn = dn;
     A.prep = prep;
-    stage_prepass<Mix><<<grid_for(n, 256), 256, 0, s>>>(A, mix);
+    const int pb = stage_tuning().prepass_block;
+    stage_prepass<Mix><<<grid_for(n, pb), pb, 0, s>>>(A, mix);
     if ((e = cudaGetLastError()) != cudaSuccess || (e = mark(1 + kPrepass)) != cudaSuccess) return e;
   }
   Fd<double> H;
@@ -455,10 +461,11 @@ cudaError_t launch_stage(const htr_fluid_view &v, const htr_rect3 &my, const htr
     A.prep = prep;
     A.g = g;
     A.fd = w.fd[D];
-    const dim3 gr = grid_for(g.nf[D], 128);
-    if (D == 0) diffusion_faces<Mix, 0><<<gr, 128, 0, s>>>(A, mix);
-    else if (D == 1) diffusion_faces<Mix, 1><<<gr, 128, 0, s>>>(A, mix);
-    else diffusion_faces<Mix, 2><<<gr, 128, 0, s>>>(A, mix);
+    const int db = stage_tuning().diffusion_block;
+    const dim3 gr = grid_for(g.nf[D], db);
+    if (D == 0) diffusion_faces<Mix, 0><<<gr, db, 0, s>>>(A, mix);
+    else if (D == 1) diffusion_faces<Mix, 1><<<gr, db, 0, s>>>(A, mix);
+    else diffusion_faces<Mix, 2><<<gr, db, 0, s>>>(A, mix);
     if ((e = cudaGetLastError()) != cudaSuccess || (e = mark(1 + kDiffZ + (2 - D))) != cudaSuccess) return e;
   }
   UpdateArgs U;
@@ -497,7 +504,8 @@ cudaError_t launch_stage(const htr_fluid_view &v, const htr_rect3 &my, const htr
   U.dt = sp.dt;
   U.chemistry = sp.chemistry;
   U.status = status;
-  stage_update<Mix><<<grid_for(n, 128), 128, 0, s>>>(U, mix);
+  const int ub = stage_tuning().update_block;
+  stage_update<Mix><<<grid_for(n, ub), ub, 0, s>>>(U, mix);
   if ((e = cudaGetLastError()) != cudaSuccess) return e;
   return mark(1 + kUpdate);
 }

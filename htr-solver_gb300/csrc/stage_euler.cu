@@ -162,7 +162,7 @@ cudaError_t launch_stage_euler(const htr_fluid_view &v, const htr_rect3 &my, con
   int dev = 0, sms = 152;
   cudaGetDevice(&dev);
   cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
-  dim3 grid((unsigned)(sms * 8));
+  dim3 grid((unsigned)(sms * stage_tuning().teno_blocks_per_sm));
   const int kind = (p.scheme == 2) ? p.kind : 0;
   if (kind == kTENO) euler_teno_faces<Mix, kTENO><<<grid, 128, 0, s>>>(T, mix);
   else if (kind == kTENOA) euler_teno_faces<Mix, kTENOA><<<grid, 128, 0, s>>>(T, mix);

@@ -16,21 +16,21 @@
 
 namespace htr {
 
-template <int D> struct KGTile {
+template <int D, int SX = 128> struct KGTile {
   static constexpr int L = (D == 0) ? 1 : 32;
-  static constexpr int S = (D == 0) ? 128 : 8;
+  static constexpr int S = (D == 0) ? SX : 8;
   static constexpr int WS = S + 6;
-  static constexpr int THREADS = (D == 0) ? 128 : 256;
+  static constexpr int THREADS = (D == 0) ? SX : 256;
 };
 
 HTR_D long long wrap_in(long long v, long long lo, long long size) {
   return ((v - lo) % size + size) % size + lo;
 }
 
-template <class Mix, int D, bool HYBRID>
-__global__ void __launch_bounds__(KGTile<D>::THREADS) euler_kg_faces(const StageEulerArgs A, const __grid_constant__ Mix mix) {
+template <class Mix, int D, bool HYBRID, int SX>
+__global__ void __launch_bounds__(KGTile<D, SX>::THREADS) euler_kg_faces(const StageEulerArgs A, const __grid_constant__ Mix mix) {
   constexpr int NS = Mix::NS, NE = NS + 4, iU = NS, iE = NS + 3;
-  constexpr int L = KGTile<D>::L, S = KGTile<D>::S, WS = KGTile<D>::WS;
+  constexpr int L = KGTile<D, SX>::L, S = KGTile<D, SX>::S, WS = KGTile<D, SX>::WS;
   extern __shared__ double win[];  // [NV][L*WS]
   __shared__ unsigned char sflag[L * WS];
   __shared__ signed char stype[L * WS];
@@ -215,16 +215,16 @@ __global__ void __launch_bounds__(KGTile<D>::THREADS) euler_kg_faces(const Stage
   }
 }
 
-template <class Mix, int D, bool HYBRID>
+template <class Mix, int D, bool HYBRID, int SX = 128>
 static cudaError_t kg_dir(const StageEulerArgs &A, const Mix &mix, cudaStream_t s) {
-  using TL = KGTile<D>;
+  using TL = KGTile<D, SX>;
   const long long n[3] = {A.e.my.size(0), A.e.my.size(1), A.e.my.size(2)};
   dim3 grid;
   if (D == 0) grid = dim3((unsigned)((n[0] + TL::S - 1) / TL::S), (unsigned)n[1], (unsigned)n[2]);
   else if (D == 1) grid = dim3((unsigned)((n[0] + TL::L - 1) / TL::L), (unsigned)((n[1] + TL::S - 1) / TL::S), (unsigned)n[2]);
   else grid = dim3((unsigned)((n[0] + TL::L - 1) / TL::L), (unsigned)n[1], (unsigned)((n[2] + TL::S - 1) / TL::S));
   const size_t sm = sizeof(double) * (Mix::NS + 6) * TL::L * TL::WS;
-  auto k = euler_kg_faces<Mix, D, HYBRID>;
+  auto k = euler_kg_faces<Mix, D, HYBRID, SX>;
   cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm);
   k<<<grid, TL::THREADS, sm, s>>>(A, mix);
   return cudaGetLastError();
@@ -232,7 +232,12 @@ static cudaError_t kg_dir(const StageEulerArgs &A, const Mix &mix, cudaStream_t 
 
 template <class Mix>
 cudaError_t launch_kg_faces(const StageEulerArgs &A, const Mix &mix, int D, bool hybrid, cudaStream_t s) {
-  if (D == 0) return hybrid ? kg_dir<Mix, 0, true>(A, mix, s) : kg_dir<Mix, 0, false>(A, mix, s);
+  if (D == 0) {
+    const int sx = stage_tuning().kg_x_tile;
+    if (sx == 64) return hybrid ? kg_dir<Mix, 0, true, 64>(A, mix, s) : kg_dir<Mix, 0, false, 64>(A, mix, s);
+    if (sx == 256) return hybrid ? kg_dir<Mix, 0, true, 256>(A, mix, s) : kg_dir<Mix, 0, false, 256>(A, mix, s);
+    return hybrid ? kg_dir<Mix, 0, true>(A, mix, s) : kg_dir<Mix, 0, false>(A, mix, s);
+  }
   if (D == 1) return hybrid ? kg_dir<Mix, 1, true>(A, mix, s) : kg_dir<Mix, 1, false>(A, mix, s);
   return hybrid ? kg_dir<Mix, 2, true>(A, mix, s) : kg_dir<Mix, 2, false>(A, mix, s);
 }

@@ -334,6 +334,17 @@ int htr_rk3_step_static(const htr_fluid_view *view, htr_rect3 interior, htr_rect
                         int *status_dev, htr_stream_t stream);
 size_t htr_rk3_static_scratch_bytes(void);
 
+/* Launch shapes of the fused stage, no counterpart in the reference
+ * (process-wide; chosen by the autotuner of the batched form).  Allowed:
+ * prepass_block 64/128/256, diffusion_block and update_block 32/64/128,
+ * teno_blocks_per_sm 1..32, kg_x_tile 64/128/256.  Defaults 256, 128, 128,
+ * 8, 128.  Set it before launching (or capturing) the steps that use it. */
+typedef struct {
+  int prepass_block, diffusion_block, update_block, teno_blocks_per_sm, kg_x_tile;
+} htr_stage_tuning;
+int htr_rk3_set_tuning(const htr_stage_tuning *tuning);
+int htr_rk3_get_tuning(htr_stage_tuning *tuning);
+
 /* Profiling aid, no counterpart in the reference: runs stage 1 of the fused
  * pipeline once (deltaTime, no sensor update) with CUDA events between its
  * kernels, waits for it, and writes the milliseconds of each kernel to
