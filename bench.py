@@ -44,6 +44,14 @@ BYTES_PER_CELL_UPDATE_AIR = 495
 MEASURED_PEAKS = os.path.join(ROOT, "MEASURED_PEAKS.json")
 
 
+_T0 = time.perf_counter()
+
+
+def log(msg):
+    """Progress of the run on stderr (the JSON line alone goes to stdout)."""
+    print(f"[bench {time.perf_counter() - _T0:7.1f}s] {msg}", file=sys.stderr, flush=True)
+
+
 def dist_env():
     ws = int(os.environ.get("WORLD_SIZE", "1"))
     rank = int(os.environ.get("RANK", "0"))
@@ -289,6 +297,7 @@ def run_batched(args, device, runtime, lib, steps=3):
     # launch shapes for these strips (the arithmetic does not depend on them)
     from htr_gb300 import autotune
     default = autotune.get_tuning()
+    log("batched: autotune")
     tuned, t_tuned, t_default, _ = autotune.autotune([(s["dev"], s["gh"], s["dt"], s["chem"]) for s in strips],
                                                      workspace=ws)
 
@@ -296,6 +305,7 @@ def run_batched(args, device, runtime, lib, steps=3):
         for s in strips:
             runtime.rk3_step(s["dev"], s["gh"], dt=s["dt"], chemistry=s["chem"], stream=st, workspace=ws)
 
+    log("batched: graph capture")
     side = torch.cuda.Stream()
     side.wait_stream(stream)
     with torch.cuda.stream(side):
@@ -328,6 +338,7 @@ def run_batched(args, device, runtime, lib, steps=3):
                 if st:
                     abi.check(lib, st, "htr_rk3_step")
 
+    log("batched: plain loop")
     loop_all()
     torch.cuda.synchronize()
     f0, f1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
@@ -367,10 +378,12 @@ def run_served(args, device):
     warm = serve.request_mix(3, rate=1e6, seed=1, steps=(1, 1), tube=(64, 64), vortex=(16, 16), box=(8, 8))
     serve.Server(device=device, streams=2).run(warm)
     serve.run_plain([serve.Request(r.rid, r.kind, r.size, r.seed, r.steps, 0.0) for r in warm], device=device)
+    log("served: server")
     server = serve.Server(device=device, hbm_budget=150e9, streams=8)
     t0 = time.perf_counter()
     server.run(mix)
     t_srv = time.perf_counter() - t0
+    log("served: plain path")
     plain = [serve.Request(r.rid, r.kind, r.size, r.seed, r.steps, r.arrival, state=r.state) for r in mix]
     t0 = time.perf_counter()
     serve.run_plain(plain, device=device)
@@ -410,6 +423,7 @@ def run_gpu(args):
     device = f"cuda:{local}"
     from htr_gb300 import runtime
     lib = runtime.lib()
+    log("building the state")
     dev, gh, mstruct = build_state(args.n, 1234 + rank, device, lib, runtime)
     ncell = dev.ncells
     dt = choose_dt(dev, gh, lib, runtime)
@@ -420,6 +434,7 @@ def run_gpu(args):
             torch.distributed.barrier()
         torch.cuda.synchronize()
 
+    log("warm-up")
     for _ in range(args.warmup):
         runtime.rk3_step(dev, gh, dt=dt, chemistry=True)
     barrier()
@@ -439,10 +454,12 @@ def run_gpu(args):
     # copies the time-dependent state host -> device, runs the step and reads
     # Conserved back.  Two device states alternate so that the copies of one
     # step overlap the compute of the previous one (copy streams + events).
+    log("end-to-end")
     e2e_value, h2d, d2h, e2e_steps = e2e_pipelined(dev, gh, dt, args.steps, runtime, barrier, device)
 
     result = None
     if rank == 0:
+        log("kernel profile")
         prof = kernel_profile(dev, gh, lib, runtime, dt)
         dominant = max(prof, key=prof.get)
         fdom = dominant.rsplit("_", 1)[0] if dominant[-2:] in ("_x", "_y", "_z") else dominant
@@ -478,15 +495,18 @@ def run_gpu(args):
         }
         if args.tubes > 0:
             try:
+                log("batched tubes")
                 result["batched"] = run_batched(args, device, runtime, lib)
             except Exception as exc:  # the headline line must still print
                 result["batched"] = {"error": f"{type(exc).__name__}: {exc}"}
         if args.serve > 0:
             try:
+                log("served mix")
                 result["served"] = run_served(args, device)
             except Exception as exc:
                 result["served"] = {"error": f"{type(exc).__name__}: {exc}"}
         if args.cpu_baseline:
+            log("CPU baseline")
             result["cpu_baseline"] = cpu_baseline(args.cpu_seconds)
     if ws > 1:
         torch.distributed.barrier()
