@@ -745,6 +745,10 @@ int htr_rk3_stage_profile(const htr_fluid_view *v, htr_rect3 inner, htr_rect3 fb
   sp.dt = p->deltaTime;
   sp.stage = 1;
   sp.active = active_dirs(inner);
+  // the profiled stage starts from the current state (Conserved_old =
+  // Conserved), so repeated profiles advance the state by forward-Euler
+  // stages instead of iterating stage 1 from an old step start
+  if (int st = cuda_status(htr::launch_copy_conserved(*v, fb, neq_of(m), (cudaStream_t)s), "profile start")) return st;
   cudaEvent_t ev[htr::kStageKernels + 1];
   int made = 0;
   cudaError_t e = cudaSuccess;
