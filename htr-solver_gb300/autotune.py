@@ -79,7 +79,9 @@ def stage_ms(grids, reps=3, workspace=None):
 
 def autotune(grids, reps=3, workspace=None, gain=0.01):
     """Coordinate descent over CANDIDATES; installs and returns (best tuning
-    as a dict, its stage ms, the default's stage ms, trials)."""
+    as a dict, its stage ms, the default's stage ms, trials).  Every timed
+    stage advances the grids it runs on (a forward-Euler stage with their dt):
+    pass copies of states that must not move."""
     best = get_tuning()
     stage_ms(grids, 1, workspace)  # warm-up
     t_best = t0 = stage_ms(grids, reps, workspace)
