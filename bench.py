@@ -298,11 +298,8 @@ def run_batched(args, device, runtime, lib, steps=3):
     from htr_gb300 import autotune
     default = autotune.get_tuning()
     log("batched: autotune")
-    # tune on copies: every trial advances the state it is timed on
-    copies = [dict(s, dev=s["dev"].copy()) for s in strips]
-    tuned, t_tuned, t_default, _ = autotune.autotune([(c["dev"], c["gh"], c["dt"], c["chem"]) for c in copies],
+    tuned, t_tuned, t_default, _ = autotune.autotune([(s["dev"], s["gh"], s["dt"], s["chem"]) for s in strips],
                                                      workspace=ws)
-    del copies
 
     def step_all(st):
         for s in strips:

@@ -3,9 +3,10 @@
 The batched and served forms run many grids of one shape family (long 1-D
 strips, small 3-D boxes) whose best launch shapes differ from the 256^3
 defaults.  `autotune` times candidate shapes of the fused stage
-(htr_rk3_stage_profile: per-kernel CUDA-event times of one stage) on the
-grids it is given and keeps the fastest, one parameter at a time (coordinate
-descent from the current setting), then installs it with htr_rk3_set_tuning.
+(htr_rk3_stage_profile: per-kernel CUDA-event times of one stage) on working
+copies of the grids it is given, every repetition restored from the same
+states, and keeps the fastest, one parameter at a time (coordinate descent
+from the current setting), then installs it with htr_rk3_set_tuning.
 The shapes change only how work is distributed, never the arithmetic, so a
 tuned run gives the same results bit for bit.
 """
@@ -56,19 +57,24 @@ def set_tuning(t):
     abi.check(l, l.htr_rk3_set_tuning(C.byref(t)), "htr_rk3_set_tuning")
 
 
-def stage_ms(grids, reps=3, workspace=None):
+def stage_ms(grids, reps=3, workspace=None, originals=None):
     """Sum over `grids` (fluid, mixture handle, dt, chemistry) of the median
-    stage time (sum of the stage's kernel times), in ms."""
+    stage time (sum of the stage's kernel times), in ms.  Each timed stage
+    advances its grid; with `originals` (fluids of the same shapes) every
+    repetition starts from a fresh copy of them."""
     l = _bind(runtime.lib())
     ws = workspace or runtime.Workspace()
     total = 0.0
-    for fl, gh, dt, chem in grids:
+    for k, (fl, gh, dt, chem) in enumerate(grids):
         v = fl.view()
         nb = runtime.workspace_bytes(fl, gh)
         ptr = ws.get(nb, fl.device)
         p = runtime.htr_step_params(runtime.SCHEMES["Hybrid"], 1.0, 0.0, dt, 1 if chem else 0)
         runs = []
         for _ in range(reps):
+            if originals is not None:
+                for name, a in fl.arrays.items():
+                    a.copy_(originals[k].arrays[name])
             out = (C.c_float * 9)()
             abi.check(l, l.htr_rk3_stage_profile(C.byref(v), fl.interior(), fl.bounds(), C.byref(p), gh,
                                                  C.c_void_p(ptr), nb, out, runtime.stream_handle()), "profile")
@@ -79,12 +85,14 @@ def stage_ms(grids, reps=3, workspace=None):
 
 def autotune(grids, reps=3, workspace=None, gain=0.01):
     """Coordinate descent over CANDIDATES; installs and returns (best tuning
-    as a dict, its stage ms, the default's stage ms, trials).  Every timed
-    stage advances the grids it runs on (a forward-Euler stage with their dt):
-    pass copies of states that must not move."""
+    as a dict, its stage ms, the default's stage ms, trials).  Trials run on
+    working copies of the grids, each repetition restored from the given
+    states, which are left untouched."""
+    work = [(fl.copy(), gh, dt, chem) for fl, gh, dt, chem in grids]
+    orig = [g[0] for g in grids]
     best = get_tuning()
-    stage_ms(grids, 1, workspace)  # warm-up
-    t_best = t0 = stage_ms(grids, reps, workspace)
+    stage_ms(work, 1, workspace, orig)  # warm-up
+    t_best = t0 = stage_ms(work, reps, workspace, orig)
     trials = [(best.as_dict(), t_best)]
     for name, values in CANDIDATES.items():
         for val in values:
@@ -93,9 +101,10 @@ def autotune(grids, reps=3, workspace=None, gain=0.01):
             trial = htr_stage_tuning(**best.as_dict())
             setattr(trial, name, val)
             set_tuning(trial)
-            t = stage_ms(grids, reps, workspace)
+            t = stage_ms(work, reps, workspace, orig)
             trials.append((trial.as_dict(), t))
             if t < t_best * (1.0 - gain):
                 best, t_best = trial, t
         set_tuning(best)
+    del work
     return best.as_dict(), t_best, t0, trials
