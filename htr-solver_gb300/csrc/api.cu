@@ -159,6 +159,10 @@ int static_scratch(void **out) {
   return HTR_OK;
 }
 
+long long ncells_of(const htr_rect3 &r) {
+  return (r.hi[0] - r.lo[0] + 1) * (r.hi[1] - r.lo[1] + 1) * (r.hi[2] - r.lo[2] + 1);
+}
+
 // Directions with more than one cell (a one-cell direction is periodic and
 // contributes nothing to the RHS).
 unsigned active_dirs(const htr_rect3 &r) {
@@ -250,6 +254,10 @@ int fused_step(const htr_fluid_view *v, htr_rect3 inner, htr_rect3 fb, const htr
   sp.chemistry = p->explicitChemistry ? 1 : 0;
   sp.dt = dt;
   sp.active = active_dirs(inner);
+  // the temperature cache of the update kernel starts empty every step
+  if (int st = cuda_status(cudaMemsetAsync(w.tcache, 0, sizeof(double) * 3 * ncells_of(inner), (cudaStream_t)s),
+                           "cache reset"))
+    return st;
   for (int stage = 1; stage <= 3; stage++) {
     sp.stage = stage;
     if (int st = with_mix(m, [&](const auto &mix) {
@@ -749,6 +757,9 @@ int htr_rk3_stage_profile(const htr_fluid_view *v, htr_rect3 inner, htr_rect3 fb
   // Conserved), so repeated profiles advance the state by forward-Euler
   // stages instead of iterating stage 1 from an old step start
   if (int st = cuda_status(htr::launch_copy_conserved(*v, fb, neq_of(m), (cudaStream_t)s), "profile start")) return st;
+  if (int st = cuda_status(cudaMemsetAsync(w.tcache, 0, sizeof(double) * 3 * ncells_of(inner), (cudaStream_t)s),
+                           "cache reset"))
+    return st;
   cudaEvent_t ev[htr::kStageKernels + 1];
   int made = 0;
   cudaError_t e = cudaSuccess;

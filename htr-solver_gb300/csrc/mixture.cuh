@@ -375,16 +375,33 @@ struct AirDev {
   // Newton for T from e (MultiComponent.inl:188-209: same tolerance, cap and
   // convergence test).  On return cpk holds the species c_p at the returned
   // temperature, Td = T * TRef and Tinv = 1 / Td.
+  // With `have`, Td = T * TRef, Tinv and logT = log(Td) of the initial T are
+  // supplied; later iterates take log T from the previous one through a
+  // log1p series when they moved by less than 2^-10 (|r|^7/7 < 1e-22).
   HTR_D double TFromInternalEnergyCp(double e0, double T, const double *Y, int *its, double *cpk,
-                                     double &Td, double &Tinv) const {
+                                     double &Td, double &Tinv, double &logT, bool have = false) const {
     const int MAXITS = 1000;
     const double TOL = 1e-8;
     double dfdT = 1.0, h[NS];
     int j = 0;
-    for (; j < MAXITS; j++) {
+    if (!have) {
       Td = T * TRef;
       Tinv = 1.0 / Td;
-      EnthalpyCp(Td, Tinv, log(Td), h, cpk);
+      logT = log(Td);
+    }
+    for (; j < MAXITS; j++) {
+      if (j > 0) {
+        const double Tn = T * TRef;
+        const double r = (Tn - Td) * Tinv;
+        if (fabs(r) < 0.0009765625) {
+          logT += r * (1.0 + r * (-0.5 + r * (1.0 / 3 + r * (-0.25 + r * (0.2 + r * (-1.0 / 6))))));
+        } else {
+          logT = log(Tn);
+        }
+        Td = Tn;
+        Tinv = 1.0 / Td;
+      }
+      EnthalpyCp(Td, Tinv, logT, h, cpk);
       double e = 0.0;
 #pragma unroll
       for (int i = 0; i < NS; i++) e += Y[i] * (h[i] - rOvW[i] * Td);
@@ -399,7 +416,8 @@ struct AirDev {
     if (j == MAXITS) {
       Td = T * TRef;
       Tinv = 1.0 / Td;
-      EnthalpyCp(Td, Tinv, log(Td), h, cpk);
+      logT = log(Td);
+      EnthalpyCp(Td, Tinv, logT, h, cpk);
     }
     if (its) *its = j;
     return T;
@@ -535,9 +553,13 @@ struct AirDev {
   // --- kinetics (Reaction.inl, MultiComponent.inl:370-415) ------------------
   HTR_D void ProductionRates(double *w, double rhon, double Pn, double Tn, const double *Y) const {
     const double T = Tn * TRef;
+    ProductionRatesT(w, rhon, Pn, T, 1.0 / T, log(T), Y);
+  }
+  // the same with T = Tn * TRef, 1/T and log T supplied by the caller
+  HTR_D void ProductionRatesT(double *w, double rhon, double Pn, double T, double Tinv, double logT,
+                              const double *Y) const {
     const double P = Pn * PRef;
     const double rho = rhon * rhoRef;
-    const double Tinv = 1.0 / T, logT = log(T);
     const double lnRP = log(kRGAS / P);
     double G[NS], C[NS];
 #pragma unroll

@@ -54,6 +54,7 @@ struct StageWorkspace {
   TenoEntry *queue; // capacity nf[0]+nf[1]+nf[2]
   unsigned *count;  // queue length
   double *prep;     // per-cell prepass values, [kPrepVals][ncell]
+  double *tcache;   // per cell: T it was computed for, log(T TRef), 1/(T TRef); [3][ncell]
 };
 
 // per-cell prepass values: velocity-gradient tensor (9), mixture molar

@@ -31,6 +31,7 @@ size_t stage_workspace_bytes(const htr_rect3 &r, int neq) {
   b += align256(sizeof(TenoEntry) * (g.nf[0] + g.nf[1] + g.nf[2]));
   b += align256(sizeof(unsigned));
   b += align256(sizeof(double) * kPrepVals * ncell);
+  b += align256(sizeof(double) * 3 * ncell);
   return b;
 }
 
@@ -49,6 +50,11 @@ bool stage_workspace_carve(void *base, size_t bytes, const htr_rect3 &r, int neq
   w.count = reinterpret_cast<unsigned *>(p);
   p += align256(sizeof(unsigned));
   w.prep = reinterpret_cast<double *>(p);
+  {
+    const long long ncell = (r.hi[0] - r.lo[0] + 1) * (r.hi[1] - r.lo[1] + 1) * (r.hi[2] - r.lo[2] + 1);
+    p += align256(sizeof(double) * kPrepVals * ncell);
+  }
+  w.tcache = reinterpret_cast<double *>(p);
   return true;
 }
 
@@ -238,6 +244,7 @@ struct UpdateArgs {
   double c1, c2, c3, dt;
   int chemistry;
   int *status;
+  double *tcache;  // [3][ncell]: T, log(T TRef), 1/(T TRef) of the last refresh
 };
 
 // Primitive recovery and property refresh of one cell from its new
@@ -245,7 +252,8 @@ struct UpdateArgs {
 // Air: the fused thermo/transport of the mixture (one Newton pass that also
 // yields the species c_p of the final temperature, batched inversions).
 template <class Mix>
-HTR_D void refresh_cell(const UpdateArgs &A, const Mix &mix, const long long *p, const double *u_) {
+HTR_D void refresh_cell(const UpdateArgs &A, const Mix &mix, const long long *p, const double *u_, long long i,
+                        double Td, double Tinv, double logT) {
   constexpr int NS = Mix::NS;
   double rhoYi[NS], Yi[NS], x[NS], vel[3], d[NS], y2[NS];
 #pragma unroll
@@ -266,8 +274,12 @@ HTR_D void refresh_cell(const UpdateArgs &A, const Mix &mix, const long long *p,
 #pragma unroll
     for (int k = 0; k < 3; k++) vel[k] = u_[NS + k] * rhoInv;
     const double e = u_[NS + 3] * rhoInv - 0.5 * mod2(vel);
-    double cpk[NS], Td, Tinv;
-    const double Tn = mix.TFromInternalEnergyCp(e, *A.T.at(p), Yi, &its, cpk, Td, Tinv);
+    double cpk[NS];
+    const double Tn = mix.TFromInternalEnergyCp(e, *A.T.at(p), Yi, &its, cpk, Td, Tinv, logT, true);
+    const long long n = A.dn.count();
+    A.tcache[i] = Tn;
+    A.tcache[n + i] = logT;
+    A.tcache[2 * n + i] = Tinv;
     const double Pn = rho * Tn * s / mix.iMixWRef;
     *A.T.at(p) = Tn;
     *A.P.at(p) = Pn;
@@ -351,11 +363,28 @@ __global__ void __launch_bounds__(128) stage_update(const UpdateArgs A, const __
       for (int k = 0; k < NE; k++) ctp[k] = 0.0;
       continue;
     }
+    // T, 1/T and log T of the current state: from the previous stage's
+    // refresh when it computed them for this very T, else evaluated here
+    double Td0 = 0.0, Tinv0 = 0.0, logT0 = 0.0;
+    if constexpr (NS > 1) {
+      const double Tn0 = *A.T.at(p);
+      Td0 = Tn0 * mix.TRef;
+      if (__double_as_longlong(A.tcache[i]) == __double_as_longlong(Tn0)) {
+        logT0 = A.tcache[n + i];
+        Tinv0 = A.tcache[2 * n + i];
+      } else {
+        Tinv0 = 1.0 / Td0;
+        logT0 = log(Td0);
+      }
+    }
     if (A.chemistry) {
       double y[NS], w[NS];
 #pragma unroll
       for (int k = 0; k < NS; k++) y[k] = ld(&A.Y.at(p)[k]);
-      mix.ProductionRates(w, ld(A.rho.at(p)), ld(A.P.at(p)), ld(A.T.at(p)), y);
+      if constexpr (NS > 1)
+        mix.ProductionRatesT(w, ld(A.rho.at(p)), ld(A.P.at(p)), Td0, Tinv0, logT0, y);
+      else
+        mix.ProductionRates(w, ld(A.rho.at(p)), ld(A.P.at(p)), ld(A.T.at(p)), y);
 #pragma unroll
       for (int k = 0; k < NS; k++) ct[k] = __dadd_rn(ct[k], w[k]);
     }
@@ -389,7 +418,7 @@ __global__ void __launch_bounds__(128) stage_update(const UpdateArgs A, const __
     }
     // primitive recovery (variables.hpp:163-193) and property refresh
     // (variables.hpp:62-89) of the new state
-    refresh_cell(A, mix, p, u_);
+    refresh_cell(A, mix, p, u_, i, Td0, Tinv0, logT0);
   }
 }
 
@@ -504,6 +533,7 @@ cudaError_t launch_stage(const htr_fluid_view &v, const htr_rect3 &my, const htr
   U.dt = sp.dt;
   U.chemistry = sp.chemistry;
   U.status = status;
+  U.tcache = w.tcache;
   const int ub = stage_tuning().update_block;
   stage_update<Mix><<<grid_for(n, ub), ub, 0, s>>>(U, mix);
   if ((e = cudaGetLastError()) != cudaSuccess) return e;
