@@ -404,6 +404,55 @@ def run_served(args, device):
                                "H2D, state derivation, dt, the steps and the D2H of the result"}}
 
 
+def run_wall(args, device, runtime, lib):
+    """Wall-bounded boundary layer: Mach-6 5-species air on a tanh-stretched
+    grid (interior cells --wall), NSCBC inflow / outflow in x, isothermal
+    wall and outflow in y, periodic z; TENO-LAD Euler flux, diffusion and
+    explicit chemistry.  Each SSP-RK3 step runs the task entry points in the
+    reference driver's order over the reference's zones (wall.BoundaryRun):
+    per stage 3 Euler + 3 diffusion + chemistry kernels, the NSCBC terms of
+    both outflows (with the interior's maximum Mach number, read back) and of
+    the inflow, the RK update and the boundary-state refresh."""
+    import torch
+    from htr_gb300 import wall
+    num = tuple(int(x) for x in args.wall.split(","))
+    host = wall.boundary_layer(num=num, seed=77)
+    g, bc = host.meta["grid"], host.meta["bc"]
+    m = workloads.make_mixture_struct(lib, host.meta["eos"], host.meta["mix"])
+    gh = runtime.load_mixture(host.meta["eos"], m)
+    dev = host.to_device(device)
+    del host
+    g.fill(dev, lib)
+    workloads.derive_state(lib, dev, gh, runtime.stream_handle())
+    mach = torch.zeros(1, dtype=torch.float64, device=device)
+    run = wall.BoundaryRun(lib, dev, gh, bc, stream=runtime.stream_handle(), max_mach_buffer=mach)
+    dt = run.spectral_dt(0.8)
+    run.step(dt)  # warm-up
+    torch.cuda.synchronize()
+    stream = torch.cuda.current_stream()
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    e0.record(stream)
+    for _ in range(args.wall_steps):
+        run.step(dt)
+    e1.record(stream)
+    torch.cuda.synchronize()
+    ms = e0.elapsed_time(e1)
+    cells = num[0] * num[1] * num[2]
+    finite = bool(torch.isfinite(dev["Conserved"]).all().item())
+    # kernels per stage: time derivatives, chemistry, 3 Euler, 3 diffusion,
+    # 2 x (max Mach), 2 outflow, 1 inflow, RK update, primitives, 3 boundary
+    # states, wall, properties, 4 boundary slabs of conserved variables
+    per_stage = 2 + 3 + 3 + 2 + 2 + 1 + 1 + 1 + 3 + 1 + 1 + len(run.all_bcs)
+    return {"value": 3.0 * cells * args.wall_steps / (ms * 1e-3), "unit": UNIT,
+            "ms_per_step": ms / args.wall_steps, "steps": args.wall_steps, "dt": dt, "finite": finite,
+            "config": {"workload": "Mach-6 boundary layer, 5-species air (AirMix), tanh-stretched wall-normal "
+                                   "grid, NSCBC inflow/outflow x, isothermal wall + outflow y, periodic z, "
+                                   "TENO-LAD + diffusion + explicit chemistry, SSP-RK3",
+                       "interior_cells": list(num), "grid_with_ghosts": list(g.shape), "cells": cells,
+                       "path": "task entry points in the reference driver's order"},
+            "gpu_launches": args.wall_steps * (3 * per_stage + 2)}
+
+
 def fp64_peak(lib):
     lib.htr_probe_fp64_tflops.argtypes = [C.c_int, C.POINTER(C.c_double)]
     lib.htr_probe_fp64_tflops.restype = C.c_int
@@ -505,6 +554,12 @@ def run_gpu(args):
                 result["served"] = run_served(args, device)
             except Exception as exc:
                 result["served"] = {"error": f"{type(exc).__name__}: {exc}"}
+        if args.wall:
+            try:
+                log("wall-bounded boundary layer")
+                result["wall"] = run_wall(args, device, runtime, lib)
+            except Exception as exc:
+                result["wall"] = {"error": f"{type(exc).__name__}: {exc}"}
         if args.cpu_baseline:
             log("CPU baseline")
             result["cpu_baseline"] = cpu_baseline(args.cpu_seconds)
@@ -579,6 +634,8 @@ def main():
     p.add_argument("--no-cpu-baseline", dest="cpu_baseline", action="store_false")
     p.add_argument("--tubes", type=int, default=4096, help="batched shock tubes (0: skip)")
     p.add_argument("--serve", type=int, default=32, help="served requests (0: skip)")
+    p.add_argument("--wall", default="512,192,128", help="boundary-layer interior cells nx,ny,nz ('' skips)")
+    p.add_argument("--wall-steps", type=int, default=10)
     args = p.parse_args()
     res = run_reference(args) if args.impl == "reference" else run_gpu(args)
     if res is not None:

@@ -186,6 +186,9 @@ PROTOTYPES["htr_SetNSCBC_OutflowBC"] = [_V, _R, _M, _P(C.c_int), _S]
 PROTOTYPES["htr_SetIsothermalWallBC"] = [_V, _R, C.c_int, _M, _S]
 PROTOTYPES["htr_SetAdiabaticWallBC"] = [_V, _R, C.c_int, _M, _S]
 PROTOTYPES["htr_UpdateNSCBCGhostCellTimeDerivatives"] = [_V, _R, C.c_double, _S]
+PROTOTYPES["htr_InitializeMetric"] = [_V, htr_field, _R, _R, _P(C.c_double), _S]
+for _d in "XYZ":
+    PROTOTYPES[f"htr_CorrectGhostMetric{_d}"] = [_V, htr_field, _R, _S]
 
 
 def bind(lib, extra=None):

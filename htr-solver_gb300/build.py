@@ -1,7 +1,8 @@
 """Builds libhtr_gb300.so (CUDA, sm_103a) in-tree under htr-solver_gb300/_build/.
 
 Translation units that evaluate TENO selections or shock sensors
-(euler.cu, sensor.cu) are compiled with -fmad=false so every floating-point
+(euler.cu, sensor.cu, stage_euler.cu) and the grid metrics (metric.cu)
+are compiled with -fmad=false so every floating-point
 operation is rounded exactly as the reference's CPU build rounds it; the
 others keep FMA contraction.
 """
@@ -16,7 +17,7 @@ OUT_DIR = os.path.join(HERE, "_build")
 LIB = os.path.join(OUT_DIR, "libhtr_gb300.so")
 
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
-EXACT_TUS = {"euler.cu", "sensor.cu", "stage_euler.cu"}
+EXACT_TUS = {"euler.cu", "sensor.cu", "stage_euler.cu", "metric.cu"}
 
 
 def nvcc():

@@ -645,6 +645,48 @@ int htr_rk3_get_tuning(htr_stage_tuning *t) {
   return HTR_OK;
 }
 
+static int check_metric_fields(const htr_fluid_view *v, const htr_field &cc) {
+  if (v == nullptr) return fail(HTR_ERR_ARGUMENT, "null view%s");
+  if (int st = check_field(cc, 8, "centerCoordinates")) return st;
+  HTR_REQ_I(*v, nType_x);
+  HTR_REQ_I(*v, nType_y);
+  HTR_REQ_I(*v, nType_z);
+  HTR_REQ_D(*v, dcsi_e);
+  HTR_REQ_D(*v, deta_e);
+  HTR_REQ_D(*v, dzet_e);
+  return HTR_OK;
+}
+
+int htr_InitializeMetric(const htr_fluid_view *v, htr_field cc, htr_rect3 my, htr_rect3 fb, const double width[3],
+                         htr_stream_t s) {
+  if (int st = check_metric_fields(v, cc)) return st;
+  if (width == nullptr) return fail(HTR_ERR_ARGUMENT, "null width%s");
+  if (!rect_ok(my) || !rect_ok(fb) || !inside(my, fb))
+    return fail(HTR_ERR_ARGUMENT, "execution rectangle outside the grid bounds%s");
+  HTR_REQ_D(*v, dcsi_d);
+  HTR_REQ_D(*v, deta_d);
+  HTR_REQ_D(*v, dzet_d);
+  HTR_REQ_D(*v, dcsi_s);
+  HTR_REQ_D(*v, deta_s);
+  HTR_REQ_D(*v, dzet_s);
+  return cuda_status(htr::launch_init_metric(*v, cc, my, fb, width, (cudaStream_t)s), "initialize metric");
+}
+
+static int correct_metric(const htr_fluid_view *v, const htr_field &cc, const htr_rect3 &my, int dir, htr_stream_t s) {
+  if (int st = check_metric_fields(v, cc)) return st;
+  if (!rect_ok(my)) return fail(HTR_ERR_ARGUMENT, "inverted execution rectangle%s");
+  return cuda_status(htr::launch_correct_metric(*v, cc, my, dir, (cudaStream_t)s), "correct ghost metric");
+}
+int htr_CorrectGhostMetricX(const htr_fluid_view *v, htr_field cc, htr_rect3 my, htr_stream_t s) {
+  return correct_metric(v, cc, my, 0, s);
+}
+int htr_CorrectGhostMetricY(const htr_fluid_view *v, htr_field cc, htr_rect3 my, htr_stream_t s) {
+  return correct_metric(v, cc, my, 1, s);
+}
+int htr_CorrectGhostMetricZ(const htr_fluid_view *v, htr_field cc, htr_rect3 my, htr_stream_t s) {
+  return correct_metric(v, cc, my, 2, s);
+}
+
 int htr_CalculateMaxMachNumber(const htr_fluid_view *v, htr_rect3 my, int dir, double *result, htr_stream_t s) {
   if (v == nullptr || result == nullptr || dir < 0 || dir > 2) return fail(HTR_ERR_ARGUMENT, "null argument or bad direction%s");
   if (!rect_ok(my)) return fail(HTR_ERR_ARGUMENT, "inverted rectangle%s");

@@ -18,6 +18,13 @@ template <class Mix>
 cudaError_t launch_diffusion(const htr_fluid_view &v, const htr_rect3 &my, const htr_rect3 &fb,
                              const Mix &mix, int dir, cudaStream_t s);
 
+// grid metrics (metric.cu): all three directions over my; Euler metric of the
+// boundary nodes of direction dir
+cudaError_t launch_init_metric(const htr_fluid_view &v, const htr_field &cc, const htr_rect3 &my,
+                               const htr_rect3 &fb, const double *width, cudaStream_t s);
+cudaError_t launch_correct_metric(const htr_fluid_view &v, const htr_field &cc, const htr_rect3 &my, int dir,
+                                  cudaStream_t s);
+
 cudaError_t launch_ducros(const htr_fluid_view &v, const htr_rect3 &my, const htr_rect3 &fb,
                           double vorticityScale, cudaStream_t s);
 // dirmask: bit d set = compute the sensor of direction d

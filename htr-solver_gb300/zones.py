@@ -1,0 +1,182 @@
+"""The reference's zone partitions of one grid tile, as lists of rectangles.
+
+Restates PartitionZones (src/prometeo_partitioner.rg:431-1015) for one tile
+covering the grid:
+
+  all         every point (p_All)
+  interior    points off the ghost layers (p_Interior)
+  all_bcs     all minus interior (p_AllBCs), as disjoint slabs
+  planes[s]   the boundary points of side s = 0 xNeg, 1 xPos, 2 yNeg, 3 yPos,
+              4 zNeg, 5 zPos (p_xNeg[0] ...): the side's face plus the edges
+              and corners it wins by the tie-break policies (walls, then
+              Dirichlet, then NSCBC inflow; outflow-like sides share edges;
+              src/prometeo_partitioner.rg:215-428, 530-733)
+  divg[d]     points where the flux divergence of direction d is applied
+              (p_x_divg ...) and `solved` the points whose RHS is computed
+              (p_solved): the interior plus the faces, edges and corners of
+              characteristic (NSCBC) boundaries in the other directions
+              (src/prometeo_partitioner.rg:745-975)
+
+The reference takes the z-side characteristic flags from the y sides' BC
+types (src/prometeo_partitioner.rg:782-783); with a periodic z axis, the case
+of every configuration here, the regions involved are empty.  The flag
+`z_flags_from_y` keeps that behaviour (default) or reads the z sides.
+"""
+from dataclasses import dataclass, field
+
+from . import abi
+from .grid import PERIODIC
+
+SIDES = ("xNeg", "xPos", "yNeg", "yPos", "zNeg", "zPos")
+WALL = {"AdiabaticWall", "IsothermalWall", "SuctionAndBlowingWall"}
+INFLOW_LIKE = {"NSCBC_Inflow", "RecycleRescaling"}
+OUTFLOW_LIKE = {"NSCBC_Outflow", "IncomingShock", "NSCBC_FarField"}
+NSCBC = {"NSCBC_Inflow", "NSCBC_Outflow", "NSCBC_FarField", "RecycleRescaling", "IncomingShock"}
+
+# region codes per axis: I interior, N negative ghosts, P positive ghosts
+REGIONS = ["III", "NII", "PII", "INI", "IPI", "IIN", "IIP",
+           "NNI", "NIN", "NPI", "NIP", "PNI", "PIN", "PPI", "PIP", "INN", "INP", "IPN", "IPP",
+           "NNN", "NPN", "NNP", "NPP", "PNN", "PPN", "PNP", "PPP"]
+
+
+def _range(code, n, b):
+    if code == "I":
+        return (b, n - 1 - b)
+    if code == "N":
+        return (0, b - 1)
+    return (n - b, n - 1)
+
+
+def _box(code, shape, bnum):
+    lo, hi = [], []
+    for c, n, b in zip(code, shape, bnum):
+        a, z = _range(c, n, b)
+        lo.append(a)
+        hi.append(z)
+    return tuple(lo), tuple(hi)
+
+
+def _empty(box):
+    lo, hi = box
+    return any(h < l for l, h in zip(lo, hi))
+
+
+def _side_of(code, d):
+    """Side index touched by a region code along axis d (None if interior)."""
+    return None if code[d] == "I" else 2 * d + (0 if code[d] == "N" else 1)
+
+
+def _winners(types):
+    """Sides (indices into `types`) that receive a shared edge or corner."""
+    for pred in (lambda t: t in WALL, lambda t: t == "Dirichlet", lambda t: t in INFLOW_LIKE):
+        for i, t in enumerate(types):
+            if pred(t):
+                return [i]
+    out = [i for i, t in enumerate(types) if t in OUTFLOW_LIKE]
+    if out:
+        return out
+    if all(t == PERIODIC for t in types):
+        return []
+    raise ValueError("unhandled tie break between " + ", ".join(types))
+
+
+@dataclass
+class Zones:
+    shape: tuple
+    bnum: tuple
+    all: tuple = None
+    interior: tuple = None
+    all_bcs: list = field(default_factory=list)
+    planes: list = field(default_factory=list)
+    divg: list = field(default_factory=list)
+    solved: list = field(default_factory=list)
+
+    @staticmethod
+    def rect(box):
+        return abi.rect(*box)
+
+
+def partition(shape, bnum, bc, z_flags_from_y=True):
+    """Zones of a grid of `shape` (with ghosts) whose axis d has `bnum[d]`
+    ghost layers per side and BC types bc[d] = (left, right)."""
+    types = [bc[0][0], bc[0][1], bc[1][0], bc[1][1], bc[2][0], bc[2][1]]
+    boxes = [_box(code, shape, bnum) for code in REGIONS]
+    z = Zones(tuple(shape), tuple(bnum))
+    z.all = ((0, 0, 0), tuple(n - 1 for n in shape))
+    z.interior = boxes[0]
+
+    # boundary planes with the tie-break policies
+    planes = [[] for _ in range(6)]
+    for k in range(1, 7):
+        if not _empty(boxes[k]):
+            planes[k - 1].append(boxes[k])
+    for k in range(7, 27):
+        if _empty(boxes[k]):
+            continue
+        code = REGIONS[k]
+        sides = [_side_of(code, d) for d in range(3) if code[d] != "I"]
+        # priority among the sides follows the direction order X, Y, Z
+        for w in _winners([types[s] for s in sides]):
+            planes[sides[w]].append(boxes[k])
+    z.planes = [_merge(p) for p in planes]
+
+    # divergence and solve regions
+    nscbc = [t in NSCBC for t in types]
+    if z_flags_from_y:
+        nscbc[4], nscbc[5] = types[2] in NSCBC, types[3] in NSCBC
+    divg = [[boxes[0]] for _ in range(3)]
+    solved = [boxes[0]]
+    for k in range(1, 7):
+        s = k - 1
+        if nscbc[s] and not _empty(boxes[k]):
+            for d in range(3):
+                if d != s // 2:
+                    divg[d].append(boxes[k])
+            solved.append(boxes[k])
+    for k in range(7, 19):
+        code = REGIONS[k]
+        ax = [d for d in range(3) if code[d] != "I"]
+        if _empty(boxes[k]) or not all(nscbc[_side_of(code, d)] for d in ax):
+            continue
+        free = [d for d in range(3) if code[d] == "I"][0]
+        divg[free].append(boxes[k])
+        solved.append(boxes[k])
+    z.divg = [_merge(r) for r in divg]
+    z.solved = _merge(solved)
+
+    # all minus interior as disjoint slabs: x ghosts, then y ghosts within the
+    # interior x range, then z ghosts within the interior x and y ranges
+    slabs = []
+    (ix0, iy0, iz0), (ix1, iy1, iz1) = boxes[0]
+    nx, ny, nz = shape
+    for lo, hi in (((0, 0, 0), (ix0 - 1, ny - 1, nz - 1)), ((ix1 + 1, 0, 0), (nx - 1, ny - 1, nz - 1)),
+                   ((ix0, 0, 0), (ix1, iy0 - 1, nz - 1)), ((ix0, iy1 + 1, 0), (ix1, ny - 1, nz - 1)),
+                   ((ix0, iy0, 0), (ix1, iy1, iz0 - 1)), ((ix0, iy0, iz1 + 1), (ix1, iy1, nz - 1))):
+        if not _empty((lo, hi)):
+            slabs.append((lo, hi))
+    z.all_bcs = slabs
+    return z
+
+
+def _merge(boxes):
+    """The union of disjoint boxes as one box when it is a rectangle (the
+    reference tasks take their region as one rectangle), else the list."""
+    boxes = [b for b in boxes if not _empty(b)]
+    if not boxes:
+        return []
+    lo = tuple(min(b[0][d] for b in boxes) for d in range(3))
+    hi = tuple(max(b[1][d] for b in boxes) for d in range(3))
+    size = 1
+    for d in range(3):
+        size *= hi[d] - lo[d] + 1
+    if sum(_count(b) for b in boxes) == size:
+        return [(lo, hi)]
+    return boxes
+
+
+def _count(box):
+    lo, hi = box
+    n = 1
+    for d in range(3):
+        n *= hi[d] - lo[d] + 1
+    return n

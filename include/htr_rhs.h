@@ -202,6 +202,25 @@ int htr_UpdatePrimitiveFromConserved(const htr_fluid_view *view, htr_rect3 my_fl
 int htr_CalculateMaxSpectralRadius(const htr_fluid_view *view, htr_rect3 my_fluid,
                                    htr_mixture_t mix, double *result_dev, htr_stream_t stream);
 
+/* --- grid metrics (set-up of a stretched grid) -----------------------------
+ * InitializeMetricTask (src/prometeo_metric.hpp:93-181,
+ * src/prometeo_metric.cc:36-178): the Euler (dcsi_e, deta_e, dzet_e),
+ * collocated diffusion (d*_d) and staggered (d*_s) metrics of every point of
+ * my_fluid from the cell-centre coordinates (Vec3 per point) and the node
+ * types; width[3] are the domain widths (bBox extents) used to unwarp
+ * periodic stencils.  CorrectGhostMetricTask<dir> (src/prometeo_metric.hpp:
+ * 183-268, src/prometeo_metric.cc:180-213): the Euler metric of direction
+ * dir at the boundary nodes (L_S, L_C, R_S, R_C) of my_fluid from one-sided
+ * coordinate differences.  Both write only metric fields. */
+int htr_InitializeMetric(const htr_fluid_view *view, htr_field centerCoordinates, htr_rect3 my_fluid,
+                         htr_rect3 fluid_bounds, const double width[3], htr_stream_t stream);
+int htr_CorrectGhostMetricX(const htr_fluid_view *view, htr_field centerCoordinates, htr_rect3 my_fluid,
+                            htr_stream_t stream);
+int htr_CorrectGhostMetricY(const htr_fluid_view *view, htr_field centerCoordinates, htr_rect3 my_fluid,
+                            htr_stream_t stream);
+int htr_CorrectGhostMetricZ(const htr_fluid_view *view, htr_field centerCoordinates, htr_rect3 my_fluid,
+                            htr_stream_t stream);
+
 /* --- SSP-RK3 bookkeeping (Regent tasks of src/prometeo_rk.rg:47-112) ---- */
 int htr_InitializeTemporaries(const htr_fluid_view *view, htr_rect3 my_fluid,
                               htr_mixture_t mix, htr_stream_t stream);

@@ -159,3 +159,70 @@ def step(lib, fl, mixh, scheme="Hybrid", vorticity_scale=1.0, cfl=0.8, dt=None, 
         A.check(lib, lib.htr_UpdateVars(C.byref(v), fl.interior(bnum), s, dt, 0, mixh, None), "rk")
         refresh(lib, fl, mixh, bnum)
     return dt
+
+
+def boundary_layer_zones(nx, ny, nz):
+    """Zones of a one-tile grid (one ghost layer in x and y, periodic z) with
+    an NSCBC inflow at xNeg, NSCBC outflows at xPos and yPos and a wall at
+    yNeg, written out by hand from PartitionZones
+    (src/prometeo_partitioner.rg:431-1015): the xNeg-yNeg and xPos-yNeg edges
+    go to the wall, xNeg-yPos to the inflow, xPos-yPos to both outflows; the
+    flux divergence of x skips the x planes, that of y skips the y planes;
+    the wall plane is not solved."""
+    X0, X1, Y0, Y1, Z1 = 0, nx - 1, 0, ny - 1, nz - 1
+    box = lambda x0, x1, y0, y1: ((x0, y0, 0), (x1, y1, Z1))
+    return dict(
+        all=box(X0, X1, Y0, Y1), interior=box(1, X1 - 1, 1, Y1 - 1), solved=box(X0, X1, 1, Y1),
+        divg=(box(1, X1 - 1, 1, Y1), box(X0, X1, 1, Y1 - 1), box(X0, X1, 1, Y1)),
+        xNeg=box(X0, X0, 1, Y1), xPos=box(X1, X1, 1, Y1), yNeg=box(X0, X1, Y0, Y0), yPos=box(1, X1, Y1, Y1),
+        all_bcs=(box(X0, X0, Y0, Y1), box(X1, X1, Y0, Y1), box(1, X1 - 1, Y0, Y0), box(1, X1 - 1, Y1, Y1)))
+
+
+def boundary_layer_step(lib, fl, mixh, dt, P_in, P_out, L_out, scheme="TENOLAD", regent=None, regent_mix=None):
+    """One SSP-RK3 step of a boundary-layer grid (zones above) in the
+    reference's order: MainLoopBody (src/prometeo.rg:1342-1486) with
+    UpdateDerivatives (:480-606), the NSCBC outflow terms of x then y with
+    the interior's maximum Mach number (src/prometeo_rhs.rg:672-765), the
+    inflow terms (:540-596), UpdatePrimitivesAndBCsFromConserved
+    (:428-478) with UpdateGhostPrimitives (src/prometeo_bc.rg:1445-1660) and
+    the inflow time derivatives (src/prometeo_bc.rg:1814-1879).  `regent`
+    provides the Regent-defined pieces (wall state, maximum Mach number,
+    NSCBC time derivatives) when `lib` lacks them, with its mixture handle
+    `regent_mix`; L_out = (LengthScale of the x outflow, of the y outflow)."""
+    A = _abi()
+    R = regent if regent is not None else lib
+    RM = regent_mix if regent is not None else mixh
+    z = boundary_layer_zones(fl.nx, fl.ny, fl.nz)
+    rc = lambda b: A.rect(*b)
+    v = fl.view()
+    fb = fl.bounds()
+    A.check(lib, lib.htr_InitializeTemporaries(C.byref(v), rc(z["all"]), mixh, None), "tmp")
+    for s in range(1, 4):
+        A.check(lib, lib.htr_InitializeTimeDerivatives(C.byref(v), rc(z["all"]), 0, mixh, None), "init_t")
+        A.check(lib, lib.htr_AddChemistrySources(C.byref(v), rc(z["solved"]), mixh, None), "chem")
+        rk = (C.c_double * 2)(RK_C[s - 1][0], RK_C[s - 1][1])
+        ddt = dt * RK_C[s - 1][2]
+        for d in (2, 1, 0):
+            fn = getattr(lib, f"htr_UpdateUsing{scheme}EulerFlux{'XYZ'[d]}")
+            A.check(lib, fn(C.byref(v), rc(z["divg"][d]), fb, rk, ddt, mixh, None), "euler")
+        for d in (2, 1, 0):
+            fn = getattr(lib, f"htr_UpdateUsingDiffusionFlux{'XYZ'[d]}")
+            A.check(lib, fn(C.byref(v), rc(z["divg"][d]), fb, mixh, None), "diffusion")
+        for d, side, L in ((0, "XPos", L_out[0]), (1, "YPos", L_out[1])):
+            mach = C.c_double(0.0)
+            A.check(R, R.htr_CalculateMaxMachNumber(C.byref(v), rc(z["interior"]), d, C.byref(mach), None), "mach")
+            fn = getattr(lib, f"htr_UpdateUsingFluxNSCBCOutflow{side}")
+            A.check(lib, fn(C.byref(v), rc(z[side[0].lower() + "Pos"]), fb, mixh, mach.value, L, P_out, None),
+                    "outflow")
+        A.check(lib, lib.htr_UpdateUsingFluxNSCBCInflowXNeg(C.byref(v), rc(z["xNeg"]), mixh, None), "inflow")
+        A.check(lib, lib.htr_UpdateVars(C.byref(v), rc(z["all"]), s, dt, 0, mixh, None), "rk")
+        A.check(lib, lib.htr_UpdatePrimitiveFromConserved(C.byref(v), rc(z["interior"]), mixh, None), "prim")
+        A.check(lib, lib.htr_SetNSCBC_InflowBCX(C.byref(v), rc(z["xNeg"]), mixh, P_in, None), "in bc")
+        A.check(lib, lib.htr_SetNSCBC_OutflowBC(C.byref(v), rc(z["xPos"]), mixh, None, None), "out bc x")
+        A.check(lib, lib.htr_SetNSCBC_OutflowBC(C.byref(v), rc(z["yPos"]), mixh, None, None), "out bc y")
+        A.check(R, R.htr_SetIsothermalWallBC(C.byref(v), rc(z["yNeg"]), 2, RM, None), "wall")
+        A.check(lib, lib.htr_UpdatePropertiesFromPrimitive(C.byref(v), rc(z["all"]), mixh, None), "props")
+        for b in z["all_bcs"]:
+            A.check(lib, lib.htr_UpdateConservedFromPrimitive(C.byref(v), rc(b), mixh, None), "cons")
+    A.check(R, R.htr_UpdateNSCBCGhostCellTimeDerivatives(C.byref(v), rc(z["xNeg"]), dt, None), "dudt")
+    return dt

@@ -44,6 +44,8 @@ template <typename T> struct Point<3, T> {
   T x, y, z;
   Point() : x(0), y(0), z(0) {}
   Point(T a, T b, T c) : x(a), y(b), z(c) {}
+  Point operator+(const Point &o) const { return Point(x + o.x, y + o.y, z + o.z); }
+  Point operator-(const Point &o) const { return Point(x - o.x, y - o.y, z - o.z); }
 };
 
 template <int N, typename T = coord_t> struct Rect {

@@ -1,0 +1,222 @@
+"""Grids with boundary conditions: zones, grid set-up, metrics and the
+time step of the wall-bounded boundary-layer workload.
+
+CPU:
+  - zones.partition against zones written out by hand from the reference's
+    partitioner for the boundary-layer BC set, and tie-break cases;
+  - node types and cell centres of stretched axes;
+  - the port's metrics against the reference's compiled InitializeMetric /
+    CorrectGhostMetric (bit for bit, where the reference sources exist);
+  - one SSP-RK3 step of the boundary layer: the library driver
+    (wall.BoundaryRun) on the port against the oracle's own step
+    (oracle.boundary_layer_step) on the reference's compiled tasks, and on
+    the port, bit for bit.
+GPU (-m gpu):
+  - metrics on the device against the port, bit for bit;
+  - one and two boundary-layer steps through the CUDA library against the
+    oracle step on the port, <= 1e-11 relative per conserved component.
+"""
+import ctypes as C
+
+import numpy as np
+import pytest
+
+from htr_gb300 import abi, grid, runtime, wall, workloads, zones
+
+import oracle
+from tests import util
+
+BL_BC = (("NSCBC_Inflow", "NSCBC_Outflow"), ("IsothermalWall", "NSCBC_Outflow"), ("Periodic", "Periodic"))
+METRICS = ("dcsi_e", "deta_e", "dzet_e", "dcsi_d", "deta_d", "dzet_d", "dcsi_s", "deta_s", "dzet_s")
+
+
+def _points(boxes):
+    pts = set()
+    for lo, hi in boxes:
+        for k in range(lo[2], hi[2] + 1):
+            for j in range(lo[1], hi[1] + 1):
+                for i in range(lo[0], hi[0] + 1):
+                    pts.add((i, j, k))
+    return pts
+
+
+@pytest.mark.parametrize("shape", [(8, 6, 3), (21, 14, 5)])
+def test_zones_match_hand_derived(shape):
+    z = zones.partition(shape, (1, 1, 0), BL_BC)
+    h = oracle.boundary_layer_zones(*shape)
+    assert z.all == h["all"] and z.interior == h["interior"]
+    assert _points(z.solved) == _points([h["solved"]])
+    for d in range(3):
+        assert _points(z.divg[d]) == _points([h["divg"][d]])
+    for s, name in enumerate(("xNeg", "xPos", "yNeg", "yPos")):
+        assert _points(z.planes[s]) == _points([h[name]]), name
+    assert not z.planes[4] and not z.planes[5]
+    assert _points(z.all_bcs) == _points([h["all"]]) - _points([h["interior"]])
+    assert _points(z.all_bcs) == _points(h["all_bcs"])
+
+
+def test_zones_periodic_and_walls():
+    per = zones.partition((6, 5, 4), (0, 0, 0), (("Periodic", "Periodic"),) * 3)
+    assert all(not p for p in per.planes) and not per.all_bcs
+    assert per.solved == [per.interior] and all(d == [per.interior] for d in per.divg)
+    walls = zones.partition((6, 5, 4), (1, 1, 1), (("IsothermalWall", "AdiabaticWall"),) * 3)
+    # walls everywhere: edges and corners go to x first, then y
+    x_neg = _points(walls.planes[0])
+    assert (0, 0, 0) in x_neg and (0, 4, 3) in x_neg
+    assert (1, 0, 0) in _points(walls.planes[2]) and (1, 0, 0) not in _points(walls.planes[4])
+    assert walls.solved == [walls.interior] and all(d == [walls.interior] for d in walls.divg)
+    out = zones.partition((6, 5, 4), (1, 1, 0), (("NSCBC_Outflow", "NSCBC_Outflow"),
+                                                 ("NSCBC_Outflow", "NSCBC_Outflow"), ("Periodic", "Periodic")))
+    # an outflow-outflow edge belongs to both sides and is solved
+    assert (5, 4, 0) in _points(out.planes[1]) and (5, 4, 0) in _points(out.planes[3])
+    assert (5, 4, 0) in _points(out.solved)
+    with pytest.raises(ValueError):
+        zones.partition((6, 5, 4), (1, 1, 0), (("Mystery", "Mystery"), ("Mystery", "Mystery"),
+                                               ("Periodic", "Periodic")))
+
+
+def test_node_types_and_centres():
+    g = grid.Grid((10, 8, 4), (1.0, 0.5, 0.25), BL_BC, kind=(("Uniform", 1.0), ("TanhMinus", 1.0), ("Uniform", 1.0)))
+    assert g.shape == (12, 10, 4) and g.bnum == (1, 1, 0)
+    assert list(g.ntype[0][:2]) == [grid.L_C, grid.LP1_C] and list(g.ntype[0][-3:]) == [grid.RM2_C, grid.RM1_C,
+                                                                                          grid.R_C]
+    assert list(g.ntype[1][:3]) == [grid.L_S, grid.LP1_S, grid.LP2_S]
+    assert list(g.ntype[1][-3:]) == [grid.RM2_C, grid.RM1_C, grid.R_C]
+    assert np.all(g.ntype[2] == grid.STD)
+    assert g.center[0][0] == pytest.approx(-0.05) and g.center[0][-1] == pytest.approx(1.05)
+    assert g.center[1][0] == 0.0  # staggered wall point on the wall
+    dy = np.diff(g.center[1][1:-1])
+    assert np.all(dy > 0) and dy[0] < dy[-1]  # clustered at the wall
+    assert np.all(np.diff(g.center[2]) == pytest.approx(0.0625))
+
+
+def _grid_fluid(bc, num, kind, width=(1.0, 0.6, 0.3)):
+    g = grid.Grid(num, width, bc, kind=kind)
+    return g, workloads.Fluid(g.shape, 1)
+
+
+GRIDS = [
+    (BL_BC, (12, 9, 4), (("Uniform", 1.0), ("TanhMinus", 1.0), ("Uniform", 1.0))),
+    ((("Periodic", "Periodic"),) * 3, (9, 7, 5), (("Tanh", 1.3), ("Cosine", 1.0), ("SinhPlus", 0.8))),
+    ((("IsothermalWall", "AdiabaticWall"), ("Dirichlet", "NSCBC_Outflow"), ("NSCBC_Inflow", "IsothermalWall")),
+     (7, 6, 5), (("TanhPlus", 2.0), ("Sinh", 1.5), ("SinhMinus", 1.1))),
+]
+
+
+@pytest.mark.parametrize("case", range(len(GRIDS)))
+def test_metric_port_matches_reference(case):
+    ref = oracle.ref_lib(1)
+    if ref is None:
+        pytest.skip("reference CPU build not present on this machine")
+    port = oracle.port_lib()
+    bc, num, kind = GRIDS[case]
+    outs = []
+    for lib in (ref, port):
+        g, fl = _grid_fluid(bc, num, kind)
+        g.fill(fl, lib)
+        outs.append(fl)
+    for name in METRICS:
+        assert np.array_equal(outs[0][name], outs[1][name]), name
+        assert np.all(np.isfinite(outs[1][name])), name
+
+
+def _bl(lib, num=(14, 10, 4), seed=3):
+    fl = wall.boundary_layer(num=num, seed=seed)
+    fl.meta["grid"].fill(fl, lib)
+    m = workloads.make_mixture_struct(lib, fl.meta["eos"], fl.meta["mix"])
+    h = oracle.load_mixture(lib, fl.meta["eos"], m)
+    workloads.derive_state(lib, fl, h)
+    return fl, h, m
+
+
+def _oracle_step(lib, fl, h, dt, regent=None, regent_mix=None):
+    bc = fl.meta["bc"]
+    oracle.boundary_layer_step(lib, fl, h, dt, bc["xNeg"][1]["P"], bc["xPos"][1]["P"],
+                               (bc["xPos"][1]["LengthScale"], bc["yPos"][1]["LengthScale"]),
+                               regent=regent, regent_mix=regent_mix)
+
+
+def test_boundary_layer_driver_matches_oracle_step():
+    port = oracle.port_lib()
+    a, ha, _ = _bl(port)
+    b, hb, _ = _bl(port)
+    run = wall.BoundaryRun(port, a, ha, a.meta["bc"])
+    dt = run.spectral_dt(0.8)
+    for n in range(2):
+        run.step(dt)
+        _oracle_step(port, b, hb, dt)
+        if n == 0:
+            # the inflow derivatives see the imposed profile replace the noisy start
+            assert np.any(a["dudtBoundary"][:, 1:, 0] != 0.0)
+    for name in a.arrays:
+        assert np.array_equal(a[name], b[name]), name
+    assert np.all(np.isfinite(a["Conserved"]))
+    assert np.array_equal(a["velocity_old_NSCBC"][:, 1:, 0], a["velocity"][:, 1:, 0])
+
+
+def test_boundary_layer_step_port_matches_reference():
+    ref = oracle.ref_lib(2)
+    if ref is None:
+        pytest.skip("reference CPU build not present on this machine")
+    port = oracle.port_lib()
+    a, ha, _ = _bl(port)
+    b, hb, _ = _bl(ref)
+    for name in a.arrays:
+        assert np.array_equal(a[name], b[name]), name
+    run = wall.BoundaryRun(port, a, ha, a.meta["bc"])
+    dt = run.spectral_dt(0.8)
+    run.step(dt)
+    _oracle_step(ref, b, hb, dt, regent=port, regent_mix=ha)
+    for name in a.arrays:
+        assert np.array_equal(a[name], b[name]), name
+
+
+def test_boundary_run_rejects_unsupported():
+    port = oracle.port_lib()
+    fl, h, _ = _bl(port, num=(6, 5, 3))
+    with pytest.raises(abi.HtrError):
+        wall.BoundaryRun(port, fl, h, fl.meta["bc"], scheme="Hybrid")
+    bc = dict(fl.meta["bc"])
+    bc["yPos"] = ("IncomingShock", {})
+    with pytest.raises(abi.HtrError):
+        wall.BoundaryRun(port, fl, h, bc)
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("case", range(len(GRIDS)))
+def test_gpu_metric_matches_port(case):
+    import torch
+    port = oracle.port_lib()
+    bc, num, kind = GRIDS[case]
+    g, host = _grid_fluid(bc, num, kind)
+    g.fill(host, port)
+    g2, dev = _grid_fluid(bc, num, kind)
+    dev = dev.to_device("cuda")
+    g2.fill(dev, runtime.lib())
+    torch.cuda.synchronize()
+    out = dev.to_host()
+    for name in METRICS:
+        assert np.array_equal(out[name], host[name]), name
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("steps", [1, 2])
+def test_gpu_boundary_layer_steps(steps):
+    import torch
+    port = oracle.port_lib()
+    host, hp, m = _bl(port, num=(24, 16, 6))
+    dev = host.to_device("cuda")
+    gh = runtime.load_mixture(host.meta["eos"], m)
+    mach = torch.zeros(1, dtype=torch.float64, device="cuda")
+    run = wall.BoundaryRun(runtime.lib(), dev, gh, host.meta["bc"], stream=runtime.stream_handle(),
+                           max_mach_buffer=mach)
+    dt = wall.BoundaryRun(port, host, hp, host.meta["bc"]).spectral_dt(0.8)
+    for _ in range(steps):
+        _oracle_step(port, host, hp, dt)
+        run.step(dt)
+    torch.cuda.synchronize()
+    out = dev.to_host()
+    err = util.rel_err(out["Conserved"], host["Conserved"])
+    assert err.max() <= util.RHS_REL_TOL, err
+    for name in ("temperature", "pressure", "velocity", "MolarFracs"):
+        assert util.rel_err(out[name], host[name]).max() <= util.RHS_REL_TOL, name
