@@ -754,6 +754,129 @@ int htr_rk3_step_ws(const htr_fluid_view *v, htr_rect3 inner, htr_rect3 fb, cons
   return fused_step(v, inner, fb, p, m, w, dt_used, status_dev, s);
 }
 
+static int check_bc_params(const htr_fluid_view *v, htr_rect3 inner, htr_rect3 fb, const htr_bc_params *bc) {
+  if (bc == nullptr) return fail(HTR_ERR_ARGUMENT, "null boundary parameters%s");
+  for (int d = 0; d < 3; d++) {
+    const int a = bc->type[2 * d], b = bc->type[2 * d + 1];
+    for (int t : {a, b})
+      if (t < HTR_BC_PERIODIC || t > HTR_BC_ADIABATIC_WALL) return fail(HTR_ERR_ARGUMENT, "unknown boundary type%s");
+    if ((a == HTR_BC_PERIODIC) != (b == HTR_BC_PERIODIC))
+      return fail(HTR_ERR_ARGUMENT, "a periodic direction is periodic on both sides%s");
+    const int g = (a == HTR_BC_PERIODIC) ? 0 : 1;
+    if (inner.lo[d] != fb.lo[d] + g || inner.hi[d] != fb.hi[d] - g || fb.hi[d] - fb.lo[d] < 4 * g)
+      return fail(HTR_ERR_ARGUMENT, "interior must be the bounds less one ghost layer on each non-periodic side%s");
+    for (int side = 2 * d; side < 2 * d + 2; side++) {
+      if (bc->type[side] == HTR_BC_PERIODIC) continue;
+      const htr_rect3 &r = bc->plane[side];
+      const int64_t at = (side % 2 == 0) ? fb.lo[d] : fb.hi[d];
+      if (!rect_ok(r) || !inside(r, fb) || r.lo[d] != at || r.hi[d] != at)
+        return fail(HTR_ERR_ARGUMENT, "a boundary plane is not the side's ghost layer%s");
+      if (bc->type[side] == HTR_BC_NSCBC_OUTFLOW && !(bc->LengthScale[side] > 0.0))
+        return fail(HTR_ERR_ARGUMENT, "outflow LengthScale must be positive%s");
+    }
+  }
+  bool inflow = false, iso = false;
+  for (int k = 0; k < 6; k++) {
+    inflow = inflow || bc->type[k] == HTR_BC_NSCBC_INFLOW;
+    iso = iso || bc->type[k] == HTR_BC_ISOTHERMAL_WALL;
+  }
+  if (inflow) {
+    HTR_REQ_D(*v, MolarFracs_profile);
+    HTR_REQ_D(*v, velocity_profile);
+    HTR_REQ_D(*v, temperature_profile);
+    HTR_REQ_D(*v, dudtBoundary);
+    HTR_REQ_D(*v, dTdtBoundary);
+    HTR_REQ_D(*v, velocity_old_NSCBC);
+    HTR_REQ_D(*v, temperature_old_NSCBC);
+  }
+  if (iso) HTR_REQ_D(*v, temperature_profile);
+  return HTR_OK;
+}
+
+int htr_rk3_step_bc_ws(const htr_fluid_view *v, htr_rect3 inner, htr_rect3 fb, const htr_step_params *p,
+                       const htr_bc_params *bc, htr_mixture_t m, void *workspace, size_t workspace_bytes,
+                       double *dt_used, int *status_dev, htr_stream_t s) {
+  int st;
+  if ((st = check_common(v, m, inner))) return st;
+  if ((st = check_step_fields(v, m))) return st;
+  if (p == nullptr) return fail(HTR_ERR_ARGUMENT, "null step parameters%s");
+  if (p->scheme == HTR_SCHEME_HYBRID)
+    return fail(HTR_ERR_UNSUPPORTED, "the boundary step runs the TENO, TENO-A, TENO-LAD and skew-symmetric schemes%s");
+  if (p->scheme < HTR_SCHEME_HYBRID || p->scheme > HTR_SCHEME_SKEW) return fail(HTR_ERR_ARGUMENT, "unknown scheme%s");
+  if ((st = check_bc_params(v, inner, fb, bc))) return st;
+  htr::StageWorkspace w;
+  if (!htr::stage_workspace_carve(workspace, workspace_bytes, fb, neq_of(m), w))
+    return fail(HTR_ERR_ARGUMENT, "workspace null or smaller than htr_rk3_workspace_bytes(fluid_bounds)%s");
+  if (reinterpret_cast<uintptr_t>(workspace) % 256 != 0) return fail(HTR_ERR_LAYOUT, "workspace not 256-byte aligned%s");
+  const cudaStream_t cs = (cudaStream_t)s;
+  double dt = p->deltaTime;
+  if (p->cfl > 0.0) {
+    if ((st = htr_CalculateMaxSpectralRadius(v, inner, m, w.scalars, s))) return st;
+    double r = 0.0;
+    if ((st = cuda_status(cudaMemcpyAsync(&r, w.scalars, sizeof(double), cudaMemcpyDeviceToHost, cs), "dt read"))) return st;
+    if ((st = cuda_status(cudaStreamSynchronize(cs), "dt sync"))) return st;
+    if (!(r > 0.0)) return fail(HTR_ERR_ARGUMENT, "non-positive spectral radius%s");
+    dt = p->cfl / r;
+  }
+  if (!(dt > 0.0)) return fail(HTR_ERR_ARGUMENT, "non-positive time step%s");
+  if (dt_used) *dt_used = dt;
+  if ((st = htr_InitializeTemporaries(v, fb, m, s))) return st;
+  htr::StageParams sp;
+  sp.scheme = p->scheme == HTR_SCHEME_SKEW ? 1 : 2;
+  sp.kind = p->scheme == HTR_SCHEME_TENOA ? htr::kTENOA : (p->scheme == HTR_SCHEME_TENOLAD ? htr::kTENOLAD : htr::kTENO);
+  sp.chemistry = p->explicitChemistry ? 1 : 0;
+  sp.dt = dt;
+  sp.active = active_dirs(fb);
+  sp.boundary = 1;
+  for (int k = 0; k < 6; k++) {
+    const int t = bc->type[k];
+    sp.bc[k] = t == HTR_BC_NSCBC_INFLOW ? htr::kBcInflow
+             : t == HTR_BC_NSCBC_OUTFLOW ? htr::kBcOutflow
+             : (t == HTR_BC_ISOTHERMAL_WALL || t == HTR_BC_ADIABATIC_WALL) ? htr::kBcWall : htr::kBcPeriodic;
+    sp.Pbc[k] = bc->P[k];
+  }
+  if ((st = cuda_status(cudaMemsetAsync(w.tcache, 0, sizeof(double) * 3 * ncells_of(fb), cs), "cache reset"))) return st;
+  const int neq = neq_of(m), ns = nspec_of(m);
+  return with_mix(m, [&](const auto &mix) -> int {
+    cudaError_t e;
+    for (int stage = 1; stage <= 3; stage++) {
+      // NSCBC terms of the stage's state, left in Conserved_t of the planes
+      for (int k = 0; k < 6; k++)
+        if (sp.bc[k] == htr::kBcInflow || sp.bc[k] == htr::kBcOutflow)
+          if ((e = htr::launch_init_rhs(*v, bc->plane[k], neq, 0, cs)) != cudaSuccess) return cuda_status(e, "plane rhs");
+      for (int d = 0; d < 3; d++) {
+        if (sp.bc[2 * d] != htr::kBcOutflow && sp.bc[2 * d + 1] != htr::kBcOutflow) continue;
+        if ((e = htr::launch_max_mach(*v, inner, d, w.scalars + d, cs)) != cudaSuccess) return cuda_status(e, "max mach");
+        for (int k = 2 * d; k < 2 * d + 2; k++)
+          if (sp.bc[k] == htr::kBcOutflow &&
+              (e = htr::launch_nscbc_outflow(*v, bc->plane[k], fb, mix, d, k % 2 == 0, 0.0, bc->LengthScale[k],
+                                             bc->P[k], cs, w.scalars + d)) != cudaSuccess)
+            return cuda_status(e, "nscbc outflow");
+      }
+      for (int k = 0; k < 6; k++)
+        if (sp.bc[k] == htr::kBcInflow &&
+            (e = htr::launch_nscbc_inflow(*v, bc->plane[k], mix, k / 2, k % 2 == 0, cs)) != cudaSuccess)
+          return cuda_status(e, "nscbc inflow");
+      sp.stage = stage;
+      if ((e = htr::launch_stage(*v, fb, fb, mix, w, sp, status_dev, cs)) != cudaSuccess) return cuda_status(e, "stage");
+      // wall ghosts from their first interior point, walls z, y, x
+      for (int k : {4, 5, 2, 3, 0, 1}) {
+        if (sp.bc[k] != htr::kBcWall) continue;
+        const bool iso = bc->type[k] == HTR_BC_ISOTHERMAL_WALL;
+        if ((e = htr::launch_wall_state(*v, bc->plane[k], ns, k, iso, cs)) != cudaSuccess ||
+            (e = htr::launch_properties(*v, bc->plane[k], mix, cs)) != cudaSuccess ||
+            (e = htr::launch_conserved(*v, bc->plane[k], mix, cs)) != cudaSuccess)
+          return cuda_status(e, "wall");
+      }
+    }
+    for (int k = 0; k < 6; k++)
+      if (sp.bc[k] == htr::kBcInflow &&
+          (e = htr::launch_nscbc_time_derivatives(*v, bc->plane[k], dt, cs)) != cudaSuccess)
+        return cuda_status(e, "inflow time derivatives");
+    return (int)HTR_OK;
+  });
+}
+
 int htr_rk3_step_static(const htr_fluid_view *v, htr_rect3 inner, htr_rect3 fb, const htr_step_params *p,
                         htr_mixture_t m, double *dt_used, int *status_dev, htr_stream_t s) {
   int st;

@@ -26,17 +26,22 @@
 
 namespace htr {
 
-// Tile geometry
-template <int D> struct Tile {
-  static constexpr int L = (D == 0) ? 1 : 32;   // pencils per block (consecutive x)
-  static constexpr int S = (D == 0) ? 256 : 8;  // cells per pencil
-  static constexpr int NF = L * (S + 1);        // faces per block
+// Tile geometry.  The TENO schemes reconstruct every face with the same
+// cost, so their tiles hold exactly one face per thread (255 x 1 or 7 x 32
+// cells: 256 faces); the others keep the 256 x 1 / 8 x 32 cell tiles.
+template <int D, int SCHEME> struct Tile {
+  static constexpr bool EQ = SCHEME == kSchemeTeno;
+  static constexpr int L = (D == 0) ? 1 : 32;                          // pencils per block (consecutive x)
+  static constexpr int S = (D == 0) ? (EQ ? 255 : 256) : (EQ ? 7 : 8);  // cells per pencil
+  static constexpr int NF = L * (S + 1);                               // faces per block
   static constexpr int THREADS = 256;
 };
 
+// Two blocks per SM (128 registers): the occupancy gain outweighs the spills
+// for every scheme.
 template <class Mix, int D, int SCHEME, int KIND>
-__global__ void __launch_bounds__(256) euler_kernel(const EulerArgs a, const __grid_constant__ Mix mix) {
-  using TL = Tile<D>;
+__global__ void __launch_bounds__(256, 2) euler_kernel(const EulerArgs a, const __grid_constant__ Mix mix) {
+  using TL = Tile<D, SCHEME>;
   using EF = EulerFace<Mix, D>;
   constexpr int NE = Mix::NS + 4;
   extern __shared__ double smem[];
@@ -97,11 +102,18 @@ __global__ void __launch_bounds__(256) euler_kernel(const EulerArgs a, const __g
     long long p[3], q[3];
     int t;
     face_point(f, p, q, t);
+    if (SCHEME == kSchemeTeno) {
+      // every face reconstructed here, one per thread: no queue
+      double F[NE];
+      const double lim_f = a.dt * (ld(a.me.at(p)) + ld(a.me.at(q)));
+      ef.template teno_flux<KIND>(F, p, t, lim_f);
+#pragma unroll
+      for (int i = 0; i < NE; i++) Fs[i * TL::NF + f] = F[i];
+      continue;
+    }
     bool smooth;
     if (SCHEME == kSchemeSkew) {
       smooth = true;
-    } else if (SCHEME == kSchemeTeno) {
-      smooth = false;
     } else {
       long long pm[3];
       ef.shift(pm, p, kNode[t].off[1], false);
@@ -149,7 +161,7 @@ __global__ void __launch_bounds__(256) euler_kernel(const EulerArgs a, const __g
 
 template <class Mix, int D, int SCHEME, int KIND>
 static cudaError_t launch_euler_dir(const EulerArgs &a, const Mix &mix, cudaStream_t s) {
-  using TL = Tile<D>;
+  using TL = Tile<D, SCHEME>;
   const long long n[3] = {a.my.size(0), a.my.size(1), a.my.size(2)};
   dim3 grid;
   if (D == 0) grid = dim3((unsigned)((n[0] + TL::S - 1) / TL::S), (unsigned)n[1], (unsigned)n[2]);

@@ -280,6 +280,15 @@ template <class Mix, int D> struct EulerFace {
 
   // Characteristic TENO flux at face p+1/2 with left point p (rhs.inl:622-759,
   // positivity limiter :710-758; lim_f = dt * (m_e[p] + m_e[right cell])).
+  //
+  // The reference projects the conserved vector and the flux of each of the
+  // six stencil points on every characteristic field, splits them, then
+  // reconstructs field by field.  Here the fields are streamed: the per-point
+  // quantities every projection row needs (normal velocity, pressure,
+  // momentum and energy, and the two species sums of the projection) are
+  // kept, and each row is projected, split and reconstructed in turn, with
+  // the reference's operations in the reference's order, so every value is
+  // bit-identical while only one field's twelve split values are live.
   template <int KIND>
   HTR_D void teno_flux(double *Flux, const long long *p, int t, double lim_f) const {
     long long pts[6][3];
@@ -291,11 +300,17 @@ template <class Mix, int D> struct EulerFace {
     shift(pts[3], p, kNode[t].off[2], true);
     shift(pts[4], p, kNode[t].off[3], true);
     shift(pts[5], p, kNode[t].off[4], true);
+    const double *Cpt[6];
+#pragma unroll
+    for (int k = 0; k < 6; k++) Cpt[k] = a.C.at(pts[k]);
     double L1 = 0, L0 = 0, LN = 0;
+    double un[6], pq[6];
 #pragma unroll
     for (int k = 0; k < 6; k++) {
-      const double un = ld(&a.u.at(pts[k])[D]), c = ld(a.SoS.at(pts[k]));
-      const double e1 = fabs(un - c), e0 = fabs(un), eN = fabs(un + c);
+      un[k] = ld(&a.u.at(pts[k])[D]);
+      pq[k] = ld(a.P.at(pts[k]));
+      const double c = ld(a.SoS.at(pts[k]));
+      const double e1 = fabs(un[k] - c), e0 = fabs(un[k]), eN = fabs(un[k] + c);
       if (k == 0) {
         L1 = e1;
         L0 = e0;
@@ -310,35 +325,88 @@ template <class Mix, int D> struct EulerFace {
     roe(R, pts[2], pts[3]);
     Proj Pj;
     proj_init(Pj, R);
-    double Fp[6][NE], Fm[6][NE];
+    // per point: the species sums of the projection (sum1 = sum bsp_i q_i,
+    // sq = sum q_i) of C and of the flux
+    double s1Q[6], sqQ[6], s1F[6], sqF[6];
 #pragma unroll
     for (int k = 0; k < 6; k++) {
-      double Cq[NE], Fq[NE], Qc[NE], Fc[NE];
+      double a1 = 0.0, a2 = 0.0, b1 = 0.0, b2 = 0.0;
 #pragma unroll
-      for (int i = 0; i < NE; i++) Cq[i] = ld(&a.C.at(pts[k])[i]);
-      const double un = ld(&a.u.at(pts[k])[D]), pq = ld(a.P.at(pts[k]));
-#pragma unroll
-      for (int i = 0; i < NE; i++) Fq[i] = Cq[i] * un;
-      Fq[iU + D] += pq;
-      Fq[iE] += pq * un;
-      to_char(Qc, Cq, R, Pj);
-      to_char(Fc, Fq, R, Pj);
-      Fp[k][0] = Fc[0] + L1 * Qc[0];
-      Fm[k][0] = Fc[0] - L1 * Qc[0];
-#pragma unroll
-      for (int i = 1; i < NE - 1; i++) {
-        Fp[k][i] = Fc[i] + L0 * Qc[i];
-        Fm[k][i] = Fc[i] - L0 * Qc[i];
+      for (int i = 0; i < NS; i++) {
+        const double q = ld(&Cpt[k][i]);
+        const double f = q * un[k];
+        a1 += Pj.bsp[i] * q;
+        a2 += q;
+        b1 += Pj.bsp[i] * f;
+        b2 += f;
       }
-      Fp[k][NE - 1] = Fc[NE - 1] + LN * Qc[NE - 1];
-      Fm[k][NE - 1] = Fc[NE - 1] - LN * Qc[NE - 1];
+      s1Q[k] = a1;
+      sqQ[k] = a2;
+      s1F[k] = b1;
+      sqF[k] = b2;
     }
-    double F[NE];
-#pragma unroll
+    double F[NE], Flc[NE];
+    // one characteristic field per iteration (not unrolled: the point data
+    // are reloaded from cache, keeping one field's values live)
+#pragma unroll 1
     for (int i = 0; i < NE; i++) {
-      const double fp = teno<KIND, false>(Fp[0][i], Fp[1][i], Fp[2][i], Fp[3][i], Fp[4][i], Fp[5][i], t, nullptr);
-      const double fm = teno<KIND, true>(Fm[0][i], Fm[1][i], Fm[2][i], Fm[3][i], Fm[4][i], Fm[5][i], t, nullptr);
-      F[i] = -0.5 * (fp + fm);
+      double fp[6], fm[6];
+      const double Lam = (i == 0) ? L1 : ((i == NE - 1) ? LN : L0);
+#pragma unroll
+      for (int k = 0; k < 6; k++) {
+        double cq[4], fq[4];
+#pragma unroll
+        for (int j = 0; j < 4; j++) {
+          cq[j] = ld(&Cpt[k][NS + j]);
+          fq[j] = cq[j] * un[k];
+        }
+        fq[D] += pq[k];
+        fq[3] += pq[k] * un[k];
+        double qc, fc;
+        if (i == 0 || i == NE - 1) {
+          // to_char rows 0 and NS+3
+          const double cD = (i == 0) ? (Pj.c[D] + Pj.ia) : (Pj.c[D] - Pj.ia);
+          qc = (i == 0 ? sqQ[k] : -sqQ[k]) * R.vel[D] * Pj.ia - s1Q[k];
+          qc -= cD * cq[D];
+          qc -= Pj.c[T1] * cq[T1];
+          qc -= Pj.c[T2] * cq[T2];
+          qc += Pj.dd * cq[3];
+          qc *= 0.5;
+          fc = (i == 0 ? sqF[k] : -sqF[k]) * R.vel[D] * Pj.ia - s1F[k];
+          fc -= cD * fq[D];
+          fc -= Pj.c[T1] * fq[T1];
+          fc -= Pj.c[T2] * fq[T2];
+          fc += Pj.dd * fq[3];
+          fc *= 0.5;
+        } else if (i <= NS) {
+          const int sp = i - 1;
+          const double q = ld(&Cpt[k][sp]);
+          const double f = q * un[k];
+          qc = R.Yi[sp] * s1Q[k];
+          qc += q;
+          fc = R.Yi[sp] * s1F[k];
+          fc += f;
+#pragma unroll
+          for (int j = 0; j < 3; j++) {
+            qc += Pj.Ycj[sp][j] * cq[j];
+            fc += Pj.Ycj[sp][j] * fq[j];
+          }
+          qc += Pj.mYd[sp] * cq[3];
+          fc += Pj.mYd[sp] * fq[3];
+        } else {
+          const int tj = (i == NS + 1) ? T1 : T2;
+          qc = -R.vel[tj] * sqQ[k];
+          qc += cq[tj];
+          fc = -R.vel[tj] * sqF[k];
+          fc += fq[tj];
+        }
+        fp[k] = fc + Lam * qc;
+        fm[k] = fc - Lam * qc;
+      }
+      const double rp = teno<KIND, false>(fp[0], fp[1], fp[2], fp[3], fp[4], fp[5], t, nullptr);
+      const double rm = teno<KIND, true>(fm[0], fm[1], fm[2], fm[3], fm[4], fm[5], t, nullptr);
+      F[i] = -0.5 * (rp + rm);
+      Flc[i] = (fp[2] + fm[3]) * -0.5;
     }
     from_char(Flux, F, R);
     if (NS > 1) {
@@ -355,10 +423,8 @@ template <class Mix, int D> struct EulerFace {
       if (limit) {
         const double eps = 1e-60;
         double theta = 1.0;
-        double Fl_c[NE], Fl[NE];
-#pragma unroll
-        for (int i = 0; i < NE; i++) Fl_c[i] = (Fp[2][i] + Fm[3][i]) * -0.5;
-        from_char(Fl, Fl_c, R);
+        double Fl[NE];
+        from_char(Fl, Flc, R);
 #pragma unroll
         for (int i = 0; i < NS; i++) {
           const double dr = lim_f * Flux[i];

@@ -57,7 +57,7 @@ cudaError_t launch_nscbc_inflow(const htr_fluid_view &v, const htr_rect3 &bc, co
 template <class Mix>
 cudaError_t launch_nscbc_outflow(const htr_fluid_view &v, const htr_rect3 &bc, const htr_rect3 &fb, const Mix &mix,
                                  int dir, bool minus, double MaxMach, double LengthScale, double PInf,
-                                 cudaStream_t s);
+                                 cudaStream_t s, const double *MaxMachDev = nullptr);
 cudaError_t launch_max_mach(const htr_fluid_view &v, const htr_rect3 &my, int dir, double *result, cudaStream_t s);
 
 // boundary-point state updates (side: 0 XNeg .. 5 ZPos)

@@ -21,6 +21,7 @@ struct BcArgs {
   Box bc, fb;
   long long n;  // points of the plane
   double MaxMach, LengthScale, PInf;
+  const double *MaxMachDev;  // if set, MaxMach is read from device memory
 };
 
 HTR_D void plane_point(const BcArgs &a, long long idx, long long *p) {
@@ -128,7 +129,8 @@ __global__ void nscbc_outflow(const BcArgs a, const __grid_constant__ Mix mix) {
     const double lambda_1 = un - c, lambda = un, lambda_N = un + c;
     const double lambda_s = MINUS ? smin(un, 0.0) : smax(un, 0.0);
     const double sigma = 0.25;
-    const double K = (a.MaxMach < 0.99) ? sigma * (1.0 - a.MaxMach * a.MaxMach) * c / a.LengthScale
+    const double MaxMach = a.MaxMachDev ? *a.MaxMachDev : a.MaxMach;
+    const double K = (MaxMach < 0.99) ? sigma * (1.0 - MaxMach * MaxMach) * c / a.LengthScale
                                         : sigma * (c - (un * un) / c) / a.LengthScale;
     double Yp[NS], LS[NS];
 #pragma unroll
@@ -215,6 +217,7 @@ static BcArgs bc_args(const htr_fluid_view &v, const htr_rect3 &bc, const htr_re
   a.fb = box(fb);
   a.n = a.bc.size(0) * a.bc.size(1) * a.bc.size(2);
   a.MaxMach = a.LengthScale = a.PInf = 0.0;
+  a.MaxMachDev = nullptr;
   return a;
 }
 
@@ -247,9 +250,10 @@ cudaError_t launch_nscbc_inflow(const htr_fluid_view &v, const htr_rect3 &bc, co
 template <class Mix>
 cudaError_t launch_nscbc_outflow(const htr_fluid_view &v, const htr_rect3 &bc, const htr_rect3 &fb, const Mix &mix,
                                  int dir, bool minus, double MaxMach, double LengthScale, double PInf,
-                                 cudaStream_t s) {
+                                 cudaStream_t s, const double *MaxMachDev) {
   BcArgs a = bc_args(v, bc, fb);
   a.MaxMach = MaxMach;
+  a.MaxMachDev = MaxMachDev;
   a.LengthScale = LengthScale;
   a.PInf = PInf;
   if (dir == 0) return minus ? outflow_dir<Mix, 0, true>(a, mix, s) : outflow_dir<Mix, 0, false>(a, mix, s);
@@ -269,7 +273,8 @@ cudaError_t launch_max_mach(const htr_fluid_view &v, const htr_rect3 &my, int di
   template cudaError_t launch_nscbc_inflow<MIX>(const htr_fluid_view &, const htr_rect3 &, const MIX &, int,  \
                                                 bool, cudaStream_t);                                         \
   template cudaError_t launch_nscbc_outflow<MIX>(const htr_fluid_view &, const htr_rect3 &, const htr_rect3 &, \
-                                                 const MIX &, int, bool, double, double, double, cudaStream_t);
+                                                 const MIX &, int, bool, double, double, double, cudaStream_t, \
+                                                 const double *);
 HTR_INST(ConstPropDev)
 HTR_INST(AirDev)
 #undef HTR_INST

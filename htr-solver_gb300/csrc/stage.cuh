@@ -55,6 +55,7 @@ struct StageWorkspace {
   unsigned *count;  // queue length
   double *prep;     // per-cell prepass values, [kPrepVals][ncell]
   double *tcache;   // per cell: T it was computed for, log(T TRef), 1/(T TRef); [3][ncell]
+  double *scalars;  // 3 doubles in the queue counter's 256-byte block (maximum Mach number per direction)
 };
 
 // per-cell prepass values: velocity-gradient tensor (9), mixture molar
@@ -74,7 +75,18 @@ struct StageParams {
   // direction contributes exactly zero to every flux difference (both faces
   // see the same cell), so its faces are not computed.
   unsigned active;
+  // Boundary conditions (the boundary step only): kind of each side (BcKind,
+  // xNeg, xPos, yNeg, yPos, zNeg, zPos) and the pressure of a supersonic
+  // NSCBC inflow.  boundary = 0 keeps the periodic / Dirichlet-ghost update.
+  int boundary = 0;
+  int bc[6] = {0, 0, 0, 0, 0, 0};
+  double Pbc[6] = {0.0, 0.0, 0.0, 0.0, 0.0, 0.0};
 };
+
+// Side kinds of the boundary step.  Walls have staggered ghost points (never
+// solved); NSCBC sides have collocated boundary points, solved without the
+// flux divergence normal to the side and refreshed by the side's rule.
+enum BcKind { kBcPeriodic = 0, kBcWall = 1, kBcInflow = 2, kBcOutflow = 3 };
 
 // Launch shapes of the fused stage (process-wide; set before launches or
 // graph captures that should use them).

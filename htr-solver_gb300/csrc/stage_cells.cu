@@ -48,6 +48,7 @@ bool stage_workspace_carve(void *base, size_t bytes, const htr_rect3 &r, int neq
   w.queue = reinterpret_cast<TenoEntry *>(p);
   p += align256(sizeof(TenoEntry) * (g.nf[0] + g.nf[1] + g.nf[2]));
   w.count = reinterpret_cast<unsigned *>(p);
+  w.scalars = reinterpret_cast<double *>(p + sizeof(double));
   p += align256(sizeof(unsigned));
   w.prep = reinterpret_cast<double *>(p);
   {
@@ -245,6 +246,10 @@ struct UpdateArgs {
   int chemistry;
   int *status;
   double *tcache;  // [3][ncell]: T, log(T TRef), 1/(T TRef) of the last refresh
+  // boundary step only
+  Fd<double> Xp, Tp, up;  // NSCBC inflow profiles
+  int bc[6];
+  double Pbc[6];
 };
 
 // Primitive recovery and property refresh of one cell from its new
@@ -342,7 +347,83 @@ HTR_D void refresh_cell(const UpdateArgs &A, const Mix &mix, const long long *p,
   }
 }
 
+// Properties of a boundary point from its primitives (the arithmetic of
+// UpdatePropertiesFromPrimitive, src/prometeo_variables.hpp:62-89), then its
+// conserved variables (UpdateConservedFromPrimitive, :91-130).
 template <class Mix>
+HTR_D void boundary_properties(const UpdateArgs &A, const Mix &mix, const long long *p, double Pp, double Tp,
+                               const double *x, const double *vel) {
+  constexpr int NS = Mix::NS;
+  double y[NS], d[NS];
+  const double MixW = mix.MolarWeightFromXi(x);
+  const double r = mix.Rho(Pp, Tp, MixW);
+  *A.rho.at(p) = r;
+  if constexpr (NS > 1) {
+    double m, l;
+    mix.Transport(Tp, Pp, MixW, x, m, l, d);
+    *A.mu.at(p) = m;
+    *A.lam.at(p) = l;
+  } else {
+    *A.mu.at(p) = mix.Viscosity(Tp, x);
+    *A.lam.at(p) = mix.HeatConductivity(Tp, x);
+    mix.Diffusivity(d, Pp, Tp, MixW, x);
+  }
+  mix.MassFractions(y, MixW, x);
+  const double gamma = mix.Gamma(Tp, MixW, y);
+  *A.SoS.at(p) = mix.SpeedOfSound(Tp, gamma, MixW);
+  double *dp = A.Di.at(p), *yp = A.Y.at(p), *c = A.C.at(p);
+#pragma unroll
+  for (int k = 0; k < NS; k++) {
+    dp[k] = d[k];
+    yp[k] = y[k];
+    c[k] = r * y[k];
+  }
+#pragma unroll
+  for (int k = 0; k < 3; k++) c[NS + k] = r * vel[k];
+  c[NS + 3] = r * (0.5 * mod2(vel) + mix.InternalEnergy(Tp, y));
+}
+
+// NSCBC inflow point after the RK update (SetNSCBC_InflowBCTask,
+// src/prometeo_bc.hpp:108-150): imposed composition, temperature and
+// velocity; pressure from the advanced density, or the imposed pressure of a
+// supersonic inflow.
+template <class Mix>
+HTR_D void inflow_refresh(const UpdateArgs &A, const Mix &mix, const long long *p, const double *u_, int side) {
+  constexpr int NS = Mix::NS;
+  double x[NS], vel[3];
+#pragma unroll
+  for (int k = 0; k < NS; k++) x[k] = ld(&A.Xp.at(p)[k]);
+#pragma unroll
+  for (int k = 0; k < 3; k++) vel[k] = ld(&A.up.at(p)[k]);
+  const double T = ld(A.Tp.at(p));
+  double P;
+  if (fabs(vel[side / 2]) >= *A.SoS.at(p)) {
+    P = A.Pbc[side];
+  } else {
+    double rhoYi[NS];
+#pragma unroll
+    for (int k = 0; k < NS; k++) rhoYi[k] = u_[k];
+    P = mix.PFromRhoAndT(mix.RhoFromRhoYi(rhoYi), mix.MolarWeightFromXi(x), T);
+  }
+  double *xp = A.X.at(p), *vp = A.u.at(p);
+#pragma unroll
+  for (int k = 0; k < NS; k++) xp[k] = x[k];
+#pragma unroll
+  for (int k = 0; k < 3; k++) vp[k] = vel[k];
+  *A.T.at(p) = T;
+  *A.P.at(p) = P;
+  boundary_properties(A, mix, p, P, T, x, vel);
+}
+
+// BC = false: periodic grids and Dirichlet ghosts (ghost nodes keep their
+// state).  BC = true: the boundary step; a point with a staggered (wall)
+// ghost node is not solved (the wall kernels refresh it after this kernel);
+// a collocated NSCBC boundary point is solved without the flux divergence
+// normal to its side(s), adds the NSCBC terms its plane kernels left in
+// Conserved_t (zero at a supersonic inflow) and is refreshed by its side's
+// rule: inflow (inflow wins an edge with an outflow), else the outflow's
+// primitive recovery; then its properties and conserved variables.
+template <class Mix, bool BC>
 __global__ void __launch_bounds__(128) stage_update(const UpdateArgs A, const __grid_constant__ Mix mix) {
   constexpr int NS = Mix::NS, NE = NS + 4;
   const long long n = A.dn.count();
@@ -352,12 +433,32 @@ __global__ void __launch_bounds__(128) stage_update(const UpdateArgs A, const __
     double ct[NE];
 #pragma unroll
     for (int k = 0; k < NE; k++) ct[k] = 0.0;
-    // boundary ghosts keep their imposed state; their RHS is zero
-    bool ghost = false;
+    unsigned div = A.active;  // directions whose flux divergence applies here
+    bool bnd = false;         // on an NSCBC plane
+    int inflow_side = -1;
+    int n_out = 0;            // outflow planes holding this point
+    bool skip = false;
+    if constexpr (BC) {
 #pragma unroll
-    for (int D = 0; D < 3; D++)
-      if (A.active & (1u << D)) ghost = ghost || ghost_node(ld(A.nt[D].at(p)));
-    if (ghost) {
+      for (int D = 0; D < 3; D++) {
+        if (!(A.active & (1u << D))) continue;
+        const int t = ld(A.nt[D].at(p));
+        if (t == L_S || t == R_S) skip = true;
+        if (t == L_C || t == R_C) {
+          div &= ~(1u << D);
+          bnd = true;
+          const int side = 2 * D + (t == R_C ? 1 : 0);
+          if (A.bc[side] == kBcInflow && inflow_side < 0) inflow_side = side;
+          if (A.bc[side] == kBcOutflow) n_out++;
+        }
+      }
+    } else {
+      // boundary ghosts keep their imposed state; their RHS is zero
+#pragma unroll
+      for (int D = 0; D < 3; D++)
+        if (A.active & (1u << D)) skip = skip || ghost_node(ld(A.nt[D].at(p)));
+    }
+    if (skip) {
       double *ctp = A.Ct.at(p);
 #pragma unroll
       for (int k = 0; k < NE; k++) ctp[k] = 0.0;
@@ -393,7 +494,7 @@ __global__ void __launch_bounds__(128) stage_update(const UpdateArgs A, const __
     for (int pass = 0; pass < 2; pass++) {
 #pragma unroll
       for (int dd = 2; dd >= 0; dd--) {
-        if (!(A.active & (1u << dd))) continue;
+        if (!(div & (1u << dd))) continue;
         long long c1[3] = {p[0], p[1], p[2]};
         c1[dd] += 1;
         const long long nf = A.g.nf[dd];
@@ -402,6 +503,21 @@ __global__ void __launch_bounds__(128) stage_update(const UpdateArgs A, const __
         const double m = pass == 0 ? ld(A.me[dd].at(p)) : ld(A.md[dd].at(p));
 #pragma unroll
         for (int k = 0; k < NE; k++) ct[k] = __dadd_rn(ct[k], __dmul_rn(m, __dsub_rn(F[k * nf + fp], F[k * nf + fm])));
+      }
+    }
+    if constexpr (BC) {
+      if (bnd) {
+        // the NSCBC terms (src/prometeo.rg:592-605), added last
+        const double *nb = A.Ct.at(p);
+#pragma unroll
+        for (int k = 0; k < NE; k++) ct[k] = __dadd_rn(ct[k], nb[k]);
+        if (inflow_side >= 0) {
+          const double un = A.u.at(p)[inflow_side / 2], c = A.SoS.at(p)[0];
+          if ((inflow_side % 2 == 0) ? (un >= c) : (un <= -c)) {
+#pragma unroll
+            for (int k = 0; k < NE; k++) ct[k] = 0.0;
+          }
+        }
       }
     }
     // SSP-RK3 update (prometeo_rk.rg:88-112)
@@ -416,9 +532,39 @@ __global__ void __launch_bounds__(128) stage_update(const UpdateArgs A, const __
                         __dmul_rn(__dmul_rn(A.c3, ct[k]), A.dt));
       cons[k] = u_[k];
     }
+    if constexpr (BC) {
+      if (inflow_side >= 0) {
+        inflow_refresh(A, mix, p, u_, inflow_side);
+        continue;
+      }
+    }
     // primitive recovery (variables.hpp:163-193) and property refresh
     // (variables.hpp:62-89) of the new state
     refresh_cell(A, mix, p, u_, i, Td0, Tinv0, logT0);
+    if constexpr (BC) {
+      if (bnd) {
+        // outflow point (SetNSCBC_OutflowBCTask): the recovery above, once per
+        // outflow plane holding the point (an edge shared by two outflows
+        // is recovered twice, the second Newton starting from the first's
+        // temperature), then its properties and conserved variables
+        for (int r = 1; r < n_out; r++) {
+          double Td = 0.0, Ti = 0.0, lT = 0.0;
+          if constexpr (NS > 1) {
+            Td = *A.T.at(p) * mix.TRef;
+            Ti = A.tcache[2 * n + i];
+            lT = A.tcache[n + i];
+          }
+          refresh_cell(A, mix, p, u_, i, Td, Ti, lT);
+        }
+        double x[NS], vel[3];
+        const double *xp = A.X.at(p), *vp = A.u.at(p);
+#pragma unroll
+        for (int k = 0; k < NS; k++) x[k] = xp[k];
+#pragma unroll
+        for (int k = 0; k < 3; k++) vel[k] = vp[k];
+        boundary_properties(A, mix, p, *A.P.at(p), *A.T.at(p), x, vel);
+      }
+    }
   }
 }
 
@@ -534,8 +680,18 @@ cudaError_t launch_stage(const htr_fluid_view &v, const htr_rect3 &my, const htr
   U.chemistry = sp.chemistry;
   U.status = status;
   U.tcache = w.tcache;
+  U.Xp = fd<double>(v.MolarFracs_profile);
+  U.Tp = fd<double>(v.temperature_profile);
+  U.up = fd<double>(v.velocity_profile);
+  for (int k = 0; k < 6; k++) {
+    U.bc[k] = sp.bc[k];
+    U.Pbc[k] = sp.Pbc[k];
+  }
   const int ub = stage_tuning().update_block;
-  stage_update<Mix><<<grid_for(n, ub), ub, 0, s>>>(U, mix);
+  if (sp.boundary)
+    stage_update<Mix, true><<<grid_for(n, ub), ub, 0, s>>>(U, mix);
+  else
+    stage_update<Mix, false><<<grid_for(n, ub), ub, 0, s>>>(U, mix);
   if ((e = cudaGetLastError()) != cudaSuccess) return e;
   return mark(1 + kUpdate);
 }

@@ -2,12 +2,12 @@
 // -fmad=false) and the Euler orchestration of one stage.
 //
 // euler_teno_faces: the faces the hybrid sensor rejected (queued by the
-// Kennedy-Gruber kernel, stage_kg.cu), or every face for the TENO schemes,
-// spread over every SM with a grid-stride loop, so the expensive
-// reconstruction is load-balanced independently of where the shocks are.
-// The arithmetic per face is the one of the per-direction task kernels
-// (euler_face.cuh), so selection flags and face fluxes are bit-identical to
-// theirs.
+// Kennedy-Gruber kernel, stage_kg.cu), spread over every SM with a
+// grid-stride loop, so the expensive reconstruction is load-balanced
+// independently of where the shocks are.  euler_teno_faces_dir: every face of
+// one direction for the TENO schemes, one face per thread.  The arithmetic
+// per face is the one of the per-direction task kernels (euler_face.cuh), so
+// selection flags and face fluxes are bit-identical to theirs.
 #include "stage_euler.cuh"
 
 namespace htr {
@@ -19,7 +19,6 @@ struct StageTenoArgs {
   double *fe[3];
   const TenoEntry *queue;
   const unsigned *count;
-  long long nall;  // > 0: every face of the three directions (no queue)
   unsigned active; // directions whose faces are computed
 };
 
@@ -62,26 +61,11 @@ HTR_D void teno_face_at(const StageTenoArgs &A, const Mix &mix, const long long 
 
 template <class Mix, int KIND>
 __global__ void __launch_bounds__(128) euler_teno_faces(const StageTenoArgs A, const __grid_constant__ Mix mix) {
-  const long long n = A.nall > 0 ? A.nall : (long long)*A.count;
+  const long long n = (long long)*A.count;
   for (long long k = blockIdx.x * (long long)blockDim.x + threadIdx.x; k < n; k += (long long)gridDim.x * blockDim.x) {
-    int D;
-    long long c[3];
-    if (A.nall > 0) {
-      long long f = k;
-      D = 0;
-      while (D < 2 && f >= A.g.nf[D]) f -= A.g.nf[D++];
-      if (!(A.active & (1u << D))) continue;
-      const long long e0 = A.g.ext[D][0], e1 = A.g.ext[D][1];
-      c[0] = A.g.lo[0] + f % e0;
-      c[1] = A.g.lo[1] + (f / e0) % e1;
-      c[2] = A.g.lo[2] + f / (e0 * e1);
-    } else {
-      const TenoEntry e = A.queue[k];
-      D = e.D;
-      c[0] = e.c0;
-      c[1] = e.c1;
-      c[2] = e.c2;
-    }
+    const TenoEntry e = A.queue[k];
+    const int D = e.D;
+    const long long c[3] = {e.c0, e.c1, e.c2};
     if (D == 0)
       teno_face_at<Mix, 0, KIND>(A, mix, c);
     else if (D == 1)
@@ -89,6 +73,26 @@ __global__ void __launch_bounds__(128) euler_teno_faces(const StageTenoArgs A, c
     else
       teno_face_at<Mix, 2, KIND>(A, mix, c);
   }
+}
+
+// Every face of direction D (the TENO schemes): one face per thread,
+// consecutive threads on consecutive x, one launch per direction, so a launch
+// holds one direction's code and no queue.
+template <class Mix, int D, int KIND>
+__global__ void __launch_bounds__(128) euler_teno_faces_dir(const StageTenoArgs A, const __grid_constant__ Mix mix) {
+  const long long nf = A.g.nf[D];
+  const long long e0 = A.g.ext[D][0], e1 = A.g.ext[D][1];
+  for (long long f = blockIdx.x * (long long)blockDim.x + threadIdx.x; f < nf; f += (long long)gridDim.x * blockDim.x) {
+    const long long c[3] = {A.g.lo[0] + f % e0, A.g.lo[1] + (f / e0) % e1, A.g.lo[2] + f / (e0 * e1)};
+    teno_face_at<Mix, D, KIND>(A, mix, c);
+  }
+}
+
+template <class Mix, int KIND>
+static void launch_teno_dir(const StageTenoArgs &T, const Mix &mix, int D, dim3 grid, cudaStream_t s) {
+  if (D == 0) euler_teno_faces_dir<Mix, 0, KIND><<<grid, 128, 0, s>>>(T, mix);
+  else if (D == 1) euler_teno_faces_dir<Mix, 1, KIND><<<grid, 128, 0, s>>>(T, mix);
+  else euler_teno_faces_dir<Mix, 2, KIND><<<grid, 128, 0, s>>>(T, mix);
 }
 
 // --- launchers --------------------------------------------------------------
@@ -157,16 +161,26 @@ cudaError_t launch_stage_euler(const htr_fluid_view &v, const htr_rect3 &my, con
   T.g = g;
   T.queue = w.queue;
   T.count = w.count;
-  T.nall = (p.scheme == 2) ? (g.nf[0] + g.nf[1] + g.nf[2]) : 0;
   T.active = p.active;
   int dev = 0, sms = 152;
   cudaGetDevice(&dev);
   cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+  if (p.scheme == 2) {
+    for (int k = 0; k < 3; k++) {
+      const int D = order[k];
+      if (!(p.active & (1u << D))) continue;
+      const long long blocks = (g.nf[D] + 127) / 128, cap = (long long)sms * 64;
+      const dim3 gd((unsigned)(blocks < cap ? blocks : cap));
+      if (p.kind == kTENO) launch_teno_dir<Mix, kTENO>(T, mix, D, gd, s);
+      else if (p.kind == kTENOA) launch_teno_dir<Mix, kTENOA>(T, mix, D, gd, s);
+      else launch_teno_dir<Mix, kTENOLAD>(T, mix, D, gd, s);
+      if ((e = cudaGetLastError()) != cudaSuccess) return e;
+    }
+    return mark(3);
+  }
+  // the hybrid scheme's sensor-rejected faces (plain TENO, rhs.inl:622-759)
   dim3 grid((unsigned)(sms * stage_tuning().teno_blocks_per_sm));
-  const int kind = (p.scheme == 2) ? p.kind : 0;
-  if (kind == kTENO) euler_teno_faces<Mix, kTENO><<<grid, 128, 0, s>>>(T, mix);
-  else if (kind == kTENOA) euler_teno_faces<Mix, kTENOA><<<grid, 128, 0, s>>>(T, mix);
-  else euler_teno_faces<Mix, kTENOLAD><<<grid, 128, 0, s>>>(T, mix);
+  euler_teno_faces<Mix, kTENO><<<grid, 128, 0, s>>>(T, mix);
   if ((e = cudaGetLastError()) != cudaSuccess) return e;
   return mark(3);
 }

@@ -25,6 +25,14 @@ class htr_step_params(C.Structure):
 SCHEMES = {"Hybrid": 0, "TENO": 1, "TENOA": 2, "TENOLAD": 3, "SkewSymmetric": 4}
 
 
+class htr_bc_params(C.Structure):
+    _fields_ = [("type", C.c_int * 6), ("P", C.c_double * 6), ("LengthScale", C.c_double * 6),
+                ("plane", abi.htr_rect3 * 6)]
+
+
+BC_TYPES = {"Periodic": 0, "NSCBC_Inflow": 1, "NSCBC_Outflow": 2, "IsothermalWall": 3, "AdiabaticWall": 4}
+
+
 def lib():
     """The loaded CUDA library (raises if it was not built)."""
     global _lib
@@ -47,6 +55,10 @@ def lib():
                                           C.POINTER(htr_step_params), C.c_void_p, C.POINTER(C.c_double),
                                           C.c_void_p, C.c_void_p]
         l.htr_rk3_step_static.restype = C.c_int
+        l.htr_rk3_step_bc_ws.argtypes = [C.POINTER(abi.htr_fluid_view), abi.htr_rect3, abi.htr_rect3,
+                                         C.POINTER(htr_step_params), C.POINTER(htr_bc_params), C.c_void_p,
+                                         C.c_void_p, C.c_size_t, C.POINTER(C.c_double), C.c_void_p, C.c_void_p]
+        l.htr_rk3_step_bc_ws.restype = C.c_int
         l.htr_rk3_static_scratch_bytes.argtypes = []
         l.htr_rk3_static_scratch_bytes.restype = C.c_size_t
         for name, args in EXTRA_PROTOTYPES.items():

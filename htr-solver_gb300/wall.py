@@ -251,3 +251,52 @@ class BoundaryRun:
                     self._ck(self.lib.htr_UpdateNSCBCGhostCellTimeDerivatives(C.byref(v), r, dt, self.stream),
                              "inflow time derivatives")
         return dt
+
+
+class FusedBoundaryRun:
+    """The same steps as BoundaryRun through htr_rk3_step_bc_ws: the fused
+    stage pipeline over the whole grid with the NSCBC and wall rules folded
+    into its per-cell kernel (CUDA library, device fields).  With a fixed dt
+    the step issues no host synchronisation and can be graph-captured."""
+
+    def __init__(self, fl, mixh, bc, scheme="TENOLAD", chemistry=True, stream=None, workspace=None):
+        from . import runtime
+        self.rt = runtime
+        self.lib = runtime.lib()
+        self.fl, self.mixh = fl, mixh
+        types = [bc[s][0] for s in zones.SIDES]
+        params = [bc[s][1] for s in zones.SIDES]
+        for t in types:
+            if t not in runtime.BC_TYPES:
+                raise abi.HtrError(f"boundary condition {t} is not supported by the fused boundary step")
+        axes = tuple((types[2 * d], types[2 * d + 1]) for d in range(3))
+        bnum = tuple(0 if a[0] == PERIODIC else 1 for a in axes)
+        z = zones.partition(fl.shape, bnum, axes)
+        self.params = runtime.htr_bc_params()
+        for k in range(6):
+            self.params.type[k] = runtime.BC_TYPES[types[k]]
+            self.params.P[k] = params[k].get("P", 0.0)
+            self.params.LengthScale[k] = params[k].get("LengthScale", 0.0)
+            if types[k] != PERIODIC:
+                if len(z.planes[k]) != 1:
+                    raise abi.HtrError(f"boundary plane {zones.SIDES[k]} is not one rectangle")
+                self.params.plane[k] = abi.rect(*z.planes[k][0])
+        self.interior = abi.rect(*z.interior)
+        self.scheme = runtime.SCHEMES[scheme]
+        self.chemistry = chemistry
+        self.stream = stream
+        self.ws = workspace or runtime.Workspace()
+        self.nbytes = self.lib.htr_rk3_workspace_bytes(fl.bounds(), mixh)
+        self.ws.get(self.nbytes, fl.device)
+
+    def step(self, dt=0.0, cfl=0.0, status_dev=None):
+        """One SSP-RK3 step with step size dt (or cfl > 0); returns the dt used."""
+        p = self.rt.htr_step_params(self.scheme, 1.0, cfl, dt, 1 if self.chemistry else 0)
+        v = self.fl.view()
+        used = C.c_double(0.0)
+        ws = self.ws.get(self.nbytes, self.fl.device)
+        st = self.lib.htr_rk3_step_bc_ws(C.byref(v), self.interior, self.fl.bounds(), C.byref(p),
+                                         C.byref(self.params), self.mixh, C.c_void_p(ws), self.nbytes,
+                                         C.byref(used), status_dev, self.rt.stream_handle(self.stream))
+        abi.check(self.lib, st, "htr_rk3_step_bc_ws")
+        return used.value

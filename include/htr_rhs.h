@@ -340,6 +340,45 @@ int htr_rk3_step_ws(const htr_fluid_view *view, htr_rect3 interior, htr_rect3 fl
                     const htr_step_params *params, htr_mixture_t mix, void *workspace,
                     size_t workspace_bytes, double *dt_used, int *status_dev, htr_stream_t stream);
 
+/* --- fused time step of a grid with boundary conditions --------------------
+ * Not a reference task.  One SSP-RK3 step of the reference driver
+ * (src/prometeo.rg:1342-1486, UpdateDerivatives :480-606,
+ * UpdatePrimitivesAndBCsFromConserved :428-478) for a grid with NSCBC inflow
+ * and outflow sides and isothermal or adiabatic walls, one ghost layer on
+ * each non-periodic side (interior = fluid_bounds shrunk by one there), on
+ * the fused stage pipeline run over the whole grid.  Per stage: the NSCBC
+ * terms of every outflow plane (the interior's maximum Mach number stays on
+ * the device) and inflow plane from the stage's state; prepass, Euler and
+ * diffusion faces; one per-cell kernel in which a collocated boundary point
+ * skips the flux divergence normal to its side, adds its NSCBC terms and
+ * takes its side's state rule, and wall ghosts (never solved) are refreshed
+ * from their first interior point after it (walls z, y, x).  After the step
+ * the inflow time derivatives.  Zones as the reference's partitioner makes
+ * them: bc->plane[s] is the side's p_xNeg[0]... (its face plus the edges and
+ * corners it wins).  Schemes TENO, TENO-A, TENO-LAD, skew-symmetric (the
+ * hybrid scheme's sensors near boundaries are not modelled: UNSUPPORTED).
+ * Workspace: htr_rk3_workspace_bytes(fluid_bounds, mix) bytes.  With cfl <= 0
+ * the call issues no host synchronisation (CUDA-graph capturable). */
+typedef enum {
+  HTR_BC_PERIODIC = 0,
+  HTR_BC_NSCBC_INFLOW = 1,
+  HTR_BC_NSCBC_OUTFLOW = 2,
+  HTR_BC_ISOTHERMAL_WALL = 3,
+  HTR_BC_ADIABATIC_WALL = 4
+} htr_bc_type;
+
+typedef struct {
+  int type[6];           /* htr_bc_type of xNeg, xPos, yNeg, yPos, zNeg, zPos */
+  double P[6];           /* inflow: pressure of a supersonic inflow; outflow: PInf */
+  double LengthScale[6]; /* outflow: relaxation length */
+  htr_rect3 plane[6];    /* boundary points of each non-periodic side */
+} htr_bc_params;
+
+int htr_rk3_step_bc_ws(const htr_fluid_view *view, htr_rect3 interior, htr_rect3 fluid_bounds,
+                       const htr_step_params *params, const htr_bc_params *bc, htr_mixture_t mix,
+                       void *workspace, size_t workspace_bytes, double *dt_used, int *status_dev,
+                       htr_stream_t stream);
+
 /* No counterpart in the reference.  The fused step of htr_rk3_step_ws on a
  * fixed scratch that the library owns: a module-scope device array of
  * htr_rk3_static_scratch_bytes() bytes, reserved when the library's module

@@ -220,3 +220,45 @@ def test_gpu_boundary_layer_steps(steps):
     assert err.max() <= util.RHS_REL_TOL, err
     for name in ("temperature", "pressure", "velocity", "MolarFracs"):
         assert util.rel_err(out[name], host[name]).max() <= util.RHS_REL_TOL, name
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("steps", [1, 2])
+def test_gpu_fused_boundary_layer_steps(steps):
+    """The fused boundary step (htr_rk3_step_bc_ws) against the oracle step."""
+    import torch
+    port = oracle.port_lib()
+    host, hp, m = _bl(port, num=(24, 16, 6))
+    dev = host.to_device("cuda")
+    gh = runtime.load_mixture(host.meta["eos"], m)
+    run = wall.FusedBoundaryRun(dev, gh, host.meta["bc"])
+    dt = wall.BoundaryRun(port, host, hp, host.meta["bc"]).spectral_dt(0.8)
+    for _ in range(steps):
+        _oracle_step(port, host, hp, dt)
+        run.step(dt)
+    torch.cuda.synchronize()
+    out = dev.to_host()
+    err = util.rel_err(out["Conserved"], host["Conserved"])
+    assert err.max() <= util.RHS_REL_TOL, err
+    for name in ("temperature", "pressure", "velocity", "MolarFracs", "rho", "SoS", "mu", "dudtBoundary"):
+        assert util.rel_err(out[name], host[name]).max() <= util.RHS_REL_TOL, name
+
+
+@pytest.mark.gpu
+def test_gpu_fused_boundary_cfl_and_errors():
+    import torch
+    port = oracle.port_lib()
+    host, hp, m = _bl(port, num=(12, 10, 4))
+    dev = host.to_device("cuda")
+    gh = runtime.load_mixture(host.meta["eos"], m)
+    run = wall.FusedBoundaryRun(dev, gh, host.meta["bc"])
+    dt_ref = wall.BoundaryRun(port, host, hp, host.meta["bc"]).spectral_dt(0.8)
+    dt = run.step(cfl=0.8)
+    torch.cuda.synchronize()
+    assert dt == pytest.approx(dt_ref, rel=1e-12)
+    with pytest.raises(abi.HtrError):
+        wall.FusedBoundaryRun(dev, gh, host.meta["bc"], scheme="Hybrid").step(dt)
+    bad = wall.FusedBoundaryRun(dev, gh, host.meta["bc"])
+    bad.params.plane[0] = abi.rect((1, 0, 0), (1, 11, 3))  # not the ghost layer
+    with pytest.raises(abi.HtrError):
+        bad.step(dt)
