@@ -288,7 +288,10 @@ HTR_D double teno(double ym2, double ym1, double y, double yp1, double yp2, doub
       cm = fmaxf(cm, __fdiv_rn(tt, __fadd_rn(__double2float_rn(s.s4), e)));
       const float arg = 3.0f + 9.5f / (1.0f + cm * 0.1f);
       const float fl = floorf(arg);
-      cut_ok = fx.ok && (arg - fl > 1e-3f) && (fl + 1.0f - arg > 1e-3f);
+      // the exact argument 3 + 9.5 theta is never below 3 (theta > 0), so a
+      // power of 3 needs the margin only towards 4 (smooth regions, where
+      // chi is huge, sit just above 3)
+      cut_ok = fx.ok && (fl <= 3.0f || arg - fl > 1e-3f) && (fl + 1.0f - arg > 1e-3f);
       fcut = double(kP10[min(max(int(fl), 0), 13)]);
     }
     if (cut_ok) fmask = fast_mask(fx, used, fcut);
@@ -381,9 +384,23 @@ HTR_D double teno(double ym2, double ym1, double y, double yp1, double yp2, doub
       v[k] = ym2 * r0 + ym1 * r1 + y * r2 + yp1 * r3 + yp2 * r4 + yp3 * r5 - base;
     }
   }
-  const double c1 = W0 * b1, c2 = W1 * b2, c3 = W2 * b3, c4 = W3 * b4;
-  const double ia = 1.0 / (c1 + c2 + c3 + c4);
-  const double w1 = c1 * ia, w2 = c2 * ia, w3 = c3 * ia, w4 = c4 * ia;
+  double w1, w2, w3, w4;
+  if (t == Std && b1 && b2 && b3 && b4) {
+    // every standard candidate kept (smooth flow): the normalised optimal
+    // weights, the same operations as below evaluated once
+    constexpr double ia = 1.0 / (((9.0 / 20.0 + 6.0 / 20.0) + 1.0 / 20.0) + 4.0 / 20.0);
+    w1 = (9.0 / 20.0) * ia;
+    w2 = (6.0 / 20.0) * ia;
+    w3 = (1.0 / 20.0) * ia;
+    w4 = (4.0 / 20.0) * ia;
+  } else {
+    const double c1 = W0 * b1, c2 = W1 * b2, c3 = W2 * b3, c4 = W3 * b4;
+    const double ia = 1.0 / (c1 + c2 + c3 + c4);
+    w1 = c1 * ia;
+    w2 = c2 * ia;
+    w3 = c3 * ia;
+    w4 = c4 * ia;
+  }
   return base + w1 * v[0] + w2 * v[1] + w3 * v[2] + w4 * v[3];
 }
 
