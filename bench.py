@@ -589,7 +589,7 @@ def run_gpu(args):
     return result
 
 
-def cpu_baseline(budget_s=20.0, n=48):
+def cpu_baseline(budget_s=20.0, n=48, wall_num=(64, 48, 32)):
     """The CPU oracle (all host threads) on a bounded sample of the same workload:
     whole SSP-RK3 steps (sensors, 3 x (chemistry, Euler Z/Y/X, diffusion Z/Y/X,
     RK update, primitive and property refresh)) of an n^3 box, the same work
@@ -615,9 +615,51 @@ def cpu_baseline(budget_s=20.0, n=48):
         if time.perf_counter() - t0 > budget_s or steps >= 200:
             break
     el = time.perf_counter() - t0
-    return {"value": 3.0 * steps * fl.ncells / el, "unit": UNIT, "cores": threads, "kind": kind,
-            "sample": f"{steps} SSP-RK3 steps (3 cell-updates per cell each) of a {n}^3 box of the same "
-                      f"workload, {el:.1f} s, OpenMP over all host threads"}
+    out = {"value": 3.0 * steps * fl.ncells / el, "unit": UNIT, "cores": threads, "kind": kind,
+           "sample": f"{steps} SSP-RK3 steps (3 cell-updates per cell each) of a {n}^3 box of the same "
+                     f"workload, {el:.1f} s, OpenMP over all host threads"}
+    if wall_num:
+        out["wall"] = cpu_wall_baseline(lib, kind, wall_num, budget_s=budget_s / 2)
+    return out
+
+
+def cpu_wall_baseline(lib, kind, num, budget_s=10.0):
+    """The boundary-layer step (task composition of wall.BoundaryRun) on the
+    CPU oracle over a bounded sample grid of the same workload; the
+    Regent-defined pieces come from the port when the compiled reference
+    lacks them."""
+    import oracle
+    from htr_gb300 import wall
+    port = oracle.port_lib()
+    fl = wall.boundary_layer(num=num, seed=77)
+    fl.meta["grid"].fill(fl, port)
+    m = workloads.make_mixture_struct(lib, abi.HTR_EOS_AIRMIX, fl.meta["mix"])
+    h = oracle.load_mixture(lib, abi.HTR_EOS_AIRMIX, m)
+    workloads.derive_state(lib, fl, h)
+    bc = fl.meta["bc"]
+    P = bc["xNeg"][1]["P"]
+    Ls = (bc["xPos"][1]["LengthScale"], bc["yPos"][1]["LengthScale"])
+    if kind == "port":
+        run = wall.BoundaryRun(port, fl, h, bc)
+        dt = run.spectral_dt(0.8)
+        step = lambda: run.step(dt)
+    else:
+        hp = oracle.load_mixture(port, abi.HTR_EOS_AIRMIX, workloads.make_mixture_struct(port, abi.HTR_EOS_AIRMIX,
+                                                                                         fl.meta["mix"]))
+        dt = wall.BoundaryRun(port, fl, hp, bc).spectral_dt(0.8)
+        step = lambda: oracle.boundary_layer_step(lib, fl, h, dt, P, P, Ls, regent=port, regent_mix=hp)
+    steps = 0
+    t0 = time.perf_counter()
+    while True:
+        step()
+        steps += 1
+        if time.perf_counter() - t0 > budget_s or steps >= 50:
+            break
+    el = time.perf_counter() - t0
+    cells = num[0] * num[1] * num[2]
+    return {"value": 3.0 * steps * cells / el, "unit": UNIT, "kind": kind,
+            "sample": f"{steps} boundary-layer SSP-RK3 steps of {num[0]}x{num[1]}x{num[2]} interior cells of the "
+                      f"same workload, {el:.1f} s"}
 
 
 def run_reference(args):
@@ -628,7 +670,7 @@ def run_reference(args):
     # K timed samples after W warm-up samples, each a bounded RHS sample
     vals = []
     for i in range(args.warmup + args.steps):
-        b = cpu_baseline(budget_s=max(2.0, args.cpu_seconds / max(1, args.steps + args.warmup)))
+        b = cpu_baseline(budget_s=max(2.0, args.cpu_seconds / max(1, args.steps + args.warmup)), wall_num=None)
         if i >= args.warmup:
             vals.append(b["value"])
     value = float(np.median(vals)) if vals else base["value"]
@@ -639,7 +681,7 @@ def run_reference(args):
                                    f"diffusion + explicit chemistry, SSP-RK3", "grid": [args.n] * 3,
                        "sample_grid": [48] * 3},
             "cpu_baseline": {"value": value, "unit": UNIT, "cores": base["cores"], "kind": base["kind"],
-                             "sample": base["sample"]},
+                             "sample": base["sample"], "wall": base.get("wall")},
             "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
 
 

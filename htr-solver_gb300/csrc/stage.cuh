@@ -51,11 +51,11 @@ struct TenoEntry {
 struct StageWorkspace {
   double *fe[3];    // Euler face fluxes, [NE][nf[D]]
   double *fd[3];    // diffusion face fluxes, [NE][nf[D]]
-  TenoEntry *queue; // capacity nf[0]+nf[1]+nf[2]
-  unsigned *count;  // queue length
+  TenoEntry *queue; // capacity nf[0]+nf[1]+nf[2]: the faces of direction D from offset nf[0]+..+nf[D-1]
+  unsigned *count;  // queue lengths of the three directions
   double *prep;     // per-cell prepass values, [kPrepVals][ncell]
   double *tcache;   // per cell: T it was computed for, log(T TRef), 1/(T TRef); [3][ncell]
-  double *scalars;  // 3 doubles in the queue counter's 256-byte block (maximum Mach number per direction)
+  double *scalars;  // 3 doubles in the queue counters' 256-byte block (maximum Mach number per direction)
 };
 
 // per-cell prepass values: velocity-gradient tensor (9), mixture molar

@@ -59,19 +59,18 @@ HTR_D void teno_face_at(const StageTenoArgs &A, const Mix &mix, const long long 
   for (int i = 0; i < NE; i++) out[i * nf + fi] = F[i];
 }
 
-template <class Mix, int KIND>
+// The queued faces of direction D (one launch per direction: a launch holds
+// one direction's code).
+template <class Mix, int D, int KIND>
 __global__ void __launch_bounds__(128) euler_teno_faces(const StageTenoArgs A, const __grid_constant__ Mix mix) {
-  const long long n = (long long)*A.count;
+  long long off = 0;
+#pragma unroll
+  for (int d = 0; d < D; d++) off += A.g.nf[d];
+  const long long n = (long long)A.count[D];
   for (long long k = blockIdx.x * (long long)blockDim.x + threadIdx.x; k < n; k += (long long)gridDim.x * blockDim.x) {
-    const TenoEntry e = A.queue[k];
-    const int D = e.D;
+    const TenoEntry e = A.queue[off + k];
     const long long c[3] = {e.c0, e.c1, e.c2};
-    if (D == 0)
-      teno_face_at<Mix, 0, KIND>(A, mix, c);
-    else if (D == 1)
-      teno_face_at<Mix, 1, KIND>(A, mix, c);
-    else
-      teno_face_at<Mix, 2, KIND>(A, mix, c);
+    teno_face_at<Mix, D, KIND>(A, mix, c);
   }
 }
 
@@ -131,7 +130,7 @@ cudaError_t launch_stage_euler(const htr_fluid_view &v, const htr_rect3 &my, con
   const FaceGrid g = face_grid(my);
   cudaError_t e = cudaSuccess;
   if (p.scheme != 2) {
-    if ((e = cudaMemsetAsync(w.count, 0, sizeof(unsigned), s)) != cudaSuccess) return e;
+    if ((e = cudaMemsetAsync(w.count, 0, 3 * sizeof(unsigned), s)) != cudaSuccess) return e;
     for (int k = 0; k < 3; k++) {
       const int D = order[k];
       if (!(p.active & (1u << D))) {
@@ -143,8 +142,10 @@ cudaError_t launch_stage_euler(const htr_fluid_view &v, const htr_rect3 &my, con
       A.H = H;
       A.g = g;
       A.fe = w.fe[D];
-      A.queue = w.queue;
-      A.count = w.count;
+      long long off = 0;
+      for (int d = 0; d < D; d++) off += g.nf[d];
+      A.queue = w.queue + off;
+      A.count = w.count + D;
       e = launch_kg_faces(A, mix, D, p.scheme == 0, s);
       if (e != cudaSuccess || (e = mark(k)) != cudaSuccess) return e;
     }
@@ -178,10 +179,17 @@ cudaError_t launch_stage_euler(const htr_fluid_view &v, const htr_rect3 &my, con
     }
     return mark(3);
   }
-  // the hybrid scheme's sensor-rejected faces (plain TENO, rhs.inl:622-759)
+  // the hybrid scheme's sensor-rejected faces (plain TENO, rhs.inl:622-759),
+  // one launch per direction over that direction's queue
   dim3 grid((unsigned)(sms * stage_tuning().teno_blocks_per_sm));
-  euler_teno_faces<Mix, kTENO><<<grid, 128, 0, s>>>(T, mix);
-  if ((e = cudaGetLastError()) != cudaSuccess) return e;
+  for (int k = 0; k < 3; k++) {
+    const int D = order[k];
+    if (!(p.active & (1u << D))) continue;
+    if (D == 0) euler_teno_faces<Mix, 0, kTENO><<<grid, 128, 0, s>>>(T, mix);
+    else if (D == 1) euler_teno_faces<Mix, 1, kTENO><<<grid, 128, 0, s>>>(T, mix);
+    else euler_teno_faces<Mix, 2, kTENO><<<grid, 128, 0, s>>>(T, mix);
+    if ((e = cudaGetLastError()) != cudaSuccess) return e;
+  }
   return mark(3);
 }
 
