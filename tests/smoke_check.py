@@ -1,4 +1,6 @@
-"""One small hybrid RHS evaluation on cuda:0 checked against the CPU oracle."""
+"""Small invocations of the hot path on cuda:0 checked against the CPU oracle:
+one hybrid RHS evaluation of a periodic box, and one fused SSP-RK3 step of a
+boundary-layer grid (metrics on the device, TENO-LAD, NSCBC and wall rules)."""
 import ctypes as C
 
 import numpy as np
@@ -38,7 +40,31 @@ def run():
         assert np.array_equal(out[f"shockSensor{d}"], host[f"shockSensor{d}"]), d
     err = util.rel_err(out["Conserved_t"], host["Conserved_t"]).max()
     assert err <= util.RHS_REL_TOL, err
-    print(f"smoke ok: max rel err {err:.3e}")
+
+    # boundary layer: the device metrics equal the port's; one fused step
+    # equals the oracle's step within the RHS tolerance
+    from htr_gb300 import wall, workloads
+    bl = wall.boundary_layer(num=(12, 8, 4), seed=2)
+    g = bl.meta["grid"]
+    g.fill(bl, port)
+    mb = workloads.make_mixture_struct(port, bl.meta["eos"], bl.meta["mix"])
+    hb = oracle.load_mixture(port, bl.meta["eos"], mb)
+    workloads.derive_state(port, bl, hb)
+    dev = bl.to_device("cuda:0")
+    g.fill(dev, gpu)
+    torch.cuda.synchronize()
+    met = dev.to_host()
+    for name in ("dcsi_e", "deta_e", "deta_d", "deta_s"):
+        assert np.array_equal(met[name], bl[name]), name
+    bc = bl.meta["bc"]
+    dt = wall.BoundaryRun(port, bl, hb, bc).spectral_dt(0.8)
+    oracle.boundary_layer_step(port, bl, hb, dt, bc["xNeg"][1]["P"], bc["xPos"][1]["P"],
+                               (bc["xPos"][1]["LengthScale"], bc["yPos"][1]["LengthScale"]))
+    wall.FusedBoundaryRun(dev, runtime.load_mixture(bl.meta["eos"], mb), bc).step(dt)
+    torch.cuda.synchronize()
+    err2 = util.rel_err(dev.to_host()["Conserved"], bl["Conserved"]).max()
+    assert err2 <= util.RHS_REL_TOL, err2
+    print(f"smoke ok: max rel err {err:.3e} (hybrid RHS), {err2:.3e} (boundary-layer step)")
 
 
 if __name__ == "__main__":

@@ -262,3 +262,49 @@ def test_gpu_fused_boundary_cfl_and_errors():
     bad.params.plane[0] = abi.rect((1, 0, 0), (1, 11, 3))  # not the ghost layer
     with pytest.raises(abi.HtrError):
         bad.step(dt)
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("scheme", ["TENO", "TENOA"])
+def test_gpu_fused_boundary_other_schemes(scheme):
+    import torch
+    port = oracle.port_lib()
+    host, hp, m = _bl(port, num=(16, 12, 4))
+    dev = host.to_device("cuda")
+    gh = runtime.load_mixture(host.meta["eos"], m)
+    dt = wall.BoundaryRun(port, host, hp, host.meta["bc"], scheme=scheme).spectral_dt(0.8)
+    bc = host.meta["bc"]
+    oracle.boundary_layer_step(port, host, hp, dt, bc["xNeg"][1]["P"], bc["xPos"][1]["P"],
+                               (bc["xPos"][1]["LengthScale"], bc["yPos"][1]["LengthScale"]), scheme=scheme)
+    wall.FusedBoundaryRun(dev, gh, bc, scheme=scheme).step(dt)
+    torch.cuda.synchronize()
+    err = util.rel_err(dev.to_host()["Conserved"], host["Conserved"])
+    assert err.max() <= util.RHS_REL_TOL, err
+
+
+@pytest.mark.gpu
+def test_gpu_fused_boundary_step_graph_capture():
+    """With a fixed dt the fused boundary step issues no host synchronisation:
+    a captured step replays to the same bits as the direct call."""
+    import torch
+    port = oracle.port_lib()
+    host, hp, m = _bl(port, num=(16, 12, 4))
+    gh = runtime.load_mixture(host.meta["eos"], m)
+    dt = wall.BoundaryRun(port, host, hp, host.meta["bc"]).spectral_dt(0.8)
+    a = host.to_device("cuda")
+    b = host.to_device("cuda")
+    wall.FusedBoundaryRun(a, gh, host.meta["bc"]).step(dt)
+    run_b = wall.FusedBoundaryRun(b, gh, host.meta["bc"])
+    s = torch.cuda.Stream()
+    torch.cuda.synchronize()
+    g = torch.cuda.CUDAGraph()
+    with torch.cuda.stream(s):
+        run_b.stream = s
+        g.capture_begin(capture_error_mode="relaxed")
+        run_b.step(dt)
+        g.capture_end()
+    g.replay()
+    torch.cuda.synchronize()
+    oa, ob = a.to_host(), b.to_host()
+    for name in ("Conserved", "temperature", "pressure", "dudtBoundary"):
+        assert np.array_equal(oa[name], ob[name]), name
