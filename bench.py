@@ -203,6 +203,12 @@ KERNEL_BYTES = {
     # -> Conserved_t, Conserved, T, p, rho, mu, lam, SoS, X, u, Di, Y
     "stage_update": 8 * (6 * NE + 6 + NS + 3 + 2 * NE) + 8 * (2 * NE + 6 + NS + 3 + NS + NS),
 }
+# Executed FP64 floating-point operations per cell (per face for the face
+# kernels) of the same kernels: DADD + DMUL + 2 x DFMA thread instructions
+# counted by ncu on the 96^3 case of this workload (profiles/
+# stage_kernels_air96_hybrid.md).  The kernels are bound by the FP64 pipe;
+# this gives their achieved FP64 rate next to the memory roofline.
+KERNEL_FP64_FLOPS = {"prepass": 80.0, "kg_faces": 259.0, "diffusion_faces": 320.0, "stage_update": 2559.0}
 
 
 STATE_FIELDS = ["Conserved", "pressure", "temperature", "MassFracs", "MolarFracs", "velocity",
@@ -555,7 +561,15 @@ def run_gpu(args):
                          "unit": "GB/s", "frac": (achieved / peak) if achieved else None,
                          "peak_source": peak_src, "traffic": None, "bytes_per_launch": bytes_launch,
                          "bytes_per_cell": per_cell, "launch_ms": prof[dominant]},
-            "fp64": {"peak_tflops_probe": fp64, "note": "measured in this run by a DFMA-chain probe"},
+            "fp64": {"peak_tflops_probe": fp64, "note": "measured in this run by a DFMA-chain probe",
+                     "kernel": dominant,
+                     "flops_per_cell": KERNEL_FP64_FLOPS.get(fdom),
+                     "achieved_tflops": (KERNEL_FP64_FLOPS[fdom] * ncell / (prof[dominant] * 1e-3) / 1e12
+                                         if fdom in KERNEL_FP64_FLOPS else None),
+                     "frac": (KERNEL_FP64_FLOPS[fdom] * ncell / (prof[dominant] * 1e-3) / 1e12 / fp64
+                              if fdom in KERNEL_FP64_FLOPS and fp64 else None),
+                     "bound": "fp64 pipe (DADD/DMUL/DFMA plus compares, conversions and the "
+                              "division/sqrt sequences)"},
             "kernel_ms_per_stage": prof,
             # per step: Ducros + shock sensors + Conserved_old copy, then per stage
             # prepass, 3 KG, 1 TENO, 3 diffusion, 1 update
