@@ -1,7 +1,8 @@
 """Wall-bounded grids: a Mach-6 boundary layer over an isothermal wall, and
 time steps of grids with boundary conditions.
 
-Workload `boundary_layer`: 5-species air (AirMix) on a stretched grid, inflow
+Workloads.  `channel`: a periodic channel between an isothermal and an
+adiabatic wall.  `boundary_layer`: 5-species air (AirMix) on a stretched grid, inflow
 and outflow in x, an isothermal wall at yNeg and an outflow at yPos, periodic
 z (the boundary types of HTR's flat-plate boundary-layer cases,
 testcases/MultispeciesTBL).  The wall-normal axis is tanh-stretched towards
@@ -100,6 +101,54 @@ def boundary_layer(num=(512, 192, 128), seed=0, mach=6.0, T_inf=220.0, p_inf=1.0
                                         yNeg=("IsothermalWall", {}),
                                         yPos=("NSCBC_Outflow", {"P": P, "LengthScale": width[1]}),
                                         zNeg=(PERIODIC, {}), zPos=(PERIODIC, {})),
+                   scheme="TENOLAD", cfl=0.8, mach=mach)
+    return fl
+
+
+def channel(num=(64, 48, 32), seed=0, mach=0.5, T_wall=300.0, p0=1.0e5, width=(0.06, 0.02, 0.03),
+            stretching=1.5, noise=0.01):
+    """Host Fluid of a wall-bounded channel: periodic x and z, an isothermal
+    wall (300 K) at yNeg and an adiabatic wall at yPos, both tanh-clustered
+    (Tanh stretching), 5-species air, a parabolic streamwise velocity of
+    centre-line Mach `mach` with 1 % seeded noise, uniform temperature and
+    pressure.  Node types are set; metrics are filled by `Grid.fill`."""
+    bc = ((PERIODIC, PERIODIC), ("IsothermalWall", "AdiabaticWall"), (PERIODIC, PERIODIC))
+    g = Grid(num, width, bc, kind=(("Uniform", 1.0), ("Tanh", stretching), ("Uniform", 1.0)))
+    nx, ny, nz = g.shape
+    rng = np.random.Generator(np.random.PCG64(seed))
+    ref = AIR_REF
+    Y = np.array([0.767, 0.233, 1.0e-4, 1.0e-6, 1.0e-5])
+    Y = Y / Y.sum()
+    X = (Y / W_AIR) / (Y / W_AIR).sum()
+    MixW = float((X * W_AIR).sum())
+    U = mach * math.sqrt(1.4 * RGAS / MixW * T_wall)
+    eta = np.clip(g.center[1] / width[1], 0.0, 1.0)
+    shape3 = (nz, ny, nx)
+    u = np.zeros(shape3 + (3,))
+    u[..., 0] = (4.0 * U * eta * (1.0 - eta))[None, :, None]
+    for k in range(3):
+        u[..., k] += noise * U * rng.uniform(-1.0, 1.0, size=shape3)
+    u[:, 0] = 0.0
+    u[:, -1] = 0.0
+    XiRef = np.where(np.array(ref["XiRef"]) > 0, np.array(ref["XiRef"]), 1e-60)
+    MixWRef = float((XiRef * W_AIR).sum())
+    rhoRef = ref["PRef"] * MixWRef / (RGAS * ref["TRef"])
+    uRef = math.sqrt(ref["PRef"] / rhoRef)
+    fl = Fluid(g.shape, 5)
+    fl["pressure"] = p0 * (1.0 + noise * rng.uniform(-1.0, 1.0, size=shape3)) / ref["PRef"]
+    fl["temperature"] = T_wall * (1.0 + noise * rng.uniform(-1.0, 1.0, size=shape3)) / ref["TRef"]
+    fl["MolarFracs"] = X
+    fl["velocity"] = u / uRef
+    fl["MolarFracs_profile"] = X
+    fl["temperature_profile"] = T_wall / ref["TRef"]
+    fl["velocity_profile"] = 0.0
+    for name, d in (("nType_x", 0), ("nType_y", 1), ("nType_z", 2)):
+        idx = [None, None, None]
+        idx[2 - d] = slice(None)
+        fl[name] = np.broadcast_to(g.ntype[d][tuple(idx)], shape3)
+    fl.meta = dict(workload="channel", eos=abi.HTR_EOS_AIRMIX, seed=seed, mix=dict(ref), grid=g, bnum=g.bnum,
+                   bc=dict(xNeg=(PERIODIC, {}), xPos=(PERIODIC, {}), yNeg=("IsothermalWall", {}),
+                           yPos=("AdiabaticWall", {}), zNeg=(PERIODIC, {}), zPos=(PERIODIC, {})),
                    scheme="TENOLAD", cfl=0.8, mach=mach)
     return fl
 

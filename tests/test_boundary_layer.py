@@ -308,3 +308,56 @@ def test_gpu_fused_boundary_step_graph_capture():
     oa, ob = a.to_host(), b.to_host()
     for name in ("Conserved", "temperature", "pressure", "dudtBoundary"):
         assert np.array_equal(oa[name], ob[name]), name
+
+
+def _channel(lib, num=(12, 10, 6), seed=4):
+    fl = wall.channel(num=num, seed=seed)
+    fl.meta["grid"].fill(fl, lib)
+    m = workloads.make_mixture_struct(lib, fl.meta["eos"], fl.meta["mix"])
+    h = oracle.load_mixture(lib, fl.meta["eos"], m)
+    workloads.derive_state(lib, fl, h)
+    return fl, h, m
+
+
+def test_channel_zones_and_step():
+    """Walls on both sides of y, periodic x and z: no NSCBC point, every wall
+    ghost unsolved; one step on the port keeps the walls at rest and the
+    isothermal wall at its temperature."""
+    port = oracle.port_lib()
+    fl, h, _ = _channel(port)
+    z = zones.partition(fl.shape, (0, 1, 0), (("Periodic", "Periodic"), ("IsothermalWall", "AdiabaticWall"),
+                                              ("Periodic", "Periodic")))
+    assert z.solved == [z.interior] and all(d == [z.interior] for d in z.divg)
+    assert _points(z.planes[2]) == _points([((0, 0, 0), (11, 0, 5))])
+    run = wall.BoundaryRun(port, fl, h, fl.meta["bc"])
+    dt = run.spectral_dt(0.8)
+    before = fl.copy()
+    run.step(dt)
+    assert np.all(fl["velocity"][:, 0] == 0.0) and np.all(fl["velocity"][:, -1] == 0.0)
+    assert np.all(fl["temperature"][:, 0] == fl["temperature_profile"][:, 0])
+    assert np.array_equal(fl["temperature"][:, -1], fl["temperature"][:, -2])  # adiabatic: copied
+    assert np.all(np.isfinite(fl["Conserved"])) and not np.array_equal(fl["Conserved"], before["Conserved"])
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("fused", [False, True])
+def test_gpu_channel_step(fused):
+    import torch
+    port = oracle.port_lib()
+    host, hp, m = _channel(port)
+    dev = host.to_device("cuda")
+    gh = runtime.load_mixture(host.meta["eos"], m)
+    ref_run = wall.BoundaryRun(port, host, hp, host.meta["bc"])
+    dt = ref_run.spectral_dt(0.8)
+    ref_run.step(dt)
+    if fused:
+        wall.FusedBoundaryRun(dev, gh, host.meta["bc"]).step(dt)
+    else:
+        mach = torch.zeros(1, dtype=torch.float64, device="cuda")
+        wall.BoundaryRun(runtime.lib(), dev, gh, host.meta["bc"], stream=runtime.stream_handle(),
+                         max_mach_buffer=mach).step(dt)
+    torch.cuda.synchronize()
+    out = dev.to_host()
+    err = util.rel_err(out["Conserved"], host["Conserved"])
+    assert err.max() <= util.RHS_REL_TOL, err
+    assert np.all(out["velocity"][:, 0] == 0.0) and np.all(out["velocity"][:, -1] == 0.0)
