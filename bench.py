@@ -209,6 +209,10 @@ KERNEL_BYTES = {
 # stage_kernels_air96_hybrid.md).  The kernels are bound by the FP64 pipe;
 # this gives their achieved FP64 rate next to the memory roofline.
 KERNEL_FP64_FLOPS = {"prepass": 80.0, "kg_faces": 259.0, "diffusion_faces": 320.0, "stage_update": 2559.0}
+# DRAM bytes per cell (dram__bytes_read.sum + dram__bytes_write.sum of one
+# launch) measured by ncu on the 96^3 case (state larger than L2); the
+# per-launch traffic scales with the cells (profiles/stage_kernels_air96_hybrid.md).
+KERNEL_DRAM_BYTES = {"prepass": 248.0, "kg_faces": 124.0, "diffusion_faces": 316.0, "stage_update": 1029.0}
 
 
 STATE_FIELDS = ["Conserved", "pressure", "temperature", "MassFracs", "MolarFracs", "velocity",
@@ -559,7 +563,9 @@ def run_gpu(args):
                               "double-buffered on copy streams overlapping the previous step"},
             "roofline": {"bound": "hbm", "kernel": dominant, "achieved": achieved, "peak": peak,
                          "unit": "GB/s", "frac": (achieved / peak) if achieved else None,
-                         "peak_source": peak_src, "traffic": None, "bytes_per_launch": bytes_launch,
+                         "peak_source": peak_src,
+                         "traffic": KERNEL_DRAM_BYTES[fdom] * ncell if fdom in KERNEL_DRAM_BYTES else None,
+                         "traffic_source": "ncu DRAM bytes per cell at 96^3 x cells", "bytes_per_launch": bytes_launch,
                          "bytes_per_cell": per_cell, "launch_ms": prof[dominant]},
             "fp64": {"peak_tflops_probe": fp64, "note": "measured in this run by a DFMA-chain probe",
                      "kernel": dominant,
