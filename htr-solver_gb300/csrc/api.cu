@@ -800,10 +800,17 @@ int htr_rk3_step_bc_ws(const htr_fluid_view *v, htr_rect3 inner, htr_rect3 fb, c
   if ((st = check_common(v, m, inner))) return st;
   if ((st = check_step_fields(v, m))) return st;
   if (p == nullptr) return fail(HTR_ERR_ARGUMENT, "null step parameters%s");
-  if (p->scheme == HTR_SCHEME_HYBRID)
-    return fail(HTR_ERR_UNSUPPORTED, "the boundary step runs the TENO, TENO-A, TENO-LAD and skew-symmetric schemes%s");
   if (p->scheme < HTR_SCHEME_HYBRID || p->scheme > HTR_SCHEME_SKEW) return fail(HTR_ERR_ARGUMENT, "unknown scheme%s");
   if ((st = check_bc_params(v, inner, fb, bc))) return st;
+  const bool hybrid = p->scheme == HTR_SCHEME_HYBRID;
+  if (hybrid) {
+    for (int d = 0; d < 3; d++)
+      if (!rect_ok(bc->sensor[d]) || !inside(bc->sensor[d], fb))
+        return fail(HTR_ERR_ARGUMENT, "a sensor zone lies outside the grid%s");
+    if ((st = check_field(v->DucrosSensor, 8, "DucrosSensor")) || (st = check_field(v->shockSensorX, 1, "shockSensorX")) ||
+        (st = check_field(v->shockSensorY, 1, "shockSensorY")) || (st = check_field(v->shockSensorZ, 1, "shockSensorZ")))
+      return st;
+  }
   htr::StageWorkspace w;
   if (!htr::stage_workspace_carve(workspace, workspace_bytes, fb, neq_of(m), w))
     return fail(HTR_ERR_ARGUMENT, "workspace null or smaller than htr_rk3_workspace_bytes(fluid_bounds)%s");
@@ -820,9 +827,17 @@ int htr_rk3_step_bc_ws(const htr_fluid_view *v, htr_rect3 inner, htr_rect3 fb, c
   }
   if (!(dt > 0.0)) return fail(HTR_ERR_ARGUMENT, "non-positive time step%s");
   if (dt_used) *dt_used = dt;
+  if (hybrid) {
+    // UpdateShockSensors (src/prometeo_sensor.rg:96-125): Ducros over p_All,
+    // the shock sensor of each direction over its faces zone
+    if ((st = htr_UpdateDucrosSensor(v, fb, fb, p->vorticityScale, s))) return st;
+    for (int d = 0; d < 3; d++)
+      if ((st = cuda_status(htr::launch_shock_sensor(*v, bc->sensor[d], fb, nspec_of(m), 1 << d, cs), "shock sensor")))
+        return st;
+  }
   if ((st = htr_InitializeTemporaries(v, fb, m, s))) return st;
   htr::StageParams sp;
-  sp.scheme = p->scheme == HTR_SCHEME_SKEW ? 1 : 2;
+  sp.scheme = hybrid ? 0 : (p->scheme == HTR_SCHEME_SKEW ? 1 : 2);
   sp.kind = p->scheme == HTR_SCHEME_TENOA ? htr::kTENOA : (p->scheme == HTR_SCHEME_TENOLAD ? htr::kTENOLAD : htr::kTENO);
   sp.chemistry = p->explicitChemistry ? 1 : 0;
   sp.dt = dt;

@@ -27,7 +27,7 @@ SCHEMES = {"Hybrid": 0, "TENO": 1, "TENOA": 2, "TENOLAD": 3, "SkewSymmetric": 4}
 
 class htr_bc_params(C.Structure):
     _fields_ = [("type", C.c_int * 6), ("P", C.c_double * 6), ("LengthScale", C.c_double * 6),
-                ("plane", abi.htr_rect3 * 6)]
+                ("plane", abi.htr_rect3 * 6), ("sensor", abi.htr_rect3 * 3)]
 
 
 BC_TYPES = {"Periodic": 0, "NSCBC_Inflow": 1, "NSCBC_Outflow": 2, "IsothermalWall": 3, "AdiabaticWall": 4}

@@ -94,6 +94,8 @@ def boundary_layer(num=(512, 192, 128), seed=0, mach=6.0, T_inf=220.0, p_inf=1.0
         idx = [None, None, None]
         idx[2 - d] = slice(None)
         fl[name] = np.broadcast_to(g.ntype[d][tuple(idx)], shape3)
+    for name in ("shockSensorX", "shockSensorY", "shockSensorZ"):
+        fl[name] = True  # the reference's initial value (src/prometeo.rg:335-338)
     P = p_inf / ref["PRef"]
     fl.meta = dict(workload="boundary_layer", eos=abi.HTR_EOS_AIRMIX, seed=seed, mix=dict(ref), grid=g,
                    bnum=g.bnum, bc=dict(xNeg=("NSCBC_Inflow", {"P": P}),
@@ -146,6 +148,8 @@ def channel(num=(64, 48, 32), seed=0, mach=0.5, T_wall=300.0, p0=1.0e5, width=(0
         idx = [None, None, None]
         idx[2 - d] = slice(None)
         fl[name] = np.broadcast_to(g.ntype[d][tuple(idx)], shape3)
+    for name in ("shockSensorX", "shockSensorY", "shockSensorZ"):
+        fl[name] = True
     fl.meta = dict(workload="channel", eos=abi.HTR_EOS_AIRMIX, seed=seed, mix=dict(ref), grid=g, bnum=g.bnum,
                    bc=dict(xNeg=(PERIODIC, {}), xPos=(PERIODIC, {}), yNeg=("IsothermalWall", {}),
                            yPos=("AdiabaticWall", {}), zNeg=(PERIODIC, {}), zPos=(PERIODIC, {})),
@@ -163,13 +167,16 @@ class BoundaryRun:
     bc      {side: (FlowBC type, params)} for the six sides (xNeg ... zPos);
             NSCBC_Inflow takes P (the pressure of a supersonic inflow),
             NSCBC_Outflow takes P and LengthScale
-    scheme  one of TENO, TENOA, TENOLAD, SkewSymmetric (the hybrid scheme's
-            sensor zones near boundaries are not modelled here)
+    scheme  one of Hybrid, TENO, TENOA, TENOLAD, SkewSymmetric; the hybrid
+            scheme updates the Ducros sensor everywhere and the shock sensor
+            of direction d over its faces zone once per step
+            (UpdateShockSensors, src/prometeo_sensor.rg:96-125)
     max_mach_buffer  where htr_CalculateMaxMachNumber writes: a device
             pointer for the CUDA library, None (a host double) for a CPU build
     """
 
-    def __init__(self, lib, fl, mixh, bc, scheme="TENOLAD", chemistry=True, stream=None, max_mach_buffer=None):
+    def __init__(self, lib, fl, mixh, bc, scheme="TENOLAD", chemistry=True, stream=None, max_mach_buffer=None,
+                 vorticity_scale=1.0):
         self.lib, self.fl, self.mixh = lib, fl, mixh
         self.types = [bc[s][0] for s in zones.SIDES]
         self.params = [bc[s][1] for s in zones.SIDES]
@@ -179,9 +186,9 @@ class BoundaryRun:
         axes = tuple((self.types[2 * d], self.types[2 * d + 1]) for d in range(3))
         self.bnum = tuple(0 if a[0] == PERIODIC else 1 for a in axes)
         self.z = zones.partition(fl.shape, self.bnum, axes)
-        if scheme not in ("TENO", "TENOA", "TENOLAD", "SkewSymmetric"):
+        if scheme not in ("Hybrid", "TENO", "TENOA", "TENOLAD", "SkewSymmetric"):
             raise abi.HtrError(f"scheme {scheme} is not supported by this driver")
-        self.scheme, self.chemistry = scheme, chemistry
+        self.scheme, self.chemistry, self.vs = scheme, chemistry, vorticity_scale
         self.stream = stream
         self.mach_buf = max_mach_buffer
         self.all = abi.rect(*self.z.all)
@@ -190,6 +197,7 @@ class BoundaryRun:
         self.divg = [_rects(r) for r in self.z.divg]
         self.planes = [_rects(p) for p in self.z.planes]
         self.all_bcs = _rects(self.z.all_bcs)
+        self.faces = [_rects(f) for f in self.z.faces]
 
     def _ck(self, st, what):
         abi.check(self.lib, st, what)
@@ -217,6 +225,16 @@ class BoundaryRun:
         self._ck(self.lib.htr_CalculateMaxSpectralRadius(C.byref(v), self.interior, self.mixh, ptr, self.stream),
                  "cfl")
         return cfl / float(self.mach_buf.item())
+
+    def sensors(self):
+        """UpdateShockSensors (src/prometeo_sensor.rg:96-125)."""
+        v = self.fl.view()
+        fb = self.fl.bounds()
+        self._ck(self.lib.htr_UpdateDucrosSensor(C.byref(v), self.all, fb, self.vs, self.stream), "ducros")
+        for d in range(3):
+            fn = getattr(self.lib, f"htr_UpdateShockSensor{'XYZ'[d]}")
+            for r in self.faces[d]:
+                self._ck(fn(C.byref(v), r, fb, self.mixh, self.stream), "shock sensor")
 
     def derivatives(self, stage, dt):
         """UpdateDerivatives (src/prometeo.rg:480-606)."""
@@ -288,6 +306,8 @@ class BoundaryRun:
         """One SSP-RK3 step; returns the step size."""
         if dt is None:
             dt = self.spectral_dt(cfl)
+        if self.scheme == "Hybrid":
+            self.sensors()
         v = self.fl.view()
         self._ck(self.lib.htr_InitializeTemporaries(C.byref(v), self.all, self.mixh, self.stream), "temporaries")
         for stage in (1, 2, 3):
@@ -308,7 +328,8 @@ class FusedBoundaryRun:
     into its per-cell kernel (CUDA library, device fields).  With a fixed dt
     the step issues no host synchronisation and can be graph-captured."""
 
-    def __init__(self, fl, mixh, bc, scheme="TENOLAD", chemistry=True, stream=None, workspace=None):
+    def __init__(self, fl, mixh, bc, scheme="TENOLAD", chemistry=True, stream=None, workspace=None,
+                 vorticity_scale=1.0):
         from . import runtime
         self.rt = runtime
         self.lib = runtime.lib()
@@ -330,8 +351,13 @@ class FusedBoundaryRun:
                 if len(z.planes[k]) != 1:
                     raise abi.HtrError(f"boundary plane {zones.SIDES[k]} is not one rectangle")
                 self.params.plane[k] = abi.rect(*z.planes[k][0])
+        for d in range(3):
+            if len(z.faces[d]) != 1:
+                raise abi.HtrError(f"sensor zone of direction {'xyz'[d]} is not one rectangle")
+            self.params.sensor[d] = abi.rect(*z.faces[d][0])
         self.interior = abi.rect(*z.interior)
         self.scheme = runtime.SCHEMES[scheme]
+        self.vs = vorticity_scale
         self.chemistry = chemistry
         self.stream = stream
         self.ws = workspace or runtime.Workspace()
@@ -340,7 +366,7 @@ class FusedBoundaryRun:
 
     def step(self, dt=0.0, cfl=0.0, status_dev=None):
         """One SSP-RK3 step with step size dt (or cfl > 0); returns the dt used."""
-        p = self.rt.htr_step_params(self.scheme, 1.0, cfl, dt, 1 if self.chemistry else 0)
+        p = self.rt.htr_step_params(self.scheme, self.vs, cfl, dt, 1 if self.chemistry else 0)
         v = self.fl.view()
         used = C.c_double(0.0)
         ws = self.ws.get(self.nbytes, self.fl.device)

@@ -16,6 +16,9 @@ covering the grid:
               (p_solved): the interior plus the faces, edges and corners of
               characteristic (NSCBC) boundaries in the other directions
               (src/prometeo_partitioner.rg:745-975)
+  faces[d]    points whose shock sensor of direction d is computed
+              (p_x_faces ...): the interior, the d-Neg ghost face, and for
+              NSCBC sides the faces and edges towards the Neg side of d
 
 The reference takes the z-side characteristic flags from the y sides' BC
 types (src/prometeo_partitioner.rg:782-783); with a periodic z axis, the case
@@ -90,6 +93,7 @@ class Zones:
     planes: list = field(default_factory=list)
     divg: list = field(default_factory=list)
     solved: list = field(default_factory=list)
+    faces: list = field(default_factory=list)
 
     @staticmethod
     def rect(box):
@@ -144,6 +148,36 @@ def partition(shape, bnum, bc, z_flags_from_y=True):
     z.divg = [_merge(r) for r in divg]
     z.solved = _merge(solved)
 
+    # sensor zones (the reconstruction colorings of the partitioner)
+    box_of = {code: boxes[k] for k, code in enumerate(REGIONS)}
+
+    def code(**ax):
+        c = ["I", "I", "I"]
+        for a, v in ax.items():
+            c["xyz".index(a)] = v
+        return "".join(c)
+
+    faces = [[boxes[0], box_of[code(**{"xyz"[d]: "N"})]] for d in range(3)]
+    for sd in range(6):
+        if not nscbc[sd]:
+            continue
+        a, sign = sd // 2, "NP"[sd % 2]
+        for b in range(3):
+            if b == a:
+                continue
+            faces[b].append(box_of[code(**{"xyz"[a]: sign})])
+            faces[b].append(box_of[code(**{"xyz"[a]: sign, "xyz"[b]: "N"})])
+    for a in range(3):
+        for b in range(a + 1, 3):
+            for sa in "NP":
+                for sb in "NP":
+                    if not (nscbc[2 * a + (sa == "P")] and nscbc[2 * b + (sb == "P")]):
+                        continue
+                    c = 3 - a - b
+                    faces[c].append(box_of[code(**{"xyz"[a]: sa, "xyz"[b]: sb})])
+                    faces[c].append(box_of[code(**{"xyz"[a]: sa, "xyz"[b]: sb, "xyz"[c]: "N"})])
+    z.faces = [_merge(_unique(f)) for f in faces]
+
     # all minus interior as disjoint slabs: x ghosts, then y ghosts within the
     # interior x range, then z ghosts within the interior x and y ranges
     slabs = []
@@ -156,6 +190,14 @@ def partition(shape, bnum, bc, z_flags_from_y=True):
             slabs.append((lo, hi))
     z.all_bcs = slabs
     return z
+
+
+def _unique(boxes):
+    out = []
+    for b in boxes:
+        if b not in out:
+            out.append(b)
+    return out
 
 
 def _merge(boxes):

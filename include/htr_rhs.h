@@ -355,8 +355,9 @@ int htr_rk3_step_ws(const htr_fluid_view *view, htr_rect3 interior, htr_rect3 fl
  * from their first interior point after it (walls z, y, x).  After the step
  * the inflow time derivatives.  Zones as the reference's partitioner makes
  * them: bc->plane[s] is the side's p_xNeg[0]... (its face plus the edges and
- * corners it wins).  Schemes TENO, TENO-A, TENO-LAD, skew-symmetric (the
- * hybrid scheme's sensors near boundaries are not modelled: UNSUPPORTED).
+ * corners it wins).  Schemes: all five; for the hybrid scheme the Ducros
+ * sensor is computed everywhere and the shock sensors once per step over
+ * bc->sensor[d] (UpdateShockSensors, src/prometeo_sensor.rg:96-125).
  * Workspace: htr_rk3_workspace_bytes(fluid_bounds, mix) bytes.  With cfl <= 0
  * the call issues no host synchronisation (CUDA-graph capturable). */
 typedef enum {
@@ -372,6 +373,9 @@ typedef struct {
   double P[6];           /* inflow: pressure of a supersonic inflow; outflow: PInf */
   double LengthScale[6]; /* outflow: relaxation length */
   htr_rect3 plane[6];    /* boundary points of each non-periodic side */
+  htr_rect3 sensor[3];   /* hybrid scheme: the points whose shock sensor of
+                            direction d is computed (p_x_faces ...); the others
+                            keep their value (true after initialisation) */
 } htr_bc_params;
 
 int htr_rk3_step_bc_ws(const htr_fluid_view *view, htr_rect3 interior, htr_rect3 fluid_bounds,

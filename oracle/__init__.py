@@ -168,17 +168,21 @@ def boundary_layer_zones(nx, ny, nz):
     (src/prometeo_partitioner.rg:431-1015): the xNeg-yNeg and xPos-yNeg edges
     go to the wall, xNeg-yPos to the inflow, xPos-yPos to both outflows; the
     flux divergence of x skips the x planes, that of y skips the y planes;
-    the wall plane is not solved."""
+    the wall plane is not solved.  Sensor zones (p_{x,y,z}_faces): the
+    interior and the Neg ghost face of the direction, plus the NSCBC x faces
+    and the yPos outflow face with their edges towards the Neg sides."""
     X0, X1, Y0, Y1, Z1 = 0, nx - 1, 0, ny - 1, nz - 1
     box = lambda x0, x1, y0, y1: ((x0, y0, 0), (x1, y1, Z1))
     return dict(
         all=box(X0, X1, Y0, Y1), interior=box(1, X1 - 1, 1, Y1 - 1), solved=box(X0, X1, 1, Y1),
         divg=(box(1, X1 - 1, 1, Y1), box(X0, X1, 1, Y1 - 1), box(X0, X1, 1, Y1)),
         xNeg=box(X0, X0, 1, Y1), xPos=box(X1, X1, 1, Y1), yNeg=box(X0, X1, Y0, Y0), yPos=box(1, X1, Y1, Y1),
+        faces=(box(X0, X1 - 1, 1, Y1), box(X0, X1, Y0, Y1 - 1), box(X0, X1, 1, Y1)),
         all_bcs=(box(X0, X0, Y0, Y1), box(X1, X1, Y0, Y1), box(1, X1 - 1, Y0, Y0), box(1, X1 - 1, Y1, Y1)))
 
 
-def boundary_layer_step(lib, fl, mixh, dt, P_in, P_out, L_out, scheme="TENOLAD", regent=None, regent_mix=None):
+def boundary_layer_step(lib, fl, mixh, dt, P_in, P_out, L_out, scheme="TENOLAD", regent=None, regent_mix=None,
+                        vorticity_scale=1.0):
     """One SSP-RK3 step of a boundary-layer grid (zones above) in the
     reference's order: MainLoopBody (src/prometeo.rg:1342-1486) with
     UpdateDerivatives (:480-606), the NSCBC outflow terms of x then y with
@@ -196,6 +200,12 @@ def boundary_layer_step(lib, fl, mixh, dt, P_in, P_out, L_out, scheme="TENOLAD",
     rc = lambda b: A.rect(*b)
     v = fl.view()
     fb = fl.bounds()
+    if scheme == "Hybrid":
+        # UpdateShockSensors (src/prometeo_sensor.rg:96-125)
+        A.check(lib, lib.htr_UpdateDucrosSensor(C.byref(v), rc(z["all"]), fb, vorticity_scale, None), "ducros")
+        for d in range(3):
+            fn = getattr(lib, f"htr_UpdateShockSensor{'XYZ'[d]}")
+            A.check(lib, fn(C.byref(v), rc(z["faces"][d]), fb, mixh, None), "shock")
     A.check(lib, lib.htr_InitializeTemporaries(C.byref(v), rc(z["all"]), mixh, None), "tmp")
     for s in range(1, 4):
         A.check(lib, lib.htr_InitializeTimeDerivatives(C.byref(v), rc(z["all"]), 0, mixh, None), "init_t")

@@ -154,7 +154,8 @@ def test_boundary_layer_driver_matches_oracle_step():
     assert np.array_equal(a["velocity_old_NSCBC"][:, 1:, 0], a["velocity"][:, 1:, 0])
 
 
-def test_boundary_layer_step_port_matches_reference():
+@pytest.mark.parametrize("scheme", ["TENOLAD", "Hybrid"])
+def test_boundary_layer_step_port_matches_reference(scheme):
     ref = oracle.ref_lib(2)
     if ref is None:
         pytest.skip("reference CPU build not present on this machine")
@@ -163,10 +164,13 @@ def test_boundary_layer_step_port_matches_reference():
     b, hb, _ = _bl(ref)
     for name in a.arrays:
         assert np.array_equal(a[name], b[name]), name
-    run = wall.BoundaryRun(port, a, ha, a.meta["bc"])
+    run = wall.BoundaryRun(port, a, ha, a.meta["bc"], scheme=scheme)
     dt = run.spectral_dt(0.8)
     run.step(dt)
-    _oracle_step(ref, b, hb, dt, regent=port, regent_mix=ha)
+    bc = b.meta["bc"]
+    oracle.boundary_layer_step(ref, b, hb, dt, bc["xNeg"][1]["P"], bc["xPos"][1]["P"],
+                               (bc["xPos"][1]["LengthScale"], bc["yPos"][1]["LengthScale"]), scheme=scheme,
+                               regent=port, regent_mix=ha)
     for name in a.arrays:
         assert np.array_equal(a[name], b[name]), name
 
@@ -175,7 +179,7 @@ def test_boundary_run_rejects_unsupported():
     port = oracle.port_lib()
     fl, h, _ = _bl(port, num=(6, 5, 3))
     with pytest.raises(abi.HtrError):
-        wall.BoundaryRun(port, fl, h, fl.meta["bc"], scheme="Hybrid")
+        wall.BoundaryRun(port, fl, h, fl.meta["bc"], scheme="WENO")
     bc = dict(fl.meta["bc"])
     bc["yPos"] = ("IncomingShock", {})
     with pytest.raises(abi.HtrError):
@@ -256,8 +260,6 @@ def test_gpu_fused_boundary_cfl_and_errors():
     dt = run.step(cfl=0.8)
     torch.cuda.synchronize()
     assert dt == pytest.approx(dt_ref, rel=1e-12)
-    with pytest.raises(abi.HtrError):
-        wall.FusedBoundaryRun(dev, gh, host.meta["bc"], scheme="Hybrid").step(dt)
     bad = wall.FusedBoundaryRun(dev, gh, host.meta["bc"])
     bad.params.plane[0] = abi.rect((1, 0, 0), (1, 11, 3))  # not the ghost layer
     with pytest.raises(abi.HtrError):
@@ -361,3 +363,55 @@ def test_gpu_channel_step(fused):
     err = util.rel_err(out["Conserved"], host["Conserved"])
     assert err.max() <= util.RHS_REL_TOL, err
     assert np.all(out["velocity"][:, 0] == 0.0) and np.all(out["velocity"][:, -1] == 0.0)
+
+
+def test_zones_sensor_faces_match_hand_derived():
+    for shape in ((8, 6, 3), (21, 14, 5)):
+        z = zones.partition(shape, (1, 1, 0), BL_BC)
+        h = oracle.boundary_layer_zones(*shape)
+        for d in range(3):
+            assert _points(z.faces[d]) == _points([h["faces"][d]]), d
+
+
+def test_hybrid_boundary_layer_driver_matches_oracle():
+    port = oracle.port_lib()
+    a, ha, _ = _bl(port)
+    b, hb, _ = _bl(port)
+    run = wall.BoundaryRun(port, a, ha, a.meta["bc"], scheme="Hybrid")
+    dt = run.spectral_dt(0.8)
+    bc = a.meta["bc"]
+    for _ in range(2):
+        run.step(dt)
+        oracle.boundary_layer_step(port, b, hb, dt, bc["xNeg"][1]["P"], bc["xPos"][1]["P"],
+                                   (bc["xPos"][1]["LengthScale"], bc["yPos"][1]["LengthScale"]), scheme="Hybrid")
+    for name in a.arrays:
+        assert np.array_equal(a[name], b[name]), name
+    # sensors outside the faces zones keep their initial value
+    assert np.all(a["shockSensorX"][:, :, -1]) and np.all(a["shockSensorY"][:, -1, :])
+    assert not np.all(a["shockSensorX"])  # the noisy Mach-6 layer trips the sensor somewhere
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("fused", [False, True])
+def test_gpu_hybrid_boundary_layer_step(fused):
+    import torch
+    port = oracle.port_lib()
+    host, hp, m = _bl(port, num=(24, 16, 6))
+    dev = host.to_device("cuda")
+    gh = runtime.load_mixture(host.meta["eos"], m)
+    bc = host.meta["bc"]
+    dt = wall.BoundaryRun(port, host, hp, bc).spectral_dt(0.8)
+    oracle.boundary_layer_step(port, host, hp, dt, bc["xNeg"][1]["P"], bc["xPos"][1]["P"],
+                               (bc["xPos"][1]["LengthScale"], bc["yPos"][1]["LengthScale"]), scheme="Hybrid")
+    if fused:
+        wall.FusedBoundaryRun(dev, gh, bc, scheme="Hybrid").step(dt)
+    else:
+        mach = torch.zeros(1, dtype=torch.float64, device="cuda")
+        wall.BoundaryRun(runtime.lib(), dev, gh, bc, scheme="Hybrid", stream=runtime.stream_handle(),
+                         max_mach_buffer=mach).step(dt)
+    torch.cuda.synchronize()
+    out = dev.to_host()
+    for d in "XYZ":
+        assert np.array_equal(out[f"shockSensor{d}"], host[f"shockSensor{d}"]), d
+    err = util.rel_err(out["Conserved"], host["Conserved"])
+    assert err.max() <= util.RHS_REL_TOL, err
