@@ -457,6 +457,10 @@ def run_wall(args, device, runtime, lib):
 
     ms_t, fin_t = timed(tasks.step)
     ms_f, fin_f = timed(lambda d: fused.step(d))
+    # the same grid with the hybrid scheme (HTR's own boundary-layer cases),
+    # fused boundary step, for comparison
+    hyb = wall.FusedBoundaryRun(dev, gh, bc, scheme="Hybrid", workspace=fused.ws)
+    ms_h, fin_h = timed(lambda d: hyb.step(d))
     del start
     # task path kernels per stage: time derivatives, chemistry, 3 Euler, 3
     # diffusion, 2 x (max Mach), 2 outflow, 1 inflow, RK update, primitives,
@@ -474,6 +478,9 @@ def run_wall(args, device, runtime, lib):
                       "gpu_launches": args.wall_steps * (3 * per_stage_t + 2)},
             "fused": {"value": 3.0 * cells * args.wall_steps / (ms_f * 1e-3), "ms_per_step": ms_f / args.wall_steps,
                       "gpu_launches": args.wall_steps * (3 * per_stage_f + 2)},
+            "hybrid_fused": {"value": 3.0 * cells * args.wall_steps / (ms_h * 1e-3),
+                             "ms_per_step": ms_h / args.wall_steps, "finite": fin_h,
+                             "note": "same grid and state, hybrid TENO/KG scheme instead of TENO-LAD"},
             "config": {"workload": "Mach-6 boundary layer, 5-species air (AirMix), tanh-stretched wall-normal "
                                    "grid, NSCBC inflow/outflow x, isothermal wall + outflow y, periodic z, "
                                    "TENO-LAD + diffusion + explicit chemistry, SSP-RK3",
