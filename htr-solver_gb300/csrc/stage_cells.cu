@@ -351,8 +351,8 @@ HTR_D void refresh_cell(const UpdateArgs &A, const Mix &mix, const long long *p,
 // UpdatePropertiesFromPrimitive, src/prometeo_variables.hpp:62-89), then its
 // conserved variables (UpdateConservedFromPrimitive, :91-130).
 template <class Mix>
-HTR_D void boundary_properties(const UpdateArgs &A, const Mix &mix, const long long *p, double Pp, double Tp,
-                               const double *x, const double *vel) {
+__device__ __noinline__ void boundary_properties(const UpdateArgs &A, const Mix &mix, const long long *p, double Pp,
+                                                 double Tp, const double *x, const double *vel) {
   constexpr int NS = Mix::NS;
   double y[NS], d[NS];
   const double MixW = mix.MolarWeightFromXi(x);
@@ -388,7 +388,8 @@ HTR_D void boundary_properties(const UpdateArgs &A, const Mix &mix, const long l
 // velocity; pressure from the advanced density, or the imposed pressure of a
 // supersonic inflow.
 template <class Mix>
-HTR_D void inflow_refresh(const UpdateArgs &A, const Mix &mix, const long long *p, const double *u_, int side) {
+__device__ __noinline__ void inflow_refresh(const UpdateArgs &A, const Mix &mix, const long long *p, const double *u_,
+                                            int side) {
   constexpr int NS = Mix::NS;
   double x[NS], vel[3];
 #pragma unroll
@@ -413,6 +414,33 @@ HTR_D void inflow_refresh(const UpdateArgs &A, const Mix &mix, const long long *
   *A.T.at(p) = T;
   *A.P.at(p) = P;
   boundary_properties(A, mix, p, P, T, x, vel);
+}
+
+// NSCBC outflow point after the first primitive recovery: the recovery again
+// for each further outflow plane holding the point, then its properties and
+// conserved variables (out of line: the boundary paths stay out of the
+// per-cell kernel's hot instruction stream).
+template <class Mix>
+__device__ __noinline__ void outflow_refresh(const UpdateArgs &A, const Mix &mix, const long long *p, const double *u_,
+                                             long long i, int n_out) {
+  constexpr int NS = Mix::NS;
+  const long long n = A.dn.count();
+  for (int r = 1; r < n_out; r++) {
+    double Td = 0.0, Ti = 0.0, lT = 0.0;
+    if constexpr (NS > 1) {
+      Td = *A.T.at(p) * mix.TRef;
+      Ti = A.tcache[2 * n + i];
+      lT = A.tcache[n + i];
+    }
+    refresh_cell(A, mix, p, u_, i, Td, Ti, lT);
+  }
+  double x[NS], vel[3];
+  const double *xp = A.X.at(p), *vp = A.u.at(p);
+#pragma unroll
+  for (int k = 0; k < NS; k++) x[k] = xp[k];
+#pragma unroll
+  for (int k = 0; k < 3; k++) vel[k] = vp[k];
+  boundary_properties(A, mix, p, *A.P.at(p), *A.T.at(p), x, vel);
 }
 
 // BC = false: periodic grids and Dirichlet ghosts (ghost nodes keep their
@@ -547,22 +575,7 @@ __global__ void __launch_bounds__(128) stage_update(const UpdateArgs A, const __
         // outflow plane holding the point (an edge shared by two outflows
         // is recovered twice, the second Newton starting from the first's
         // temperature), then its properties and conserved variables
-        for (int r = 1; r < n_out; r++) {
-          double Td = 0.0, Ti = 0.0, lT = 0.0;
-          if constexpr (NS > 1) {
-            Td = *A.T.at(p) * mix.TRef;
-            Ti = A.tcache[2 * n + i];
-            lT = A.tcache[n + i];
-          }
-          refresh_cell(A, mix, p, u_, i, Td, Ti, lT);
-        }
-        double x[NS], vel[3];
-        const double *xp = A.X.at(p), *vp = A.u.at(p);
-#pragma unroll
-        for (int k = 0; k < NS; k++) x[k] = xp[k];
-#pragma unroll
-        for (int k = 0; k < 3; k++) vel[k] = vp[k];
-        boundary_properties(A, mix, p, *A.P.at(p), *A.T.at(p), x, vel);
+        outflow_refresh(A, mix, p, u_, i, n_out);
       }
     }
   }
