@@ -259,7 +259,9 @@ HTR_D int fast_mask(const FastX &f, unsigned used, double cut) {
 // One TENO reconstruction at face c+1/2 from y = (c-2 .. c+3); MINUS gives
 // the right-biased value (metric.inl:431-1038).  Returns the 4 selection
 // flags in *mask (bit k = stencil k kept).
-template <int KIND, bool MINUS>
+// FMA: contract the reconstruction from the selected stencils (it feeds no
+// selection) into fused multiply-adds; false keeps the reference's rounding.
+template <int KIND, bool MINUS, bool FMA = false>
 HTR_D double teno(double ym2, double ym1, double y, double yp1, double yp2, double yp3, int t,
                   unsigned *mask) {
   // optimal weights of this side (tables indexed directly: constant space)
@@ -358,7 +360,21 @@ HTR_D double teno(double ym2, double ym1, double y, double yp1, double yp2, doub
   }
   const double base = MINUS ? yp1 : y;
   double v[4];
-  if (t == Std) {
+  if (FMA && t == Std) {
+    if (!MINUS) {
+      v[0] = __fma_rn(ym1, -1.0 / 6.0, __fma_rn(y, 5.0 / 6.0, __fma_rn(yp1, 2.0 / 6.0, -base)));
+      v[1] = __fma_rn(y, 2.0 / 6.0, __fma_rn(yp1, 5.0 / 6.0, __fma_rn(yp2, -1.0 / 6.0, -base)));
+      v[2] = __fma_rn(ym2, 2.0 / 6.0, __fma_rn(ym1, -7.0 / 6.0, __fma_rn(y, 11.0 / 6.0, -base)));
+      v[3] = __fma_rn(y, 3.0 / 12.0,
+                      __fma_rn(yp1, 13.0 / 12.0, __fma_rn(yp2, -5.0 / 12.0, __fma_rn(yp3, 1.0 / 12.0, -base))));
+    } else {
+      v[0] = __fma_rn(y, 2.0 / 6.0, __fma_rn(yp1, 5.0 / 6.0, __fma_rn(yp2, -1.0 / 6.0, -base)));
+      v[1] = __fma_rn(ym1, -1.0 / 6.0, __fma_rn(y, 5.0 / 6.0, __fma_rn(yp1, 2.0 / 6.0, -base)));
+      v[2] = __fma_rn(yp1, 11.0 / 6.0, __fma_rn(yp2, -7.0 / 6.0, __fma_rn(yp3, 2.0 / 6.0, -base)));
+      v[3] = __fma_rn(ym2, 1.0 / 12.0,
+                      __fma_rn(ym1, -5.0 / 12.0, __fma_rn(y, 13.0 / 12.0, __fma_rn(yp1, 3.0 / 12.0, -base))));
+    }
+  } else if (t == Std) {
     // zero entries of the standard stencils skipped: adding an exact zero
     // does not change a rounded sum.
     if (!MINUS) {
@@ -401,6 +417,7 @@ HTR_D double teno(double ym2, double ym1, double y, double yp1, double yp2, doub
     w3 = c3 * ia;
     w4 = c4 * ia;
   }
+  if (FMA) return __fma_rn(w4, v[3], __fma_rn(w3, v[2], __fma_rn(w2, v[1], __fma_rn(w1, v[0], base))));
   return base + w1 * v[0] + w2 * v[1] + w3 * v[2] + w4 * v[3];
 }
 
