@@ -55,7 +55,7 @@ struct StageWorkspace {
   unsigned *count;  // queue lengths of the three directions
   double *prep;     // per-cell prepass values, [kPrepVals][ncell]
   double *tcache;   // per cell: T it was computed for, log(T TRef), 1/(T TRef); [3][ncell]
-  double *scalars;  // 3 doubles in the queue counters' 256-byte block (maximum Mach number per direction)
+  double *scalars;  // 3 doubles in the counters' 256-byte block (maximum Mach number per direction)
 };
 
 // per-cell prepass values: velocity-gradient tensor (9), mixture molar

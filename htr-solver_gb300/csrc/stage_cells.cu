@@ -48,7 +48,7 @@ bool stage_workspace_carve(void *base, size_t bytes, const htr_rect3 &r, int neq
   w.queue = reinterpret_cast<TenoEntry *>(p);
   p += align256(sizeof(TenoEntry) * (g.nf[0] + g.nf[1] + g.nf[2]));
   w.count = reinterpret_cast<unsigned *>(p);
-  w.scalars = reinterpret_cast<double *>(p + 2 * sizeof(double));
+  w.scalars = reinterpret_cast<double *>(p + 48);
   p += align256(sizeof(unsigned));
   w.prep = reinterpret_cast<double *>(p);
   {
