@@ -415,3 +415,90 @@ def test_gpu_hybrid_boundary_layer_step(fused):
         assert np.array_equal(out[f"shockSensor{d}"], host[f"shockSensor{d}"]), d
     err = util.rel_err(out["Conserved"], host["Conserved"])
     assert err.max() <= util.RHS_REL_TOL, err
+
+
+def _pointwise_zones(shape, bnum, types):
+    """The partitioner's rules applied point by point (an independent
+    restatement used to check zones.partition's rectangle bookkeeping)."""
+    nscbc_t = {"NSCBC_Inflow", "NSCBC_Outflow", "NSCBC_FarField", "RecycleRescaling", "IncomingShock"}
+    wall_t = {"AdiabaticWall", "IsothermalWall", "SuctionAndBlowingWall"}
+    nscbc = [t in nscbc_t for t in types]
+    nscbc[4], nscbc[5] = types[2] in nscbc_t, types[3] in nscbc_t  # the z flags read the y sides
+
+    def rank(t):
+        if t in wall_t:
+            return 0
+        if t == "Dirichlet":
+            return 1
+        if t in ("NSCBC_Inflow", "RecycleRescaling"):
+            return 2
+        if t in ("NSCBC_Outflow", "IncomingShock", "NSCBC_FarField"):
+            return 3
+        return 9
+
+    planes = [set() for _ in range(6)]
+    divg = [set() for _ in range(3)]
+    solved, faces = set(), [set() for _ in range(3)]
+    for k in range(shape[2]):
+        for j in range(shape[1]):
+            for i in range(shape[0]):
+                p = (i, j, k)
+                sides = []
+                for d in range(3):
+                    if p[d] < bnum[d]:
+                        sides.append(2 * d)
+                    elif p[d] >= shape[d] - bnum[d]:
+                        sides.append(2 * d + 1)
+                if not sides:
+                    solved.add(p)
+                    for d in range(3):
+                        divg[d].add(p)
+                        faces[d].add(p)
+                    continue
+                # planes: best rank wins (lowest axis first); outflow-like sides all win
+                best = min(rank(types[s]) for s in sides)
+                if best == 3:
+                    for s in sides:
+                        planes[s].add(p)
+                elif best < 3:
+                    planes[next(s for s in sides if rank(types[s]) == best)].add(p)
+                axes = [s // 2 for s in sides]
+                if all(nscbc[s] for s in sides) and len(sides) <= 2:
+                    solved.add(p)
+                    for d in range(3):
+                        if d not in axes:
+                            divg[d].add(p)
+                # sensor zones: the Neg ghost face of d; NSCBC sides towards d's Neg side
+                for d in range(3):
+                    other = [s for s in sides if s // 2 != d]
+                    own = [s for s in sides if s // 2 == d]
+                    if own and own != [2 * d]:
+                        continue
+                    if not other and own == [2 * d]:
+                        faces[d].add(p)
+                    elif other and all(nscbc[s] for s in other) and len(other) <= 2:
+                        faces[d].add(p)
+    return planes, divg, solved, faces
+
+
+@pytest.mark.parametrize("seed", range(40))
+def test_zones_match_pointwise_rules(seed):
+    rng = np.random.default_rng(seed)
+    kinds = ["NSCBC_Inflow", "NSCBC_Outflow", "IsothermalWall", "AdiabaticWall", "Dirichlet"]
+    axes = []
+    for d in range(3):
+        if rng.random() < 0.3:
+            axes.append(("Periodic", "Periodic"))
+        else:
+            axes.append((kinds[rng.integers(len(kinds))], kinds[rng.integers(len(kinds))]))
+    bnum = tuple(0 if a[0] == "Periodic" else 1 for a in axes)
+    shape = tuple(int(n) + 2 * b for n, b in zip(rng.integers(3, 6, size=3), bnum))
+    types = [axes[0][0], axes[0][1], axes[1][0], axes[1][1], axes[2][0], axes[2][1]]
+    z = zones.partition(shape, bnum, axes)
+    planes, divg, solved, faces = _pointwise_zones(shape, bnum, types)
+    for s in range(6):
+        assert _points(z.planes[s]) == planes[s], (axes, s)
+    for d in range(3):
+        assert _points(z.divg[d]) == divg[d], (axes, d)
+        assert _points(z.faces[d]) == faces[d], (axes, "faces", d)
+    assert _points(z.solved) == solved, axes
