@@ -849,6 +849,7 @@ int htr_rk3_step_bc_ws(const htr_fluid_view *v, htr_rect3 inner, htr_rect3 fb, c
              : t == HTR_BC_NSCBC_OUTFLOW ? htr::kBcOutflow
              : (t == HTR_BC_ISOTHERMAL_WALL || t == HTR_BC_ADIABATIC_WALL) ? htr::kBcWall : htr::kBcPeriodic;
     sp.Pbc[k] = bc->P[k];
+    sp.plane[k] = bc->plane[k];
   }
   if ((st = cuda_status(cudaMemsetAsync(w.tcache, 0, sizeof(double) * 3 * ncells_of(fb), cs), "cache reset"))) return st;
   const int neq = neq_of(m), ns = nspec_of(m);

@@ -81,6 +81,7 @@ struct StageParams {
   int boundary = 0;
   int bc[6] = {0, 0, 0, 0, 0, 0};
   double Pbc[6] = {0.0, 0.0, 0.0, 0.0, 0.0, 0.0};
+  htr_rect3 plane[6] = {};  // the sides' boundary points (NSCBC sides are refreshed plane by plane)
 };
 
 // Side kinds of the boundary step.  Walls have staggered ghost points (never

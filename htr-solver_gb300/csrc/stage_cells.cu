@@ -561,23 +561,75 @@ __global__ void __launch_bounds__(128) stage_update(const UpdateArgs A, const __
       cons[k] = u_[k];
     }
     if constexpr (BC) {
-      if (inflow_side >= 0) {
-        inflow_refresh(A, mix, p, u_, inflow_side);
-        continue;
-      }
+      // an NSCBC point keeps its stage state until boundary_refresh (after
+      // this kernel) applies its side's rule, so no warp here diverges
+      if (bnd) continue;
     }
     // primitive recovery (variables.hpp:163-193) and property refresh
     // (variables.hpp:62-89) of the new state
     refresh_cell(A, mix, p, u_, i, Td0, Tinv0, logT0);
-    if constexpr (BC) {
-      if (bnd) {
-        // outflow point (SetNSCBC_OutflowBCTask): the recovery above, once per
-        // outflow plane holding the point (an edge shared by two outflows
-        // is recovered twice, the second Newton starting from the first's
-        // temperature), then its properties and conserved variables
-        outflow_refresh(A, mix, p, u_, i, n_out);
+  }
+}
+
+// The NSCBC points of one boundary plane after the update, each refreshed
+// once by the first NSCBC plane (in side order) that holds it: the inflow
+// rule (inflow wins an edge with an outflow), else the outflow's primitive
+// recovery, repeated once per outflow plane holding the point (an edge
+// shared by two outflows is recovered twice, the second Newton starting
+// from the first's temperature), then properties and conserved variables.
+template <class Mix>
+__global__ void boundary_refresh(const UpdateArgs A, const __grid_constant__ Mix mix, const Box plane, int side) {
+  constexpr int NS = Mix::NS, NE = NS + 4;
+  const long long np = plane.size(0) * plane.size(1) * plane.size(2);
+  const long long n = A.dn.count();
+  for (long long q = blockIdx.x * (long long)blockDim.x + threadIdx.x; q < np; q += (long long)gridDim.x * blockDim.x) {
+    long long p[3];
+    p[0] = plane.lo[0] + q % plane.size(0);
+    p[1] = plane.lo[1] + (q / plane.size(0)) % plane.size(1);
+    p[2] = plane.lo[2] + q / (plane.size(0) * plane.size(1));
+    int first_out = -1, inflow_side = -1, n_out = 0;
+    bool wall = false;
+#pragma unroll
+    for (int D = 0; D < 3; D++) {
+      if (!(A.active & (1u << D))) continue;
+      const int t = ld(A.nt[D].at(p));
+      if (t == L_S || t == R_S) wall = true;
+      if (t == L_C || t == R_C) {
+        const int s = 2 * D + (t == R_C ? 1 : 0);
+        if (A.bc[s] == kBcInflow && inflow_side < 0) inflow_side = s;
+        if (A.bc[s] == kBcOutflow) {
+          if (first_out < 0) first_out = s;
+          n_out++;
+        }
       }
     }
+    // the planes holding the point: its first inflow side alone (an inflow
+    // wins an edge), else every outflow side; the first of them refreshes it
+    const int owner = inflow_side >= 0 ? inflow_side : first_out;
+    if (wall || owner != side) continue;
+    double u_[NE];
+    const double *cp = A.C.at(p);
+#pragma unroll
+    for (int k = 0; k < NE; k++) u_[k] = cp[k];
+    if (inflow_side >= 0) {
+      inflow_refresh(A, mix, p, u_, inflow_side);
+      continue;
+    }
+    const long long i = A.dn.idx(p);
+    double Td0 = 0.0, Tinv0 = 0.0, logT0 = 0.0;
+    if constexpr (NS > 1) {
+      const double Tn0 = *A.T.at(p);
+      Td0 = Tn0 * mix.TRef;
+      if (__double_as_longlong(A.tcache[i]) == __double_as_longlong(Tn0)) {
+        logT0 = A.tcache[n + i];
+        Tinv0 = A.tcache[2 * n + i];
+      } else {
+        Tinv0 = 1.0 / Td0;
+        logT0 = log(Td0);
+      }
+    }
+    refresh_cell(A, mix, p, u_, i, Td0, Tinv0, logT0);
+    outflow_refresh(A, mix, p, u_, i, n_out);
   }
 }
 
@@ -701,10 +753,17 @@ cudaError_t launch_stage(const htr_fluid_view &v, const htr_rect3 &my, const htr
     U.Pbc[k] = sp.Pbc[k];
   }
   const int ub = stage_tuning().update_block;
-  if (sp.boundary)
+  if (sp.boundary) {
     stage_update<Mix, true><<<grid_for(n, ub), ub, 0, s>>>(U, mix);
-  else
+    for (int k = 0; k < 6; k++) {
+      if (sp.bc[k] != kBcInflow && sp.bc[k] != kBcOutflow) continue;
+      if ((e = cudaGetLastError()) != cudaSuccess) return e;
+      const Box pl = box(sp.plane[k]);
+      boundary_refresh<Mix><<<grid_for(pl.size(0) * pl.size(1) * pl.size(2), 128), 128, 0, s>>>(U, mix, pl, k);
+    }
+  } else {
     stage_update<Mix, false><<<grid_for(n, ub), ub, 0, s>>>(U, mix);
+  }
   if ((e = cudaGetLastError()) != cudaSuccess) return e;
   return mark(1 + kUpdate);
 }

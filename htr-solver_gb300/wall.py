@@ -342,6 +342,11 @@ class FusedBoundaryRun:
         axes = tuple((types[2 * d], types[2 * d + 1]) for d in range(3))
         bnum = tuple(0 if a[0] == PERIODIC else 1 for a in axes)
         z = zones.partition(fl.shape, bnum, axes)
+        nscbc = lambda t: t in ("NSCBC_Inflow", "NSCBC_Outflow")
+        if types[4] != PERIODIC and (nscbc(types[4]) != nscbc(types[2]) or nscbc(types[5]) != nscbc(types[3])):
+            # the reference's zones take the z sides' characteristic flags from
+            # the y sides; the fused step reads the z sides' node types
+            raise abi.HtrError("the fused boundary step needs z periodic, or z sides of the y sides' kinds")
         self.params = runtime.htr_bc_params()
         for k in range(6):
             self.params.type[k] = runtime.BC_TYPES[types[k]]
