@@ -23,6 +23,8 @@ STATUS_NAMES = {
     4: "HTR_ERR_ITERATION_CAP",
     5: "HTR_ERR_UNSUPPORTED",
     6: "HTR_ERR_NO_DEVICE",
+    7: "HTR_ERR_IO",
+    8: "HTR_ERR_FORMAT",
 }
 
 
@@ -33,6 +35,8 @@ HTR_ERR_CUDA = 3
 HTR_ERR_ITERATION_CAP = 4
 HTR_ERR_UNSUPPORTED = 5
 HTR_ERR_NO_DEVICE = 6
+HTR_ERR_IO = 7
+HTR_ERR_FORMAT = 8
 
 
 class HtrError(RuntimeError):
@@ -189,6 +193,28 @@ PROTOTYPES["htr_UpdateNSCBCGhostCellTimeDerivatives"] = [_V, _R, C.c_double, _S]
 PROTOTYPES["htr_InitializeMetric"] = [_V, htr_field, _R, _R, _P(C.c_double), _S]
 for _d in "XYZ":
     PROTOTYPES[f"htr_CorrectGhostMetric{_d}"] = [_V, htr_field, _R, _S]
+
+
+# include/htr_restart.h
+HTR_RESTART_HOST_VIEW = 1
+HTR_RESTART_PROFILES = 2
+
+
+class htr_restart_info(C.Structure):
+    _fields_ = [("timeStep", C.c_int64), ("simTime", C.c_double), ("channelForcing", C.c_double)]
+
+
+_CP = C.c_char_p
+PROTOTYPES["htr_restart_tile_filename"] = [_CP, htr_rect3, C.c_char_p, C.c_size_t]
+PROTOTYPES["htr_restart_write_tile"] = [_CP, _V, htr_rect3, C.c_int, C.c_int, _S]
+PROTOTYPES["htr_restart_read_tile"] = [_CP, _V, htr_rect3, C.c_int, C.c_int, _S]
+PROTOTYPES["htr_restart_write_master"] = [_CP, _P(htr_restart_info), htr_rect3, _P(C.c_int64), _P(htr_rect3),
+                                          C.c_int, _P(C.c_char_p), _P(C.c_char_p)]
+PROTOTYPES["htr_restart_read_master"] = [_CP, _P(htr_restart_info), _P(htr_rect3), _P(C.c_int64),
+                                         _P(htr_rect3), C.c_int64]
+PROTOTYPES["htr_h5_dataset_shape"] = [_CP, _CP, _P(C.c_int), _P(C.c_int64), _P(C.c_int64)]
+PROTOTYPES["htr_h5_read_doubles"] = [_CP, _CP, _P(C.c_double), C.c_int64]
+PROTOTYPES["htr_h5_string_attribute"] = [_CP, _CP, _CP, C.c_int64, C.c_char_p, C.c_size_t]
 
 
 def bind(lib, extra=None):

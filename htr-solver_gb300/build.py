@@ -28,7 +28,8 @@ def nvcc():
 
 
 def _sources():
-    return sorted(f for f in os.listdir(CSRC) if f.endswith(".cu"))
+    # CUDA translation units and host-only C++ (compiled by nvcc's host compiler)
+    return sorted(f for f in os.listdir(CSRC) if f.endswith((".cu", ".cpp")))
 
 
 def _deps():
@@ -58,7 +59,7 @@ def build(force=False, verbose=False):
         base += ["-Xptxas", "-v"]
 
     def compile_one(src):
-        obj = os.path.join(OUT_DIR, src.replace(".cu", ".o"))
+        obj = os.path.join(OUT_DIR, os.path.splitext(src)[0] + ".o")
         cmd = base + (["-fmad=false"] if src in EXACT_TUS else []) + ["-c", os.path.join(CSRC, src), "-o", obj]
         r = subprocess.run(cmd, capture_output=True, text=True)
         if r.returncode != 0:

@@ -270,6 +270,14 @@ int fused_step(const htr_fluid_view *v, htr_rect3 inner, htr_rect3 fb, const htr
 
 }  // namespace
 
+namespace htr {
+// the message htr_last_error() returns, for entry points in other files
+int set_last_error(int code, const std::string &msg) {
+  g_err = msg;
+  return code;
+}
+}  // namespace htr
+
 extern "C" {
 
 

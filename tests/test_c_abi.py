@@ -42,6 +42,88 @@ int main(void) {
 }
 """
 
+# A C program that dumps the restart fields of a host-resident 6x5x4 grid as
+# two tiles plus the master file, reads them back into zeroed arrays and
+# compares.
+RESTART_PROGRAM = r"""
+#include <stdio.h>
+#include <stdlib.h>
+#include <string.h>
+#include "htr_restart.h"
+
+#define NX 6
+#define NY 5
+#define NZ 4
+#define NS 5
+
+static void bind(htr_field *f, double *p, int comps) {
+  f->base = p;
+  f->stride[0] = 8 * comps;
+  f->stride[1] = 8 * comps * NX;
+  f->stride[2] = 8 * comps * NX * NY;
+}
+
+int main(int argc, char **argv) {
+  static const int comps[7] = {1, 1, 1, NS, 3, 3, 1};
+  double *a[7], *b[7];
+  htr_fluid_view va, vb;
+  htr_field *fa[7] = {&va.rho, &va.pressure, &va.temperature, &va.MolarFracs, &va.velocity,
+                      &va.dudtBoundary, &va.dTdtBoundary};
+  htr_field *fb[7] = {&vb.rho, &vb.pressure, &vb.temperature, &vb.MolarFracs, &vb.velocity,
+                      &vb.dudtBoundary, &vb.dTdtBoundary};
+  htr_rect3 whole = {{0, 0, 0}, {NX - 1, NY - 1, NZ - 1}};
+  htr_rect3 parts[2] = {{{0, 0, 0}, {2, NY - 1, NZ - 1}}, {{3, 0, 0}, {NX - 1, NY - 1, NZ - 1}}};
+  const int64_t tiles[3] = {2, 1, 1};
+  htr_restart_info info = {42, 0.5, 0.0}, back;
+  htr_rect3 bounds, got[2];
+  int64_t nt[3];
+  int i, k, st;
+  if (argc < 2) return 9;
+  memset(&va, 0, sizeof va);
+  memset(&vb, 0, sizeof vb);
+  for (k = 0; k < 7; k++) {
+    size_t n = (size_t)NX * NY * NZ * comps[k];
+    a[k] = malloc(n * sizeof(double));
+    b[k] = calloc(n, sizeof(double));
+    for (i = 0; i < (int)n; i++) a[k][i] = k * 1000.0 + i * 0.25;
+    bind(fa[k], a[k], comps[k]);
+    bind(fb[k], b[k], comps[k]);
+  }
+  for (k = 0; k < 2; k++)
+    if ((st = htr_restart_write_tile(argv[1], &va, parts[k], NS, HTR_RESTART_HOST_VIEW, NULL)) != HTR_OK) {
+      printf("write %d %s\n", st, htr_last_error());
+      return 1;
+    }
+  if (htr_restart_write_master(argv[1], &info, whole, tiles, parts, NS, NULL, NULL) != HTR_OK) return 2;
+  if (htr_restart_read_master(argv[1], &back, &bounds, nt, got, 2) != HTR_OK) return 3;
+  for (k = 0; k < 2; k++)
+    if (htr_restart_read_tile(argv[1], &vb, got[k], NS, HTR_RESTART_HOST_VIEW, NULL) != HTR_OK) return 4;
+  for (k = 0; k < 7; k++)
+    if (memcmp(a[k], b[k], (size_t)NX * NY * NZ * comps[k] * sizeof(double)) != 0) return 5;
+  printf("timeStep %ld tiles %ld\n", (long)back.timeStep, (long)(nt[0] * nt[1] * nt[2]));
+  return 0;
+}
+"""
+
+
+def test_c_program_writes_and_reads_a_restart(tmp_path):
+    if shutil.which("gcc") is None:
+        pytest.skip("no host compiler")
+    if not os.path.exists(runtime.LIB_PATH):
+        pytest.skip("CUDA library not built")
+    src = tmp_path / "r.c"
+    src.write_text(RESTART_PROGRAM)
+    exe = tmp_path / "r"
+    libdir = os.path.dirname(runtime.LIB_PATH)
+    subprocess.run(["gcc", "-std=c99", "-I", os.path.join(ROOT, "include"), str(src), "-o", str(exe),
+                    "-L", libdir, "-l:" + os.path.basename(runtime.LIB_PATH), "-Wl,-rpath," + libdir], check=True)
+    d = tmp_path / "restart"
+    d.mkdir()
+    r = subprocess.run([str(exe), str(d)], capture_output=True, text=True)
+    assert r.returncode == 0, (r.returncode, r.stdout)
+    assert r.stdout.split() == ["timeStep", "42", "tiles", "2"]
+    assert sorted(os.listdir(d)) == ["0,0,0-2,4,3.hdf", "3,0,0-5,4,3.hdf", "master.hdf"]
+
 
 def test_headers_compile_as_c_and_cxx(tmp_path):
     if shutil.which("gcc") is None or shutil.which("g++") is None:
@@ -50,8 +132,11 @@ def test_headers_compile_as_c_and_cxx(tmp_path):
     src.write_text(PROGRAM)
     inc = os.path.join(ROOT, "include")
     subprocess.run(["gcc", "-std=c99", "-Wall", "-Wextra", "-Werror", "-fsyntax-only", "-I", inc, str(src)], check=True)
+    rst = tmp_path / "r.c"
+    rst.write_text(RESTART_PROGRAM)
+    subprocess.run(["gcc", "-std=c99", "-Wall", "-Wextra", "-Werror", "-fsyntax-only", "-I", inc, str(rst)], check=True)
     cxx = tmp_path / "t.cpp"
-    cxx.write_text('#include "htr_rhs.h"\nint main() { return 0; }\n')
+    cxx.write_text('#include "htr_rhs.h"\n#include "htr_restart.h"\nint main() { return 0; }\n')
     subprocess.run(["g++", "-std=c++17", "-Wall", "-Werror", "-fsyntax-only", "-I", inc, str(cxx)], check=True)
 
 
