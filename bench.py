@@ -491,6 +491,46 @@ def run_wall(args, device, runtime, lib):
             "gpu_launches": args.wall_steps * (3 * (per_stage_f if best == "fused" else per_stage_t) + 2)}
 
 
+def run_restart(dev, device, reps=3):
+    """Restart dump and load of the benchmark state through
+    include/htr_restart.h (2 tiles plus master.hdf in a temporary
+    directory): seconds and GB/s of restart fields, median of `reps`."""
+    import shutil
+    import tempfile
+
+    import torch
+    from htr_gb300 import fluid, restart
+    back = fluid.Fluid(dev.shape, dev.nspec, device=device, fields=list(restart.IO_FIELDS))
+    nbytes = sum(dev.arrays[k].numel() * 8 for k in restart.IO_FIELDS)
+    base = tempfile.mkdtemp(prefix="htr_restart_")
+    dump_s, load_s, equal, fbytes = [], [], True, 0
+    try:
+        for rep in range(reps):
+            d = os.path.join(base, f"fluid_iter{rep:010d}")
+            torch.cuda.synchronize()
+            t0 = time.perf_counter()
+            restart.dump(d, dev, tiles=(1, 1, 2), time_step=rep)
+            t1 = time.perf_counter()
+            for k in restart.IO_FIELDS:
+                back.arrays[k].zero_()
+            torch.cuda.synchronize()
+            t2 = time.perf_counter()
+            restart.load(d, back)
+            torch.cuda.synchronize()
+            t3 = time.perf_counter()
+            equal = equal and all(torch.equal(dev.arrays[k], back.arrays[k]) for k in restart.IO_FIELDS)
+            fbytes = sum(os.path.getsize(os.path.join(d, x)) for x in os.listdir(d))
+            dump_s.append(t1 - t0)
+            load_s.append(t3 - t2)
+            shutil.rmtree(d)
+    finally:
+        shutil.rmtree(base, ignore_errors=True)
+    md, ml = sorted(dump_s)[len(dump_s) // 2], sorted(load_s)[len(load_s) // 2]
+    return {"field_bytes": nbytes, "file_bytes": fbytes, "tiles": [1, 1, 2], "dump_s": md, "load_s": ml,
+            "dump_gbps": nbytes / md / 1e9, "load_gbps": nbytes / ml / 1e9, "bit_identical": equal,
+            "note": "host wall clock, device synchronised on both sides; files in the page cache (no fsync)"}
+
+
 def fp64_peak(lib):
     lib.htr_probe_fp64_tflops.argtypes = [C.c_int, C.POINTER(C.c_double)]
     lib.htr_probe_fp64_tflops.restype = C.c_int
@@ -608,6 +648,12 @@ def run_gpu(args):
                 result["wall"] = run_wall(args, device, runtime, lib)
             except Exception as exc:
                 result["wall"] = {"error": f"{type(exc).__name__}: {exc}"}
+        if args.restart:
+            try:
+                log("restart dump/load")
+                result["restart"] = run_restart(dev, device)
+            except Exception as exc:
+                result["restart"] = {"error": f"{type(exc).__name__}: {exc}"}
         if args.cpu_baseline:
             log("CPU baseline")
             result["cpu_baseline"] = cpu_baseline(args.cpu_seconds)
@@ -726,6 +772,7 @@ def main():
     p.add_argument("--serve", type=int, default=32, help="served requests (0: skip)")
     p.add_argument("--wall", default="512,192,128", help="boundary-layer interior cells nx,ny,nz ('' skips)")
     p.add_argument("--wall-steps", type=int, default=10)
+    p.add_argument("--no-restart", dest="restart", action="store_false", help="skip the restart dump/load timing")
     args = p.parse_args()
     res = run_reference(args) if args.impl == "reference" else run_gpu(args)
     if res is not None:
