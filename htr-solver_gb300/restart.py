@@ -18,17 +18,24 @@ IO_FIELDS = ("rho", "pressure", "temperature", "MolarFracs", "velocity", "dudtBo
 PROFILE_FIELDS = ("MolarFracs_profile", "velocity_profile", "temperature_profile")
 
 
-def split(fluid, tiles):
-    """Tiles of the whole grid (ghost layers included), x fastest: axis `a`
-    of length N in T tiles gets blocks [k*N//T, (k+1)*N//T)."""
+def split(fluid, tiles, halo=(0, 0, 0)):
+    """Tiles of the whole grid, x fastest, as the reference cuts its output
+    partition: the interior (the grid without `halo` ghost layers on each
+    side of an axis) in T equal blocks, [k*M//T, (k+1)*M//T) for M interior
+    points, the ghost layers joined to the first and last tile
+    (scripts/modules/HTRrestart.py:150-161; it asks M % T == 0, where the
+    blocks are M/T wide)."""
     n = fluid.shape
     out = []
     for kz in range(tiles[2]):
         for ky in range(tiles[1]):
             for kx in range(tiles[0]):
                 k = (kx, ky, kz)
-                lo = [k[a] * n[a] // tiles[a] for a in range(3)]
-                hi = [(k[a] + 1) * n[a] // tiles[a] - 1 for a in range(3)]
+                lo, hi = [], []
+                for a in range(3):
+                    m = n[a] - 2 * halo[a]
+                    lo.append(k[a] * m // tiles[a] + halo[a] - (halo[a] if k[a] == 0 else 0))
+                    hi.append((k[a] + 1) * m // tiles[a] - 1 + halo[a] + (halo[a] if k[a] == tiles[a] - 1 else 0))
                 out.append(abi.rect(lo, hi))
     return out
 
@@ -48,9 +55,11 @@ def tile_filename(dirname, rect):
 
 
 def dump(dirname, fluid, tiles=(1, 1, 1), time_step=0, sim_time=0.0, channel_forcing=0.0,
-         species_names=None, versions=None, profiles=False, stream=None):
+         species_names=None, versions=None, profiles=False, stream=None, halo=(0, 0, 0)):
     """Writes the restart fields of `fluid` (host arrays or device tensors)
-    as len(tiles) tile files plus master.hdf under `dirname`."""
+    as one file per tile (`split`; `halo` = the grid's ghost layers per side
+    of each axis gives the reference's tile rectangles and file names) plus
+    master.hdf under `dirname`."""
     if fluid.ncells == 0:
         raise abi.HtrError("empty grid")
     os.makedirs(dirname, exist_ok=True)
@@ -58,7 +67,9 @@ def dump(dirname, fluid, tiles=(1, 1, 1), time_step=0, sim_time=0.0, channel_for
     if profiles:
         flags |= abi.HTR_RESTART_PROFILES
     view = fluid.view()
-    parts = split(fluid, tiles)
+    if any(t < 1 for t in tiles) or any(tiles[a] > fluid.shape[a] - 2 * halo[a] for a in range(3)):
+        raise abi.HtrError(f"cannot cut {fluid.shape} (ghost layers {halo}) into {tiles} tiles")
+    parts = split(fluid, tiles, halo)
     d = os.fsencode(dirname)
     for r in parts:
         abi.check(lib, lib.htr_restart_write_tile(d, C.byref(view), r, fluid.nspec, flags, s), "htr_restart_write_tile")

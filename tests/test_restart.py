@@ -164,10 +164,37 @@ def test_restart_round_trip_host(tmp_path, tiles, profiles):
     assert not g["Conserved"].any()  # not a restart field
 
 
+def test_tiles_follow_the_reference_partition():
+    """With the ghost layers given, the tiles are the reference's: equal
+    interior blocks, ghosts joined to the outer tiles (the rule of
+    scripts/modules/HTRrestart.py:130-161, written out here)."""
+    f = fluid.Fluid((514, 194, 128), 5, fields=["rho"])  # 512 x 192 x 128 interior, ghosts in x and y
+    tiles, halo = (4, 2, 2), (1, 1, 0)
+    got = restart.split(f, tiles, halo)
+    nt = [512 // 4, 192 // 2, 128 // 2]
+    k = 0
+    for z in range(tiles[2]):
+        for y in range(tiles[1]):
+            for x in range(tiles[0]):
+                c = (x, y, z)
+                lo = [c[a] * nt[a] + halo[a] for a in range(3)]
+                hi = [(c[a] + 1) * nt[a] - 1 + halo[a] for a in range(3)]
+                for a in range(3):
+                    if c[a] == 0:
+                        lo[a] -= halo[a]
+                    if c[a] == tiles[a] - 1:
+                        hi[a] += halo[a]
+                assert list(got[k].lo) == lo and list(got[k].hi) == hi, (c, list(got[k].lo), list(got[k].hi))
+                k += 1
+    # without ghost layers: blocks of the whole grid
+    assert [list(r.hi) for r in restart.split(fluid.Fluid((6, 4, 2), 1, fields=["rho"]), (2, 1, 1))] == \
+        [[2, 3, 1], [5, 3, 1]]
+
+
 @needs_lib
 def test_load_reads_the_tiling_of_the_master_file(tmp_path):
     f = random_fluid((8, 6, 5), seed=4)
-    restart.dump(str(tmp_path), f, tiles=(2, 3, 1))
+    restart.dump(str(tmp_path), f, tiles=(2, 3, 1), halo=(1, 0, 1))
     g = fluid.Fluid(f.shape, f.nspec)
     restart.load(str(tmp_path), g)
     for n in restart.IO_FIELDS:
