@@ -361,6 +361,54 @@ bool decode_type(Cur &c, Type &t, int depth = 0) {
   return !c.bad;
 }
 
+// Bob Jenkins' lookup3 `hashlittle` (public domain, 2006), byte-wise form:
+// the checksum HDF5 stores after metadata blocks of its newer format
+// versions (superblock 2/3, version-2 object headers), with initial value 0.
+uint32_t lookup3(const uint8_t *k, size_t length, uint32_t initval) {
+  auto rot = [](uint32_t x, int s) { return (x << s) | (x >> (32 - s)); };
+  auto word = [](const uint8_t *q) {
+    return uint32_t(q[0]) | uint32_t(q[1]) << 8 | uint32_t(q[2]) << 16 | uint32_t(q[3]) << 24;
+  };
+  uint32_t a, b, c;
+  a = b = c = 0xdeadbeefu + static_cast<uint32_t>(length) + initval;
+  while (length > 12) {
+    a += word(k);
+    b += word(k + 4);
+    c += word(k + 8);
+    a -= c; a ^= rot(c, 4);  c += b;
+    b -= a; b ^= rot(a, 6);  a += c;
+    c -= b; c ^= rot(b, 8);  b += a;
+    a -= c; a ^= rot(c, 16); c += b;
+    b -= a; b ^= rot(a, 19); a += c;
+    c -= b; c ^= rot(b, 4);  b += a;
+    length -= 12;
+    k += 12;
+  }
+  switch (length) {  // the last 1..12 bytes
+    case 12: c += uint32_t(k[11]) << 24; [[fallthrough]];
+    case 11: c += uint32_t(k[10]) << 16; [[fallthrough]];
+    case 10: c += uint32_t(k[9]) << 8;   [[fallthrough]];
+    case 9:  c += k[8];                  [[fallthrough]];
+    case 8:  b += uint32_t(k[7]) << 24;  [[fallthrough]];
+    case 7:  b += uint32_t(k[6]) << 16;  [[fallthrough]];
+    case 6:  b += uint32_t(k[5]) << 8;   [[fallthrough]];
+    case 5:  b += k[4];                  [[fallthrough]];
+    case 4:  a += uint32_t(k[3]) << 24;  [[fallthrough]];
+    case 3:  a += uint32_t(k[2]) << 16;  [[fallthrough]];
+    case 2:  a += uint32_t(k[1]) << 8;   [[fallthrough]];
+    case 1:  a += k[0]; break;
+    case 0:  return c;
+  }
+  c ^= b; c -= rot(b, 14);
+  a ^= c; a -= rot(c, 11);
+  b ^= a; b -= rot(a, 25);
+  c ^= b; c -= rot(b, 16);
+  a ^= c; a -= rot(c, 4);
+  b ^= a; b -= rot(a, 14);
+  c ^= b; c -= rot(b, 24);
+  return c;
+}
+
 struct Space {
   std::vector<uint64_t> dims;
   bool null = false;
@@ -714,70 +762,142 @@ struct Parser {
       if (std::memcmp(s, sig, 8) == 0) break;
       at = at ? at * 2 : 512;
     }
-    std::vector<uint8_t> h(24);
-    if (!read_abs(at, h.data(), 24)) return false;
+    std::vector<uint8_t> h(12);
+    if (!read_abs(at, h.data(), 12)) return false;
     const int version = h[8];
-    if (version > 1)
-      return fail(HTR_ERR_UNSUPPORTED, "superblock version " + std::to_string(version) +
-                                           " (only the earliest file format, versions 0 and 1, is read)");
-    so = h[13];
-    sl = h[14];
+    if (version > 3) return fail(HTR_ERR_UNSUPPORTED, "superblock version " + std::to_string(version));
+    if (version < 2) {
+      std::vector<uint8_t> v(24);
+      if (!read_abs(at, v.data(), 24)) return false;
+      so = v[13];
+      sl = v[14];
+    } else {
+      so = h[9];
+      sl = h[10];
+    }
     if ((so != 2 && so != 4 && so != 8) || (sl != 2 && sl != 4 && sl != 8))
       return fail(HTR_ERR_FORMAT, "bad sizes of offsets/lengths");
-    const size_t rest = (version == 1 ? 4 : 0) + 4 * so + (2 * so + 8 + 16);
-    std::vector<uint8_t> b(rest);
-    if (!read_abs(at + 24, b.data(), rest)) return false;
-    Cur c(b);
-    if (version == 1) c.skip(4);
-    r.base_ = c.addr(so);
-    c.addr(so);  // free-space info
-    const uint64_t eof = c.addr(so);
-    c.addr(so);  // driver info
-    c.addr(so);  // root link name offset
-    const uint64_t root = c.addr(so);
-    if (c.bad || root == kUndef) return fail(HTR_ERR_FORMAT, "bad root group entry");
+    uint64_t eof = kUndef, root = kUndef;
+    if (version >= 2) {
+      // versions 2 and 3: addresses, root object header, lookup3 checksum
+      const size_t n = 12 + 4 * size_t(so) + 4;
+      std::vector<uint8_t> b(n);
+      if (!read_abs(at, b.data(), n)) return false;
+      Cur c(b.data() + 12, n - 12);
+      r.base_ = c.addr(so);
+      c.addr(so);  // superblock extension (file-space settings; not needed to read)
+      eof = c.addr(so);
+      root = c.addr(so);
+      const uint32_t sum = c.u32();
+      if (c.bad || sum != lookup3(b.data(), n - 4, 0)) return fail(HTR_ERR_FORMAT, "superblock checksum mismatch");
+    } else {
+      const size_t rest = (version == 1 ? 4 : 0) + 4 * so + (2 * so + 8 + 16);
+      std::vector<uint8_t> b(rest);
+      if (!read_abs(at + 24, b.data(), rest)) return false;
+      Cur c(b);
+      if (version == 1) c.skip(4);
+      r.base_ = c.addr(so);
+      c.addr(so);  // free-space info
+      eof = c.addr(so);
+      c.addr(so);  // driver info
+      c.addr(so);  // root link name offset
+      root = c.addr(so);
+      if (c.bad) return fail(HTR_ERR_FORMAT, "bad root group entry");
+    }
+    if (root == kUndef) return fail(HTR_ERR_FORMAT, "no root group");
     if (eof != kUndef && eof > r.size_)
       return fail(HTR_ERR_FORMAT, "truncated file (" + std::to_string(r.size_) + " of " + std::to_string(eof) + " bytes)");
     return group(root, "", true);
   }
 
-  // all messages of a version-1 object header, continuation blocks followed
+  // Messages of one object header block.  Version 1: 8-byte message
+  // headers, bodies padded to 8.  Version 2: type (1), size (2), flags (1)
+  // and a creation order (2) when the header tracks it; a gap smaller than
+  // a message header may end the block.
+  bool messages(const uint8_t *p, size_t n, int version, bool crt_order, std::vector<Msg> &msgs,
+                std::vector<std::pair<uint64_t, uint64_t>> &chunks) {
+    Cur c(p, n);
+    const size_t hdr = version == 1 ? 8 : (crt_order ? 6 : 4);
+    while (c.left() >= hdr) {
+      uint16_t type, size;
+      uint8_t flags;
+      if (version == 1) {
+        type = c.u16();
+        size = c.u16();
+        flags = c.u8();
+        c.skip(3);
+      } else {
+        type = c.u8();
+        size = c.u16();
+        flags = c.u8();
+        if (crt_order) c.skip(2);
+      }
+      if (!c.need(size)) return fail(HTR_ERR_FORMAT, "object header message beyond its block");
+      Msg m{type, flags, std::vector<uint8_t>(c.p + c.i, c.p + c.i + size)};
+      c.skip(size);
+      if (type == 0x0010) {
+        Cur k(m.data);
+        const uint64_t addr = k.addr(so), len = k.uint(sl);
+        if (k.bad || addr == kUndef) return fail(HTR_ERR_FORMAT, "bad continuation message");
+        chunks.emplace_back(addr, len);
+      }
+      msgs.push_back(std::move(m));
+      if (msgs.size() > 65536) return fail(HTR_ERR_FORMAT, "too many header messages");
+    }
+    return true;
+  }
+
+  // all messages of an object header (version 1, or version 2 "OHDR" with
+  // "OCHK" continuation blocks and lookup3 checksums), continuations followed
   bool object(uint64_t rel, std::vector<Msg> &msgs) {
     std::vector<uint8_t> pre;
-    if (!block(rel, 16, pre)) return false;
-    if (std::memcmp(pre.data(), "OHDR", 4) == 0)
-      return fail(HTR_ERR_UNSUPPORTED, "version-2 object header (written with the latest file format)");
-    if (pre[0] != 1) return fail(HTR_ERR_FORMAT, "bad object header version " + std::to_string(pre[0]));
-    Cur p(pre);
-    p.skip(2);
-    const unsigned nmsgs = p.u16();
-    p.u32();
-    const uint32_t hsize = p.u32();
-    std::vector<std::pair<uint64_t, uint64_t>> chunks{{rel + 16, hsize}};
+    if (!block(rel, 6, pre)) return false;
+    std::vector<std::pair<uint64_t, uint64_t>> chunks;
+    int version = 1;
+    bool crt_order = false;
+    if (std::memcmp(pre.data(), "OHDR", 4) == 0) {
+      version = 2;
+      if (pre[4] != 2) return fail(HTR_ERR_FORMAT, "bad object header version " + std::to_string(pre[4]));
+      const uint8_t flags = pre[5];
+      crt_order = (flags & 0x04) != 0;
+      const size_t fixed = 6 + ((flags & 0x20) ? 16 : 0) + ((flags & 0x10) ? 4 : 0);
+      const int szb = 1 << (flags & 0x03);
+      std::vector<uint8_t> h;
+      if (!block(rel, fixed + szb, h)) return false;
+      Cur c(h.data() + fixed, szb);
+      const uint64_t chunk0 = c.uint(szb);
+      if (chunk0 > r.size_) return fail(HTR_ERR_FORMAT, "object header beyond the end of the file");
+      const size_t total = fixed + szb + chunk0 + 4;
+      std::vector<uint8_t> all;
+      if (!block(rel, total, all)) return false;
+      uint32_t sum = 0;
+      for (int k = 0; k < 4; k++) sum |= uint32_t(all[total - 4 + k]) << (8 * k);
+      if (sum != lookup3(all.data(), total - 4, 0)) return fail(HTR_ERR_FORMAT, "object header checksum mismatch");
+      if (!messages(all.data() + fixed + szb, chunk0, 2, crt_order, msgs, chunks)) return false;
+    } else {
+      if (!block(rel, 16, pre)) return false;
+      if (pre[0] != 1) return fail(HTR_ERR_FORMAT, "bad object header version " + std::to_string(pre[0]));
+      Cur p(pre);
+      p.skip(8);
+      const uint32_t hsize = p.u32();
+      chunks.emplace_back(rel + 16, hsize);
+    }
     for (size_t ci = 0; ci < chunks.size(); ci++) {
       if (ci > 256) return fail(HTR_ERR_FORMAT, "too many object header continuation blocks");
       std::vector<uint8_t> body;
       if (!block(chunks[ci].first, chunks[ci].second, body)) return false;
-      Cur c(body);
-      while (c.left() >= 8) {
-        const uint16_t type = c.u16();
-        const uint16_t size = c.u16();
-        const uint8_t flags = c.u8();
-        c.skip(3);
-        if (!c.need(size)) return fail(HTR_ERR_FORMAT, "object header message beyond its block");
-        Msg m{type, flags, std::vector<uint8_t>(c.p + c.i, c.p + c.i + size)};
-        c.skip(size);
-        if (type == 0x0010) {
-          Cur k(m.data);
-          const uint64_t addr = k.addr(so), len = k.uint(sl);
-          if (k.bad || addr == kUndef) return fail(HTR_ERR_FORMAT, "bad continuation message");
-          chunks.emplace_back(addr, len);
-        }
-        msgs.push_back(std::move(m));
-        if (msgs.size() > 65536) return fail(HTR_ERR_FORMAT, "too many header messages");
+      if (version == 1) {
+        if (!messages(body.data(), body.size(), 1, false, msgs, chunks)) return false;
+        continue;
       }
+      if (body.size() < 8 || std::memcmp(body.data(), "OCHK", 4) != 0)
+        return fail(HTR_ERR_FORMAT, "bad object header continuation block");
+      uint32_t sum = 0;
+      for (int k = 0; k < 4; k++) sum |= uint32_t(body[body.size() - 4 + k]) << (8 * k);
+      if (sum != lookup3(body.data(), body.size() - 4, 0))
+        return fail(HTR_ERR_FORMAT, "object header continuation checksum mismatch");
+      if (!messages(body.data() + 4, body.size() - 8, 2, crt_order, msgs, chunks)) return false;
     }
-    (void)nmsgs;
     return true;
   }
 

@@ -11,6 +11,8 @@
 //
 //   - superblock version 0 (a user block before it is allowed);
 //   - version-1 object headers with continuation blocks;
+//   - when reading, also the newer format's superblock versions 1-3 and
+//     version-2 object headers ("OHDR"/"OCHK", lookup3 checksums verified);
 //   - groups stored as a symbol table: a version-1 B-tree of group nodes
 //     (type 0), symbol table nodes and a local heap of link names; groups
 //     made of link messages are read as well;
@@ -19,9 +21,10 @@
 //   - dataspaces versions 1-2; data layout versions 1-4, contiguous or
 //     compact storage; attribute messages versions 1-3.
 //
-// What the reader meets outside that subset (chunked, filtered or virtual
-// storage, version-2 object headers, dense attribute or link storage,
-// variable-length types) is reported as unsupported, never guessed at.
+// The writer makes only the earliest format.  What the reader meets outside
+// the subset (chunked, filtered or virtual storage, dense attribute or link
+// storage in fractal heaps, variable-length types) is reported as
+// unsupported, never guessed at.
 #pragma once
 
 #include <cstdint>

@@ -31,10 +31,11 @@
  * file I/O overlapped; each call returns when its data are in the file or
  * in the view (it synchronises `stream`).  Errors: HTR_ERR_ARGUMENT,
  * HTR_ERR_LAYOUT, HTR_ERR_IO, HTR_ERR_FORMAT (a file that is not HDF5, is
- * truncated, or lacks a field or has another shape), HTR_ERR_UNSUPPORTED
- * (HDF5 storage outside the earliest format: chunked, compressed, dense
- * groups, version-2 object headers), HTR_ERR_CUDA; htr_last_error() tells
- * which.
+ * truncated, fails a metadata checksum, or lacks a field or has another
+ * shape), HTR_ERR_UNSUPPORTED (chunked, compressed or virtual storage,
+ * dense link or attribute storage), HTR_ERR_CUDA; htr_last_error() tells
+ * which.  Files are read in the earliest format and in the newer one
+ * (superblock 2/3, version-2 object headers, compact link groups).
  */
 #ifndef HTR_RESTART_H
 #define HTR_RESTART_H

@@ -382,3 +382,77 @@ def test_run_continues_from_a_restart(tmp_path):
     oa, ob = a.to_host(), b.to_host()
     for n in ("Conserved", "temperature", "pressure", "velocity", "rho"):
         assert util.rel_err(ob[n], oa[n]).max() <= util.RHS_REL_TOL, n
+
+
+# ---------------------------------------------------------------- newer file format
+
+def test_lookup3_published_vectors():
+    """Bob Jenkins' lookup3.c self-test values for hashlittle."""
+    from tests import h5_v2
+    assert h5_v2.lookup3(b"", 0) == 0xDEADBEEF
+    assert h5_v2.lookup3(b"", 0xDEADBEEF) == 0xBD5B7DDE
+    assert h5_v2.lookup3(b"Four score and seven years ago", 0) == 0x17770551
+    assert h5_v2.lookup3(b"Four score and seven years ago", 1) == 0xCD628161
+
+
+@needs_lib
+@pytest.mark.parametrize("kw", [{}, {"crt_order": True, "times": True}, {"split": True},
+                                {"split": True, "crt_order": True}])
+def test_reader_takes_the_newer_file_format(tmp_path, kw):
+    """Superblock 2, version-2 object headers (checksummed; continuation
+    blocks, creation order, times), link-message groups, attribute
+    version 3: a tile file in that format loads like one in the earliest."""
+    from tests import h5_v2
+    lib = runtime.lib()
+    f = random_fluid((5, 4, 3), seed=11)
+    r = abi.rect((0, 0, 0), (4, 3, 2))
+    d = tmp_path / "r"
+    d.mkdir()
+    path = restart.tile_filename(str(d), r)
+    h5_v2.tile_file(path, f, r, restart.IO_FIELDS, **kw).write(path)
+    g = fluid.Fluid(f.shape, f.nspec)
+    gv = g.view()
+    st = lib.htr_restart_read_tile(str(d).encode(), C.byref(gv), r, 5, abi.HTR_RESTART_HOST_VIEW, None)
+    assert st == abi.HTR_OK, lib.htr_last_error()
+    for n in restart.IO_FIELDS:
+        assert np.array_equal(g[n], f[n]), n
+    s = C.create_string_buffer(16)
+    abi.check(lib, lib.htr_h5_string_attribute(path.encode(), None, b"note", 0, s, 16))
+    assert s.value == b"latest"
+    rank, dims, per = C.c_int(), (C.c_int64 * 8)(), C.c_int64()
+    abi.check(lib, lib.htr_h5_dataset_shape(path.encode(), b"velocity", C.byref(rank), dims, C.byref(per)))
+    assert (rank.value, list(dims[:3]), per.value) == (3, [3, 4, 5], 3)
+
+
+@needs_lib
+def test_newer_format_checksums_and_dense_groups(tmp_path):
+    from tests import h5_v2
+    lib = runtime.lib()
+    f = random_fluid((4, 3, 2), seed=12)
+    r = abi.rect((0, 0, 0), (3, 2, 1))
+    path = restart.tile_filename(str(tmp_path), r)
+    w = h5_v2.tile_file(path, f, r, restart.IO_FIELDS, split=True)
+    w.write(path)
+    good = open(path, "rb").read()
+    g = fluid.Fluid(f.shape, f.nspec)
+    gv = g.view()
+    H = abi.HTR_RESTART_HOST_VIEW
+
+    def status(data):
+        with open(path, "wb") as fh:
+            fh.write(data)
+        return lib.htr_restart_read_tile(str(tmp_path).encode(), C.byref(gv), r, 5, H, None)
+
+    # one flipped bit in each kind of metadata block: the superblock's base
+    # address, an object header's chunk size, a continuation block's message
+    for marker, off in ((b"\x89HDF", 12), (b"OHDR", 6), (b"OCHK", 6)):
+        at = good.index(marker) + off
+        bad = bytearray(good)
+        bad[at] ^= 0x10
+        assert status(bytes(bad)) == abi.HTR_ERR_FORMAT, marker
+        assert b"checksum mismatch" in lib.htr_last_error(), (marker, lib.htr_last_error())
+    assert status(good) == abi.HTR_OK
+    # links in a fractal heap (dense storage) are outside the subset
+    w.write(path, root_links_dense=True)
+    assert lib.htr_restart_read_tile(str(tmp_path).encode(), C.byref(gv), r, 5, H, None) == abi.HTR_ERR_UNSUPPORTED
+    assert b"dense" in lib.htr_last_error()
