@@ -108,9 +108,14 @@ def read_master(dirname):
     }
 
 
-def load(dirname, fluid, profiles=False, stream=None):
+def load(dirname, fluid, profiles=False, stream=None, mixture=None):
     """Fills the restart fields of `fluid` from `dirname`; returns the
-    master file's timeStep, simTime and channelForcing."""
+    master file's timeStep, simTime and channelForcing.  With `mixture` (a
+    loaded mixture handle; device grids) the transport properties and the
+    conserved variables are then rebuilt from the loaded primitives over the
+    whole grid, as a run started from a restart initialises them."""
+    if mixture is not None and fluid.device is None:
+        raise abi.HtrError("rebuilding the state from a restart needs a device grid")
     m = read_master(dirname)
     b, fb = m["bounds"], fluid.bounds()
     if list(b.lo) != list(fb.lo) or list(b.hi) != list(fb.hi):
@@ -123,4 +128,10 @@ def load(dirname, fluid, profiles=False, stream=None):
     d = os.fsencode(dirname)
     for r in m["partitions"]:
         abi.check(lib, lib.htr_restart_read_tile(d, C.byref(view), r, fluid.nspec, flags, s), "htr_restart_read_tile")
+    if mixture is not None:
+        b = fluid.bounds()
+        abi.check(lib, lib.htr_UpdatePropertiesFromPrimitive(C.byref(view), b, mixture, s),
+                  "htr_UpdatePropertiesFromPrimitive")
+        abi.check(lib, lib.htr_UpdateConservedFromPrimitive(C.byref(view), b, mixture, s),
+                  "htr_UpdateConservedFromPrimitive")
     return {k: m[k] for k in ("timeStep", "simTime", "channelForcing")}

@@ -276,6 +276,9 @@ def test_errors(tmp_path):
     arr = (abi.htr_rect3 * 1)(r)
     assert lib.htr_restart_write_master(d.encode(), C.byref(info), r, t, arr, 5, None, None) == \
         abi.HTR_ERR_ARGUMENT
+    # the state is rebuilt on device grids only
+    with pytest.raises(abi.HtrError, match="device grid"):
+        restart.load(d, fluid.Fluid(f.shape, f.nspec), mixture=C.c_void_p(1))
     # a grid of another size refuses the restart
     with pytest.raises(abi.HtrError, match="baseIndexSpace"):
         restart.load(d, fluid.Fluid((5, 3, 2), 5))
@@ -373,9 +376,8 @@ def test_run_continues_from_a_restart(tmp_path):
     b = host.to_device("cuda:0")  # grid fields (metrics, node types) of the same grid
     for n in restart.IO_FIELDS:
         b.arrays[n].zero_()
-    info = restart.load(str(tmp_path), b)
+    info = restart.load(str(tmp_path), b, mixture=gh)
     assert info["timeStep"] == 1 and info["simTime"] == dt
-    workloads.derive_state(runtime.lib(), b, gh, runtime.stream_handle())
     runtime.rk3_step(a, gh, scheme="Hybrid", dt=dt, chemistry=False)
     runtime.rk3_step(b, gh, scheme="Hybrid", dt=dt, chemistry=False)
     torch.cuda.synchronize()
