@@ -107,3 +107,37 @@ def test_step_is_translation_invariant_and_deterministic(box):
     torch.cuda.synchronize()
     for name in ("Conserved", "temperature", "shockSensorX"):
         assert torch.equal(a[name], c[name]), name
+
+
+@pytest.mark.gpu
+def test_boundary_layer_step_is_z_translation_invariant():
+    """The 512 x 192 x 128 TENO-LAD boundary layer (NSCBC inflow/outflow in
+    x, isothermal wall and outflow in y, periodic z): one fused step of the
+    state rolled along z equals the rolled step bit for bit, NSCBC planes,
+    walls and the interior's maximum Mach number included."""
+    import torch
+
+    from htr_gb300 import runtime, wall, workloads
+    lib = runtime.lib()
+    host = wall.boundary_layer(num=(512, 192, 128), seed=77)
+    g, bc = host.meta["grid"], host.meta["bc"]
+    m = workloads.make_mixture_struct(lib, host.meta["eos"], host.meta["mix"])
+    gh = runtime.load_mixture(host.meta["eos"], m)
+    a = host.to_device("cuda:0")
+    del host
+    g.fill(a, lib)
+    workloads.derive_state(lib, a, gh, runtime.stream_handle())
+    mach = torch.zeros(1, dtype=torch.float64, device="cuda:0")
+    dt = wall.BoundaryRun(lib, a, gh, bc, stream=runtime.stream_handle(), max_mach_buffer=mach).spectral_dt(0.8)
+    b = a.copy()
+    for name, arr in b.arrays.items():
+        arr.copy_(torch.roll(a.arrays[name], shifts=37, dims=0))
+    wall.FusedBoundaryRun(a, gh, bc).step(dt)
+    wall.FusedBoundaryRun(b, gh, bc).step(dt)
+    torch.cuda.synchronize()
+    assert torch.isfinite(a["Conserved"]).all()
+    for name in ("Conserved", "temperature", "pressure", "velocity", "mu", "dudtBoundary", "dTdtBoundary"):
+        rolled = torch.roll(a[name], shifts=37, dims=0)
+        diff = ((rolled - b[name]).abs().max() / rolled.abs().max().clamp_min(1e-300)).item()
+        print(f"{name}: max |shifted - rolled| / max = {diff:.3e}")
+        assert torch.equal(rolled, b[name]), name
