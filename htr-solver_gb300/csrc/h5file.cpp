@@ -1004,6 +1004,84 @@ struct Parser {
     return !c.bad || fail(HTR_ERR_FORMAT, "truncated B-tree node");
   }
 
+  // reads a checksummed block of `n` bytes (the last 4 are its lookup3
+  // checksum) that starts with `sig`
+  bool checked(uint64_t rel, size_t n, const char *sig, std::vector<uint8_t> &out) {
+    if (!block(rel, n, out)) return false;
+    if (std::memcmp(out.data(), sig, 4) != 0) return fail(HTR_ERR_FORMAT, std::string("bad ") + sig + " signature");
+    uint32_t sum = 0;
+    for (int k = 0; k < 4; k++) sum |= uint32_t(out[n - 4 + k]) << (8 * k);
+    if (sum != lookup3(out.data(), n - 4, 0)) return fail(HTR_ERR_FORMAT, std::string(sig) + " checksum mismatch");
+    return true;
+  }
+
+  // Links of a group in dense storage: link messages kept as objects of a
+  // fractal heap, found through the version-2 B-tree of link-name records
+  // (type 5: name hash, heap ID).  Handled: an unfiltered heap that is one
+  // root direct block and a B-tree that is one root leaf — the shape of a
+  // group of up to about fifteen links with short names, more than any
+  // restart file has; a larger heap or tree is reported as unsupported.
+  bool dense_links(uint64_t fheap, uint64_t bt2, std::vector<std::pair<std::string, uint64_t>> &links) {
+    const size_t hsize = 4 + 1 + 2 + 2 + 1 + 4 + 12 * size_t(sl) + 3 * size_t(so) + 2 + 2 + 2 + 2 + 4;
+    std::vector<uint8_t> h;
+    if (!checked(fheap, hsize, "FRHP", h)) return false;
+    Cur c(h.data() + 4, hsize - 4);
+    if (c.u8() != 0) return fail(HTR_ERR_UNSUPPORTED, "fractal heap version");
+    const uint16_t id_len = c.u16(), filt_len = c.u16();
+    c.u8();   // flags
+    c.u32();  // maximum size of managed objects
+    c.uint(sl);
+    c.addr(so);  // huge objects
+    c.uint(sl);
+    c.addr(so);  // free-space manager
+    for (int k = 0; k < 8; k++) c.uint(sl);  // managed space, iterator, object counts and sizes
+    const uint16_t width = c.u16();
+    const uint64_t start_block = c.uint(sl), max_direct = c.uint(sl);
+    const uint16_t max_bits = c.u16();
+    c.u16();  // starting rows of the root indirect block
+    const uint64_t root = c.addr(so);
+    const uint16_t rows = c.u16();
+    if (c.bad) return fail(HTR_ERR_FORMAT, "truncated fractal heap header");
+    if (filt_len != 0) return fail(HTR_ERR_UNSUPPORTED, "filtered fractal heap");
+    const int off_size = (max_bits + 7) / 8;
+    const int len_size = int(id_len) - 1 - off_size;
+    if (width == 0 || start_block == 0 || max_direct < start_block || off_size < 1 || off_size > 8 || len_size < 1 ||
+        len_size > 8)
+      return fail(HTR_ERR_FORMAT, "bad fractal heap parameters");
+    if (rows != 0) return fail(HTR_ERR_UNSUPPORTED, "fractal heap grown past its root direct block");
+    // the name index: header, then its root leaf
+    const size_t bsize = 4 + 1 + 1 + 4 + 2 + 2 + 1 + 1 + size_t(so) + 2 + size_t(sl) + 4;
+    std::vector<uint8_t> bh;
+    if (!checked(bt2, bsize, "BTHD", bh)) return false;
+    Cur b(bh.data() + 4, bsize - 4);
+    b.u8();
+    const uint8_t type = b.u8();
+    b.u32();  // node size
+    const uint16_t rec = b.u16(), depth = b.u16();
+    b.u8();
+    b.u8();
+    const uint64_t leaf = b.addr(so);
+    const uint16_t nrec = b.u16();
+    if (type != 5 || rec != 4 + id_len) return fail(HTR_ERR_FORMAT, "link name index of another record type");
+    if (depth != 0) return fail(HTR_ERR_UNSUPPORTED, "link name index deeper than one leaf");
+    if (nrec == 0) return true;
+    std::vector<uint8_t> lf;
+    if (!checked(leaf, 6 + size_t(nrec) * rec + 4, "BTLF", lf)) return false;
+    for (unsigned r = 0; r < nrec; r++) {
+      Cur e(lf.data() + 6 + size_t(r) * rec, rec);
+      e.u32();  // name hash
+      const uint8_t idb = e.u8();
+      if (((idb >> 4) & 0x03) != 0) return fail(HTR_ERR_UNSUPPORTED, "link stored as a huge or tiny heap object");
+      const uint64_t off = e.uint(off_size), len = e.uint(len_size);
+      // an object's offset counts from the start of the root direct block
+      if (len == 0 || off >= start_block || len > start_block - off) return fail(HTR_ERR_FORMAT, "bad heap ID");
+      Msg m{0x0006, 0, {}};
+      if (!block(root + off, len, m.data)) return false;
+      if (!link_message(m, links)) return false;
+    }
+    return true;
+  }
+
   bool link_message(const Msg &m, std::vector<std::pair<std::string, uint64_t>> &links) {
     Cur c(m.data);
     if (c.u8() != 1) return fail(HTR_ERR_UNSUPPORTED, "link message version");
@@ -1044,7 +1122,9 @@ struct Parser {
         const uint8_t flags = c.u8();
         if (flags & 0x01) c.skip(8);
         const uint64_t fheap = c.addr(so);
-        if (fheap != kUndef) return fail(HTR_ERR_UNSUPPORTED, "group with dense link storage");
+        const uint64_t names = c.addr(so);
+        if (c.bad) return fail(HTR_ERR_FORMAT, "bad link info message");
+        if (fheap != kUndef && !dense_links(fheap, names, links)) return false;
       } else if (m.type == 0x000c && root) {
         std::string name;
         Value v;

@@ -11,8 +11,10 @@
 //
 //   - superblock version 0 (a user block before it is allowed);
 //   - version-1 object headers with continuation blocks;
-//   - when reading, also the newer format's superblock versions 1-3 and
-//     version-2 object headers ("OHDR"/"OCHK", lookup3 checksums verified);
+//   - when reading, also the newer format's superblock versions 1-3,
+//     version-2 object headers ("OHDR"/"OCHK", lookup3 checksums verified)
+//     and dense groups (links in a one-block fractal heap, indexed by a
+//     one-leaf version-2 B-tree);
 //   - groups stored as a symbol table: a version-1 B-tree of group nodes
 //     (type 0), symbol table nodes and a local heap of link names; groups
 //     made of link messages are read as well;
@@ -22,8 +24,8 @@
 //     compact storage; attribute messages versions 1-3.
 //
 // The writer makes only the earliest format.  What the reader meets outside
-// the subset (chunked, filtered or virtual storage, dense attribute or link
-// storage in fractal heaps, variable-length types) is reported as
+// the subset (chunked, filtered or virtual storage, dense attribute storage,
+// larger fractal heaps or B-trees, variable-length types) is reported as
 // unsupported, never guessed at.
 #pragma once
 

@@ -1,7 +1,8 @@
 """Test helper: writes small HDF5 files in the newer ("1.8") file format —
 superblock version 2, version-2 object headers ("OHDR", optional "OCHK"
 continuation blocks, creation-order and time fields), groups of link
-messages, attribute messages version 3, dataspace version 2, compound
+messages or dense groups (links in a fractal heap indexed by a version-2
+B-tree of name hashes), attribute messages version 3, dataspace version 2, compound
 version 3 and array version 3 datatypes, contiguous layout version 3 — so
 that the library's reader is tested on a format its writer does not make.
 Written from the HDF5 File Format Specification (version 3.0); the metadata
@@ -137,7 +138,42 @@ class Writer:
         blk += struct.pack("<I", lookup3(blk))
         return blk, cont
 
-    def write(self, path, root_links_dense=False):
+    def _dense(self, at, links):
+        """Fractal heap (one 512-byte root direct block holding the link
+        messages) and a version-2 B-tree (one leaf of type-5 records) at
+        `at`: returns (bytes, heap address, B-tree address)."""
+        start_block, off_size, len_size = 512, 4, 2
+        heap_at = at
+        hdr_len = 4 + 1 + 2 + 2 + 1 + 4 + 12 * 8 + 3 * 8 + 8 + 4
+        dblock_at = heap_at + hdr_len
+        objs, ids = b"", []
+        head = 4 + 1 + 8 + off_size  # FHDB, version, heap address, block offset
+        for name, addr in links:
+            body = link(name, addr)
+            ids.append((lookup3(name.encode()),
+                        bytes([0]) + (head + len(objs)).to_bytes(off_size, "little") +
+                        len(body).to_bytes(len_size, "little")))
+            objs += body
+        assert head + len(objs) <= start_block
+        dblock = b"FHDB" + bytes([0]) + struct.pack("<Q", heap_at) + bytes(off_size) + objs
+        dblock += bytes(start_block - len(dblock))
+        hdr = b"FRHP" + bytes([0]) + struct.pack("<HHBI", 1 + off_size + len_size, 0, 0, 4096)
+        hdr += struct.pack("<QQQQ", 0, UNDEF, start_block - head - len(objs), UNDEF)
+        hdr += struct.pack("<QQQQQQQQ", start_block, start_block, start_block, len(links), 0, 0, 0, 0)
+        hdr += struct.pack("<HQQHHQH", 4, start_block, 65536, 8 * off_size, 0, dblock_at, 0)
+        hdr += struct.pack("<I", lookup3(hdr))
+        assert len(hdr) == hdr_len
+        bt_at = dblock_at + len(dblock)
+        rec = 4 + len(ids[0][1])
+        leaf_at = bt_at + 4 + 1 + 1 + 4 + 2 + 2 + 1 + 1 + 8 + 2 + 8 + 4
+        bth = b"BTHD" + bytes([0, 5]) + struct.pack("<IHHBBQHQ", 512, rec, 0, 100, 40, leaf_at, len(ids), len(ids))
+        bth += struct.pack("<I", lookup3(bth))
+        leaf = b"BTLF" + bytes([0, 5]) + b"".join(struct.pack("<I", h) + i for h, i in sorted(ids))
+        leaf += struct.pack("<I", lookup3(leaf))
+        leaf += bytes(512 - len(leaf))
+        return hdr + dblock + bth + leaf, heap_at, bt_at
+
+    def write(self, path, root_links_dense=False, dense=False):
         so = 8
         sb_size = 12 + 4 * so + 4
         at = sb_size
@@ -155,9 +191,16 @@ class Writer:
             set_addr.append(at)
             blobs += [oh, cont]
             at += len(oh) + len(cont)
-        linfo = LINK_INFO if not root_links_dense else bytes([0, 0]) + struct.pack("<QQ", 1234, 5678)
-        root_msgs = [(0x02, linfo), (0x0A, GROUP_INFO)] + \
-            [(0x06, link(name, set_addr[k])) for k, (name, _m, _d) in enumerate(self.sets)] + self.root_msgs
+        links = [(name, set_addr[k]) for k, (name, _m, _d) in enumerate(self.sets)]
+        if dense:
+            blob, heap_at, bt_at = self._dense(at, links)
+            blobs.append(blob)
+            at += len(blob)
+            root_msgs = [(0x02, bytes([0, 0]) + struct.pack("<QQ", heap_at, bt_at)), (0x0A, GROUP_INFO)] + \
+                self.root_msgs
+        else:
+            linfo = LINK_INFO if not root_links_dense else bytes([0, 0]) + struct.pack("<QQ", 1234, 5678)
+            root_msgs = [(0x02, linfo), (0x0A, GROUP_INFO)] + [(0x06, link(n, a)) for n, a in links] + self.root_msgs
         oh, cont = self._header(root_msgs, at)
         root = at
         blobs += [oh, cont]

@@ -454,7 +454,52 @@ def test_newer_format_checksums_and_dense_groups(tmp_path):
         assert status(bytes(bad)) == abi.HTR_ERR_FORMAT, marker
         assert b"checksum mismatch" in lib.htr_last_error(), (marker, lib.htr_last_error())
     assert status(good) == abi.HTR_OK
-    # links in a fractal heap (dense storage) are outside the subset
+    # a link info message pointing at no fractal heap
     w.write(path, root_links_dense=True)
-    assert lib.htr_restart_read_tile(str(tmp_path).encode(), C.byref(gv), r, 5, H, None) == abi.HTR_ERR_UNSUPPORTED
-    assert b"dense" in lib.htr_last_error()
+    assert lib.htr_restart_read_tile(str(tmp_path).encode(), C.byref(gv), r, 5, H, None) == abi.HTR_ERR_FORMAT
+    assert b"FRHP" in lib.htr_last_error()
+
+
+@needs_lib
+@pytest.mark.parametrize("kw", [{}, {"crt_order": True, "split": True}])
+def test_reader_takes_dense_groups(tmp_path, kw):
+    """A tile with the three profile fields has ten links, more than the
+    newer format keeps in the object header: they sit in a fractal heap
+    indexed by a version-2 B-tree of name hashes."""
+    from tests import h5_v2
+    lib = runtime.lib()
+    f = random_fluid((5, 4, 3), seed=13, profiles=True)
+    r = abi.rect((0, 0, 0), (4, 3, 2))
+    path = restart.tile_filename(str(tmp_path), r)
+    names = restart.IO_FIELDS + restart.PROFILE_FIELDS
+    h5_v2.tile_file(path, f, r, names, **kw).write(path, dense=True)
+    assert b"FRHP" in open(path, "rb").read() and b"BTLF" in open(path, "rb").read()
+    g = fluid.Fluid(f.shape, f.nspec)
+    gv = g.view()
+    st = lib.htr_restart_read_tile(str(tmp_path).encode(), C.byref(gv), r, 5,
+                                   abi.HTR_RESTART_HOST_VIEW | abi.HTR_RESTART_PROFILES, None)
+    assert st == abi.HTR_OK, lib.htr_last_error()
+    for n in names:
+        assert np.array_equal(g[n], f[n]), n
+    # a flipped bit in the heap header or the name index is caught
+    good = open(path, "rb").read()
+    for marker in (b"FRHP", b"BTHD", b"BTLF"):
+        bad = bytearray(good)
+        bad[good.index(marker) + 8] ^= 0x04
+        with open(path, "wb") as fh:
+            fh.write(bytes(bad))
+        assert lib.htr_restart_read_tile(str(tmp_path).encode(), C.byref(gv), r, 5,
+                                         abi.HTR_RESTART_HOST_VIEW | abi.HTR_RESTART_PROFILES,
+                                         None) == abi.HTR_ERR_FORMAT, marker
+        assert b"checksum mismatch" in lib.htr_last_error(), marker
+    # a name index deeper than one leaf is outside the subset (checksum kept valid)
+    at = good.index(b"BTHD")
+    bad = bytearray(good)
+    bad[at + 12] = 1
+    bad[at + 34:at + 38] = h5_v2.lookup3(bytes(bad[at:at + 34])).to_bytes(4, "little")
+    with open(path, "wb") as fh:
+        fh.write(bytes(bad))
+    assert lib.htr_restart_read_tile(str(tmp_path).encode(), C.byref(gv), r, 5,
+                                     abi.HTR_RESTART_HOST_VIEW | abi.HTR_RESTART_PROFILES,
+                                     None) == abi.HTR_ERR_UNSUPPORTED
+    assert b"deeper" in lib.htr_last_error()
