@@ -1015,13 +1015,15 @@ struct Parser {
     return true;
   }
 
-  // Links of a group in dense storage: link messages kept as objects of a
-  // fractal heap, found through the version-2 B-tree of link-name records
-  // (type 5: name hash, heap ID).  Handled: an unfiltered heap that is one
-  // root direct block and a B-tree that is one root leaf — the shape of a
-  // group of up to about fifteen links with short names, more than any
-  // restart file has; a larger heap or tree is reported as unsupported.
-  bool dense_links(uint64_t fheap, uint64_t bt2, std::vector<std::pair<std::string, uint64_t>> &links) {
+  // Objects of dense storage: messages kept as objects of a fractal heap,
+  // found through a version-2 B-tree of name records — type 5 for links
+  // (name hash, heap ID), type 8 for attributes (heap ID, message flags,
+  // creation order, name hash).  Handled: an unfiltered heap that is one
+  // root direct block and a B-tree that is one root leaf — the shape of up
+  // to about fifteen short links or a few attributes, more than any restart
+  // file has; a larger heap or tree is reported as unsupported.
+  bool dense_objects(uint64_t fheap, uint64_t bt2, int want, std::vector<std::vector<uint8_t>> &objects) {
+    const char *what = want == 5 ? "link" : "attribute";
     const size_t hsize = 4 + 1 + 2 + 2 + 1 + 4 + 12 * size_t(sl) + 3 * size_t(so) + 2 + 2 + 2 + 2 + 4;
     std::vector<uint8_t> h;
     if (!checked(fheap, hsize, "FRHP", h)) return false;
@@ -1062,22 +1064,51 @@ struct Parser {
     b.u8();
     const uint64_t leaf = b.addr(so);
     const uint16_t nrec = b.u16();
-    if (type != 5 || rec != 4 + id_len) return fail(HTR_ERR_FORMAT, "link name index of another record type");
-    if (depth != 0) return fail(HTR_ERR_UNSUPPORTED, "link name index deeper than one leaf");
+    if (type != want || rec != id_len + (want == 5 ? 4 : 9))
+      return fail(HTR_ERR_FORMAT, std::string(what) + " name index of another record type");
+    if (depth != 0) return fail(HTR_ERR_UNSUPPORTED, std::string(what) + " name index deeper than one leaf");
     if (nrec == 0) return true;
     std::vector<uint8_t> lf;
     if (!checked(leaf, 6 + size_t(nrec) * rec + 4, "BTLF", lf)) return false;
     for (unsigned r = 0; r < nrec; r++) {
       Cur e(lf.data() + 6 + size_t(r) * rec, rec);
-      e.u32();  // name hash
+      if (want == 5) e.u32();  // name hash first in a link record
       const uint8_t idb = e.u8();
-      if (((idb >> 4) & 0x03) != 0) return fail(HTR_ERR_UNSUPPORTED, "link stored as a huge or tiny heap object");
+      if (((idb >> 4) & 0x03) != 0)
+        return fail(HTR_ERR_UNSUPPORTED, std::string(what) + " stored as a huge or tiny heap object");
       const uint64_t off = e.uint(off_size), len = e.uint(len_size);
       // an object's offset counts from the start of the root direct block
       if (len == 0 || off >= start_block || len > start_block - off) return fail(HTR_ERR_FORMAT, "bad heap ID");
-      Msg m{0x0006, 0, {}};
-      if (!block(root + off, len, m.data)) return false;
-      if (!link_message(m, links)) return false;
+      objects.emplace_back();
+      if (!block(root + off, len, objects.back())) return false;
+    }
+    return true;
+  }
+
+  bool dense_links(uint64_t fheap, uint64_t bt2, std::vector<std::pair<std::string, uint64_t>> &links) {
+    std::vector<std::vector<uint8_t>> objs;
+    if (!dense_objects(fheap, bt2, 5, objs)) return false;
+    for (auto &o : objs)
+      if (!link_message(Msg{0x0006, 0, std::move(o)}, links)) return false;
+    return true;
+  }
+
+  // attributes named by an attribute info message (dense storage), if any
+  bool dense_attributes(const Msg &info, std::vector<std::pair<std::string, Value>> &out) {
+    Cur c(info.data);
+    if (c.u8() != 0) return fail(HTR_ERR_UNSUPPORTED, "attribute info message version");
+    const uint8_t flags = c.u8();
+    if (flags & 0x01) c.skip(2);
+    const uint64_t fheap = c.addr(so), names = c.addr(so);
+    if (c.bad) return fail(HTR_ERR_FORMAT, "bad attribute info message");
+    if (fheap == kUndef) return true;
+    std::vector<std::vector<uint8_t>> objs;
+    if (!dense_objects(fheap, names, 8, objs)) return false;
+    for (auto &o : objs) {
+      std::string name;
+      Value v;
+      if (!attribute(Msg{0x000c, 0, std::move(o)}, name, v)) return false;
+      out.emplace_back(name, std::move(v));
     }
     return true;
   }
@@ -1125,6 +1156,8 @@ struct Parser {
         const uint64_t names = c.addr(so);
         if (c.bad) return fail(HTR_ERR_FORMAT, "bad link info message");
         if (fheap != kUndef && !dense_links(fheap, names, links)) return false;
+      } else if (m.type == 0x0015 && root) {
+        if (!dense_attributes(m, r.attrs_)) return false;
       } else if (m.type == 0x000c && root) {
         std::string name;
         Value v;
@@ -1208,6 +1241,9 @@ struct Parser {
           d.attrs.emplace_back(an, std::move(v));
           break;
         }
+        case 0x0015:
+          if (!dense_attributes(m, d.attrs)) return false;
+          break;
         default:
           break;
       }

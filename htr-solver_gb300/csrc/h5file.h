@@ -13,8 +13,8 @@
 //   - version-1 object headers with continuation blocks;
 //   - when reading, also the newer format's superblock versions 1-3,
 //     version-2 object headers ("OHDR"/"OCHK", lookup3 checksums verified)
-//     and dense groups (links in a one-block fractal heap, indexed by a
-//     one-leaf version-2 B-tree);
+//     and dense storage of links and attributes (objects of a one-block
+//     fractal heap, indexed by a one-leaf version-2 B-tree);
 //   - groups stored as a symbol table: a version-1 B-tree of group nodes
 //     (type 0), symbol table nodes and a local heap of link names; groups
 //     made of link messages are read as well;
@@ -24,9 +24,9 @@
 //     compact storage; attribute messages versions 1-3.
 //
 // The writer makes only the earliest format.  What the reader meets outside
-// the subset (chunked, filtered or virtual storage, dense attribute storage,
-// larger fractal heaps or B-trees, variable-length types) is reported as
-// unsupported, never guessed at.
+// the subset (chunked, filtered or virtual storage, larger fractal heaps or
+// B-trees, variable-length types) is reported as unsupported, never guessed
+// at.
 #pragma once
 
 #include <cstdint>

@@ -33,10 +33,10 @@
  * HTR_ERR_LAYOUT, HTR_ERR_IO, HTR_ERR_FORMAT (a file that is not HDF5, is
  * truncated, fails a metadata checksum, or lacks a field or has another
  * shape), HTR_ERR_UNSUPPORTED (chunked, compressed or virtual storage,
- * dense attribute storage, link heaps beyond one block), HTR_ERR_CUDA;
+ * link or attribute heaps beyond one block), HTR_ERR_CUDA;
  * htr_last_error() tells which.  Files are read in the earliest format and
  * in the newer one (superblock 2/3, version-2 object headers, compact or
- * dense link groups).
+ * dense links and attributes).
  */
 #ifndef HTR_RESTART_H
 #define HTR_RESTART_H

@@ -2,7 +2,8 @@
 superblock version 2, version-2 object headers ("OHDR", optional "OCHK"
 continuation blocks, creation-order and time fields), groups of link
 messages or dense groups (links in a fractal heap indexed by a version-2
-B-tree of name hashes), attribute messages version 3, dataspace version 2, compound
+B-tree of name hashes), attribute messages version 3 (also in dense
+storage), dataspace version 2, compound
 version 3 and array version 3 datatypes, contiguous layout version 3 — so
 that the library's reader is tested on a format its writer does not make.
 Written from the HDF5 File Format Specification (version 3.0); the metadata
@@ -138,42 +139,44 @@ class Writer:
         blk += struct.pack("<I", lookup3(blk))
         return blk, cont
 
-    def _dense(self, at, links):
-        """Fractal heap (one 512-byte root direct block holding the link
-        messages) and a version-2 B-tree (one leaf of type-5 records) at
-        `at`: returns (bytes, heap address, B-tree address)."""
-        start_block, off_size, len_size = 512, 4, 2
+    def _dense(self, at, objects, rtype):
+        """Fractal heap (one 512-byte root direct block holding the message
+        bodies of `objects`, (name, body) pairs) and a version-2 B-tree (one
+        leaf of records of type `rtype`: 5 links, 8 attributes) at `at`:
+        returns (bytes, heap address, B-tree address)."""
+        start_block, off_size = 512, 4
+        len_size = 2 if rtype == 5 else 3  # heap IDs of 7 (links) or 8 (attributes) bytes
         heap_at = at
         hdr_len = 4 + 1 + 2 + 2 + 1 + 4 + 12 * 8 + 3 * 8 + 8 + 4
         dblock_at = heap_at + hdr_len
-        objs, ids = b"", []
+        objs, recs = b"", []
         head = 4 + 1 + 8 + off_size  # FHDB, version, heap address, block offset
-        for name, addr in links:
-            body = link(name, addr)
-            ids.append((lookup3(name.encode()),
-                        bytes([0]) + (head + len(objs)).to_bytes(off_size, "little") +
-                        len(body).to_bytes(len_size, "little")))
+        for k, (name, body) in enumerate(objects):
+            hid = bytes([0]) + (head + len(objs)).to_bytes(off_size, "little") + len(body).to_bytes(len_size, "little")
+            h = lookup3(name.encode())
+            recs.append((h, struct.pack("<I", h) + hid if rtype == 5 else hid + bytes([0]) + struct.pack("<II", k, h)))
             objs += body
         assert head + len(objs) <= start_block
         dblock = b"FHDB" + bytes([0]) + struct.pack("<Q", heap_at) + bytes(off_size) + objs
         dblock += bytes(start_block - len(dblock))
         hdr = b"FRHP" + bytes([0]) + struct.pack("<HHBI", 1 + off_size + len_size, 0, 0, 4096)
         hdr += struct.pack("<QQQQ", 0, UNDEF, start_block - head - len(objs), UNDEF)
-        hdr += struct.pack("<QQQQQQQQ", start_block, start_block, start_block, len(links), 0, 0, 0, 0)
+        hdr += struct.pack("<QQQQQQQQ", start_block, start_block, start_block, len(objects), 0, 0, 0, 0)
         hdr += struct.pack("<HQQHHQH", 4, start_block, 65536, 8 * off_size, 0, dblock_at, 0)
         hdr += struct.pack("<I", lookup3(hdr))
         assert len(hdr) == hdr_len
         bt_at = dblock_at + len(dblock)
-        rec = 4 + len(ids[0][1])
+        rec = len(recs[0][1])
         leaf_at = bt_at + 4 + 1 + 1 + 4 + 2 + 2 + 1 + 1 + 8 + 2 + 8 + 4
-        bth = b"BTHD" + bytes([0, 5]) + struct.pack("<IHHBBQHQ", 512, rec, 0, 100, 40, leaf_at, len(ids), len(ids))
+        bth = b"BTHD" + bytes([0, rtype]) + struct.pack("<IHHBBQHQ", 512, rec, 0, 100, 40, leaf_at, len(recs),
+                                                        len(recs))
         bth += struct.pack("<I", lookup3(bth))
-        leaf = b"BTLF" + bytes([0, 5]) + b"".join(struct.pack("<I", h) + i for h, i in sorted(ids))
+        leaf = b"BTLF" + bytes([0, rtype]) + b"".join(r for _h, r in sorted(recs))
         leaf += struct.pack("<I", lookup3(leaf))
         leaf += bytes(512 - len(leaf))
         return hdr + dblock + bth + leaf, heap_at, bt_at
 
-    def write(self, path, root_links_dense=False, dense=False):
+    def write(self, path, root_links_dense=False, dense=False, dense_attrs=False):
         so = 8
         sb_size = 12 + 4 * so + 4
         at = sb_size
@@ -192,15 +195,22 @@ class Writer:
             blobs += [oh, cont]
             at += len(oh) + len(cont)
         links = [(name, set_addr[k]) for k, (name, _m, _d) in enumerate(self.sets)]
-        if dense:
-            blob, heap_at, bt_at = self._dense(at, links)
+        attrs = self.root_msgs
+        if dense_attrs:
+            # version-3 attribute: 9 bytes of header, then the name and its NUL
+            named = [(body[9:9 + struct.unpack("<H", body[2:4])[0] - 1].decode(), body) for _t, body in attrs]
+            blob, heap_at, bt_at = self._dense(at, named, 8)
             blobs.append(blob)
             at += len(blob)
-            root_msgs = [(0x02, bytes([0, 0]) + struct.pack("<QQ", heap_at, bt_at)), (0x0A, GROUP_INFO)] + \
-                self.root_msgs
+            attrs = [(0x15, bytes([0, 0]) + struct.pack("<QQ", heap_at, bt_at))]
+        if dense:
+            blob, heap_at, bt_at = self._dense(at, [(n, link(n, a)) for n, a in links], 5)
+            blobs.append(blob)
+            at += len(blob)
+            root_msgs = [(0x02, bytes([0, 0]) + struct.pack("<QQ", heap_at, bt_at)), (0x0A, GROUP_INFO)] + attrs
         else:
             linfo = LINK_INFO if not root_links_dense else bytes([0, 0]) + struct.pack("<QQ", 1234, 5678)
-            root_msgs = [(0x02, linfo), (0x0A, GROUP_INFO)] + [(0x06, link(n, a)) for n, a in links] + self.root_msgs
+            root_msgs = [(0x02, linfo), (0x0A, GROUP_INFO)] + [(0x06, link(n, a)) for n, a in links] + attrs
         oh, cont = self._header(root_msgs, at)
         root = at
         blobs += [oh, cont]

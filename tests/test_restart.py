@@ -503,3 +503,32 @@ def test_reader_takes_dense_groups(tmp_path, kw):
                                      abi.HTR_RESTART_HOST_VIEW | abi.HTR_RESTART_PROFILES,
                                      None) == abi.HTR_ERR_UNSUPPORTED
     assert b"deeper" in lib.htr_last_error()
+
+
+@needs_lib
+def test_reader_takes_dense_attributes(tmp_path):
+    """Root attributes in dense storage (attribute info message, fractal
+    heap, version-2 B-tree of type-8 records), links dense as well."""
+    from tests import h5_v2
+    lib = runtime.lib()
+    f = random_fluid((4, 3, 2), seed=14, profiles=True)
+    r = abi.rect((0, 0, 0), (3, 2, 1))
+    path = restart.tile_filename(str(tmp_path), r)
+    names = restart.IO_FIELDS + restart.PROFILE_FIELDS
+    w = h5_v2.tile_file(path, f, r, names, crt_order=True)
+    for k in range(9):
+        w.attribute(f"extra{k}", h5_v2.string_type(8), [], f"value{k}".encode().ljust(8, b"\0"))
+    w.write(path, dense=True, dense_attrs=True)
+    s = C.create_string_buffer(16)
+    for k in range(9):
+        abi.check(lib, lib.htr_h5_string_attribute(path.encode(), None, f"extra{k}".encode(), 0, s, 16))
+        assert s.value == f"value{k}".encode()
+    abi.check(lib, lib.htr_h5_string_attribute(path.encode(), None, b"note", 0, s, 16))
+    assert s.value == b"latest"
+    g = fluid.Fluid(f.shape, f.nspec)
+    gv = g.view()
+    st = lib.htr_restart_read_tile(str(tmp_path).encode(), C.byref(gv), r, 5,
+                                   abi.HTR_RESTART_HOST_VIEW | abi.HTR_RESTART_PROFILES, None)
+    assert st == abi.HTR_OK, lib.htr_last_error()
+    for n in names:
+        assert np.array_equal(g[n], f[n]), n
