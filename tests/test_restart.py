@@ -532,3 +532,51 @@ def test_reader_takes_dense_attributes(tmp_path):
     assert st == abi.HTR_OK, lib.htr_last_error()
     for n in names:
         assert np.array_equal(g[n], f[n]), n
+
+
+# ---------------------------------------------------------------- golden files
+
+GOLDEN = os.path.join(os.path.dirname(os.path.abspath(__file__)), "golden")
+
+
+def _golden_maker():
+    import importlib.util
+    spec = importlib.util.spec_from_file_location("make_restart_golden",
+                                                  os.path.join(GOLDEN, "make_restart_golden.py"))
+    mod = importlib.util.module_from_spec(spec)
+    spec.loader.exec_module(mod)
+    return mod
+
+
+def test_oracle_reads_the_golden_restart():
+    """The committed restart (tests/golden/restart) holds the seeded fields
+    and the master attributes, read by the oracle alone."""
+    mk = _golden_maker()
+    f = mk.fields()
+    d = os.path.join(GOLDEN, "restart")
+    m = h5read.File(os.path.join(d, "master.hdf"))
+    assert int(m.attrs["timeStep"]) == 1234 and float(m.attrs["simTime"]) == 0.5
+    assert list(m.attrs["SpeciesNames"]) == [s.encode() for s in mk.SPECIES]
+    parts, _ = m.datasets["partitions"]
+    assert parts.shape == (1, 1, 2)
+    for p in parts.ravel():
+        lo, hi = p["lo"], p["hi"]
+        name = f"{lo[0]},{lo[1]},{lo[2]}-{hi[0]},{hi[1]},{hi[2]}.hdf"
+        t = h5read.File(os.path.join(d, name))
+        for n in restart.IO_FIELDS:
+            want = f[n][lo[2]:hi[2] + 1, lo[1]:hi[1] + 1, lo[0]:hi[0] + 1]
+            assert np.array_equal(t.datasets[n][0], want), (name, n)
+
+
+@needs_lib
+def test_writer_reproduces_the_golden_restart(tmp_path):
+    """The writer's bytes are stable: rewriting the golden restart gives the
+    committed files byte for byte (no time stamps or addresses that vary)."""
+    mk = _golden_maker()
+    out = str(tmp_path / "r")
+    mk.write(out)
+    d = os.path.join(GOLDEN, "restart")
+    assert sorted(os.listdir(out)) == sorted(os.listdir(d))
+    for name in os.listdir(d):
+        with open(os.path.join(d, name), "rb") as a, open(os.path.join(out, name), "rb") as b:
+            assert a.read() == b.read(), name
