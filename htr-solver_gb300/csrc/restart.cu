@@ -29,6 +29,10 @@ using htr::h5::Status;
 using htr::h5::Type;
 using htr::h5::Value;
 
+// field data go to and from the files as the host holds them: the files
+// store little-endian doubles and int64 rectangles
+static_assert(__BYTE_ORDER__ == __ORDER_LITTLE_ENDIAN__, "restart files need a little-endian host");
+
 constexpr size_t kSlabBytes = size_t(64) << 20;
 constexpr int kThreads = 256;
 
