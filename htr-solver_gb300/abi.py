@@ -171,7 +171,12 @@ PROTOTYPES = {
     "htr_InitializeTemporaries": [_V, _R, _M, _S],
     "htr_InitializeTimeDerivatives": [_V, _R, C.c_int, _M, _S],
     "htr_UpdateVars": [_V, _R, C.c_int, C.c_double, C.c_int, _M, _S],
+    "htr_decision_counters": [C.c_int, _P(C.c_ulonglong)],
 }
+HTR_DECISION_COUNTERS = 7
+# order of the counts of htr_decision_counters
+DECISION_COUNTERS = ("teno_filtered", "teno_exact", "sensor_filtered", "sensor_exact", "cut_filtered",
+                     "cut_exact", "limiter_blend")
 for _d in "XYZ":
     for _s in ("Hybrid", "TENO", "TENOA", "TENOLAD"):
         PROTOTYPES[f"htr_UpdateUsing{_s}EulerFlux{_d}"] = [_V, _R, _R, _D2, C.c_double, _M, _S]

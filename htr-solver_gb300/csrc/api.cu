@@ -137,25 +137,32 @@ int neq_of(htr_mixture_t m) { return m->eos == HTR_EOS_AIRMIX ? 9 : 5; }
 int nspec_of(htr_mixture_t m) { return m->eos == HTR_EOS_AIRMIX ? 5 : 1; }
 
 
-// Fixed device scratch of htr_rk3_step_static: module-scope, allocated once
-// when the module loads; its address is looked up once per device.
+// Fixed device scratch of htr_rk3_step_static: module-scope, reserved on a
+// device when this translation unit's module loads there.  The module has no
+// kernels, so under CUDA's lazy module loading it loads at the first lookup
+// of the array's address; htr_load_mixture does that lookup (set-up time)
+// and refreshes the cached address of the current device, so the step
+// itself neither loads a module nor reserves memory.  A step on a device
+// where no mixture was loaded does the lookup on its first call.
 constexpr size_t kStaticScratchBytes = size_t(32) << 20;
 static __device__ __align__(256) unsigned char g_static_scratch[kStaticScratchBytes];
 std::mutex g_static_scratch_mu;
 constexpr int kMaxDevices = 64;
 void *g_static_scratch_ptr[kMaxDevices] = {};
 
-int static_scratch(void **out) {
+// refresh = true: look the address up again (after a cudaDeviceReset the
+// module, and the array with it, is loaded anew)
+int static_scratch(void **out, bool refresh = false) {
   int dev = 0;
   if (int st = cuda_status(cudaGetDevice(&dev), "cudaGetDevice")) return st;
   if (dev < 0 || dev >= kMaxDevices) return fail(HTR_ERR_UNSUPPORTED, "device ordinal out of range%s");
   std::lock_guard<std::mutex> lock(g_static_scratch_mu);
-  if (g_static_scratch_ptr[dev] == nullptr) {
+  if (refresh || g_static_scratch_ptr[dev] == nullptr) {
     void *p = nullptr;
     if (int st = cuda_status(cudaGetSymbolAddress(&p, g_static_scratch), "scratch symbol")) return st;
     g_static_scratch_ptr[dev] = p;
   }
-  *out = g_static_scratch_ptr[dev];
+  if (out) *out = g_static_scratch_ptr[dev];
   return HTR_OK;
 }
 
@@ -205,6 +212,8 @@ extern "C" int htr_CalculateMaxSpectralRadius(const htr_fluid_view *, htr_rect3,
 namespace {
 
 // Step size, sensors (once per step) and Conserved_old (src/prometeo.rg:1342-1380).
+// dt, sensors and (unless the step starts with implicit chemistry, which
+// moves it after the chemistry solve) InitializeTemporaries of one step.
 int step_prologue(const htr_fluid_view *v, htr_rect3 inner, htr_rect3 fb, const htr_step_params *p,
                   htr_mixture_t m, double *dt_out, htr_stream_t s, unsigned sensor_dirs = 7u) {
   if (p == nullptr) return fail(HTR_ERR_ARGUMENT, "null step parameters%s");
@@ -237,6 +246,24 @@ int step_prologue(const htr_fluid_view *v, htr_rect3 inner, htr_rect3 fb, const 
                           "shock sensors")))
       return st;
   }
+  if (p->implicitChemistry) return check_field(v->Conserved_t_old, 8, "Conserved_t_old");
+  return htr_InitializeTemporaries(v, fb, m, s);
+}
+
+// The implicit chemistry block at the start of a step (src/prometeo.rg:1360-1398)
+// after the transport RHS of the start state is in Conserved_t: UpdateChemistry
+// over dt, then UpdatePrimitivesAndBCsFromConserved (primitives of the
+// interior, properties everywhere) and InitializeTemporaries.
+int implicit_chemistry_block(const htr_fluid_view *v, htr_rect3 inner, htr_rect3 fb, htr_mixture_t m, double dt,
+                             int *status_dev, htr_stream_t s) {
+  const cudaStream_t cs = (cudaStream_t)s;
+  int st;
+  if ((st = htr_UpdateChemistry(v, inner, dt, m, status_dev, s))) return st;
+  if ((st = with_mix(m, [&](const auto &mix) {
+         return cuda_status(htr::launch_primitive(*v, inner, mix, status_dev, cs), "primitive");
+       })))
+    return st;
+  if ((st = htr_UpdatePropertiesFromPrimitive(v, fb, m, s))) return st;
   return htr_InitializeTemporaries(v, fb, m, s);
 }
 
@@ -258,6 +285,17 @@ int fused_step(const htr_fluid_view *v, htr_rect3 inner, htr_rect3 fb, const htr
   if (int st = cuda_status(cudaMemsetAsync(w.tcache, 0, sizeof(double) * 3 * ncells_of(inner), (cudaStream_t)s),
                            "cache reset"))
     return st;
+  if (p->implicitChemistry) {
+    // transport RHS of the start state, then the chemistry solve
+    sp.mode = htr::kStageRhsOnly;
+    sp.stage = 1;
+    if (int st = with_mix(m, [&](const auto &mix) {
+          return cuda_status(htr::launch_stage(*v, inner, fb, mix, w, sp, status_dev, (cudaStream_t)s), "stage");
+        }))
+      return st;
+    if (int st = implicit_chemistry_block(v, inner, fb, m, dt, status_dev, s)) return st;
+    sp.mode = htr::kStageImplicit;
+  }
   for (int stage = 1; stage <= 3; stage++) {
     sp.stage = stage;
     if (int st = with_mix(m, [&](const auto &mix) {
@@ -293,6 +331,8 @@ int htr_load_mixture(int eos, const void *mix, size_t bytes, htr_mixture_t *out)
   if (e != cudaSuccess) return fail(HTR_ERR_NO_DEVICE, "cudaGetDeviceProperties: %s", cudaGetErrorString(e));
   if (prop.major != 10 || prop.minor != 3)
     return fail(HTR_ERR_NO_DEVICE, "this build targets sm_103 (GB300); device is %s", prop.name);
+  // set-up of htr_rk3_step_static on this device (loads its module)
+  if (int st = static_scratch(nullptr, true)) return st;
   htr_mixture_s *m = new (std::nothrow) htr_mixture_s();
   if (m == nullptr) return fail(HTR_ERR_ARGUMENT, "out of host memory%s");
   m->eos = eos;
@@ -626,6 +666,18 @@ int htr_UpdateNSCBCGhostCellTimeDerivatives(const htr_fluid_view *v, htr_rect3 b
   return cuda_status(htr::launch_nscbc_time_derivatives(*v, bc, dt, (cudaStream_t)s), "nscbc time derivatives");
 }
 
+int htr_decision_counters(int enable, unsigned long long counts[HTR_DECISION_COUNTERS]) {
+  if (counts == nullptr) return fail(HTR_ERR_ARGUMENT, "null counts%s");
+  for (int k = 0; k < HTR_DECISION_COUNTERS; k++) counts[k] = 0ull;
+  int st;
+  if ((st = cuda_status(cudaDeviceSynchronize(), "decision counters sync"))) return st;
+  if ((st = cuda_status(htr::decision_counters_euler(enable, counts), "decision counters")) ||
+      (st = cuda_status(htr::decision_counters_stage_euler(enable, counts), "decision counters")) ||
+      (st = cuda_status(htr::decision_counters_sensor(enable, counts), "decision counters")))
+    return st;
+  return HTR_OK;
+}
+
 int htr_rk3_set_tuning(const htr_stage_tuning *t) {
   if (t == nullptr) return fail(HTR_ERR_ARGUMENT, "null tuning%s");
   auto pow2_in = [](int v, int lo, int hi) { return v >= lo && v <= hi && (v & (v - 1)) == 0; };
@@ -711,26 +763,41 @@ int htr_rk3_step(const htr_fluid_view *v, htr_rect3 inner, htr_rect3 fb, const h
   int st;
   if ((st = step_prologue(v, inner, fb, p, m, &dt, s))) return st;
   if (dt_used) *dt_used = dt;
-  for (int stage = 1; stage <= 3; stage++) {
-    const double rk[2] = {RK[stage - 1][0], RK[stage - 1][1]};
-    const double sdt = dt * RK[stage - 1][2];
-    if ((st = htr_InitializeTimeDerivatives(v, fb, 0, m, s))) return st;
-    if (p->explicitChemistry)
-      if ((st = htr_AddChemistrySources(v, inner, m, s))) return st;
+  const int implicit = p->implicitChemistry ? 1 : 0;
+  // UpdateDerivatives (src/prometeo.rg:480-606) with the given limiter
+  // arguments: time derivatives from zero or from -Conserved_t_old,
+  // explicit chemistry sources, Euler Z, Y, X, diffusion Z, Y, X
+  auto derivatives = [&](const double rk[2], double sdt, int old) -> int {
+    int e;
+    if ((e = htr_InitializeTimeDerivatives(v, fb, old, m, s))) return e;
+    if (p->explicitChemistry && !implicit)
+      if ((e = htr_AddChemistrySources(v, inner, m, s))) return e;
     for (int d = 2; d >= 0; d--) {
       if (p->scheme == HTR_SCHEME_SKEW)
-        st = euler(v, inner, fb, nullptr, 0.0, m, d, 1, 0, s);
+        e = euler(v, inner, fb, nullptr, 0.0, m, d, 1, 0, s);
       else if (p->scheme == HTR_SCHEME_HYBRID)
-        st = euler(v, inner, fb, rk, sdt, m, d, 0, 0, s);
+        e = euler(v, inner, fb, rk, sdt, m, d, 0, 0, s);
       else
-        st = euler(v, inner, fb, rk, sdt, m, d, 2, p->scheme - 1, s);
-      if (st) return st;
+        e = euler(v, inner, fb, rk, sdt, m, d, 2, p->scheme - 1, s);
+      if (e) return e;
     }
     for (int d = 2; d >= 0; d--)
-      if ((st = diffusion(v, inner, fb, m, d, s))) return st;
+      if ((e = diffusion(v, inner, fb, m, d, s))) return e;
+    return (int)HTR_OK;
+  };
+  if (implicit) {
+    const double rk0[2] = {0.0, 1.0};
+    if ((st = derivatives(rk0, dt * 0.5, 0))) return st;
+    if ((st = implicit_chemistry_block(v, inner, fb, m, dt, status_dev, s))) return st;
+  }
+  for (int stage = 1; stage <= 3; stage++) {
+    const double rk[2] = {RK[stage - 1][0], RK[stage - 1][1]};
+    double sdt = dt * RK[stage - 1][2];
+    if (implicit) sdt *= 0.5;
+    if ((st = derivatives(rk, sdt, implicit))) return st;
     // ghost cells keep their imposed state (the reference restores them
     // from their primitives after the update)
-    if ((st = htr_UpdateVars(v, inner, stage, dt, 0, m, s))) return st;
+    if ((st = htr_UpdateVars(v, inner, stage, dt, implicit, m, s))) return st;
     if ((st = check_common(v, m, inner))) return st;
     if ((st = with_mix(m, [&](const auto &mix) {
            return cuda_status(htr::launch_primitive(*v, inner, mix, status_dev, cs), "primitive");
@@ -809,6 +876,8 @@ int htr_rk3_step_bc_ws(const htr_fluid_view *v, htr_rect3 inner, htr_rect3 fb, c
   if ((st = check_step_fields(v, m))) return st;
   if (p == nullptr) return fail(HTR_ERR_ARGUMENT, "null step parameters%s");
   if (p->scheme < HTR_SCHEME_HYBRID || p->scheme > HTR_SCHEME_SKEW) return fail(HTR_ERR_ARGUMENT, "unknown scheme%s");
+  if (p->implicitChemistry)
+    return fail(HTR_ERR_UNSUPPORTED, "implicit chemistry is not supported by the boundary step%s");
   if ((st = check_bc_params(v, inner, fb, bc))) return st;
   const bool hybrid = p->scheme == HTR_SCHEME_HYBRID;
   if (hybrid) {

@@ -219,4 +219,7 @@ template cudaError_t launch_euler<ConstPropDev>(const htr_fluid_view &, const ht
 template cudaError_t launch_euler<AirDev>(const htr_fluid_view &, const htr_rect3 &, const htr_rect3 &,
                                           const double *, double, const AirDev &, int, int, int, cudaStream_t);
 
+// decision counters of this translation unit (htr_decision_counters)
+HTR_DECISION_COUNTERS_ACCESS(decision_counters_euler)
+
 }  // namespace htr

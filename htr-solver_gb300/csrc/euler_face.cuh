@@ -425,6 +425,7 @@ template <class Mix, int D> struct EulerFace {
           limit = true;
       }
       if (limit) {
+        count_decision(kLimiterBlend);
         const double eps = 1e-60;
         double theta = 1.0;
         double Fl[NE];

@@ -75,4 +75,10 @@ cudaError_t launch_init_rhs(const htr_fluid_view &v, const htr_rect3 &my, int ne
 cudaError_t launch_rk_update(const htr_fluid_view &v, const htr_rect3 &my, int neq, int stage,
                              double dt, int implicit, cudaStream_t s);
 
+// decision counters of the translation units that take filtered decisions
+// (stencil.cuh): add this unit's counts to out[], clear them, set counting
+cudaError_t decision_counters_euler(int enable, unsigned long long *out);
+cudaError_t decision_counters_stage_euler(int enable, unsigned long long *out);
+cudaError_t decision_counters_sensor(int enable, unsigned long long *out);
+
 }  // namespace htr

@@ -144,4 +144,7 @@ cudaError_t launch_shock_sensor(const htr_fluid_view &v, const htr_rect3 &my, co
   return cudaGetLastError();
 }
 
+// decision counters of this translation unit (htr_decision_counters)
+HTR_DECISION_COUNTERS_ACCESS(decision_counters_sensor)
+
 }  // namespace htr

@@ -65,12 +65,22 @@ constexpr int kPrepVals = 11;
 size_t stage_workspace_bytes(const htr_rect3 &interior, int neq);
 bool stage_workspace_carve(void *base, size_t bytes, const htr_rect3 &interior, int neq, StageWorkspace &w);
 
+// What one launch_stage computes.
+enum StageMode {
+  kStageExplicit = 0,  // RHS from zero (+ chemistry sources), RK update, refresh
+  kStageImplicit = 1,  // implicit chemistry: RHS from -Conserved_t_old, no sources,
+                       // RK update with dt/2 (src/prometeo_rk.rg:59-112), refresh
+  kStageRhsOnly = 2    // transport RHS of the current state into Conserved_t only
+                       // (RK_coeffs {0, 1}, limiter deltaTime dt/2, src/prometeo.rg:1363-1376)
+};
+
 struct StageParams {
   int scheme;  // 0 hybrid, 1 skew, 2 TENO-only
   int kind;    // TENO flavour for scheme 2
   int chemistry;
   int stage;   // 1..3
   double dt;   // full step size
+  int mode = kStageExplicit;
   // bit D set: direction D has more than one cell.  A one-cell periodic
   // direction contributes exactly zero to every flux difference (both faces
   // see the same cell), so its faces are not computed.

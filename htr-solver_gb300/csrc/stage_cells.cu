@@ -236,7 +236,7 @@ __global__ void __launch_bounds__(128) diffusion_faces(const DiffFaceArgs A, con
 
 // ---------------------------------------------------------------------------
 struct UpdateArgs {
-  Fd<double> C, Cold, Ct, rho, P, T, X, Y, u, mu, lam, Di, SoS, me[3], md[3];
+  Fd<double> C, Cold, Ct, Ctold, rho, P, T, X, Y, u, mu, lam, Di, SoS, me[3], md[3];
   Fd<int> nt[3];
   unsigned active;
   Dense dn;
@@ -244,6 +244,7 @@ struct UpdateArgs {
   const double *fe[3], *fd[3];
   double c1, c2, c3, dt;
   int chemistry;
+  int mode;        // StageMode
   int *status;
   double *tcache;  // [3][ncell]: T, log(T TRef), 1/(T TRef) of the last refresh
   // boundary step only
@@ -459,8 +460,15 @@ __global__ void __launch_bounds__(128) stage_update(const UpdateArgs A, const __
     long long p[3];
     A.dn.point(i, p);
     double ct[NE];
+    if (A.mode == kStageImplicit) {
+      // InitializeTimeDerivatives of implicit chemistry (src/prometeo_rk.rg:59-70)
+      const double *o = A.Ctold.at(p);
 #pragma unroll
-    for (int k = 0; k < NE; k++) ct[k] = 0.0;
+      for (int k = 0; k < NE; k++) ct[k] = -ld(&o[k]);
+    } else {
+#pragma unroll
+      for (int k = 0; k < NE; k++) ct[k] = 0.0;
+    }
     unsigned div = A.active;  // directions whose flux divergence applies here
     bool bnd = false;         // on an NSCBC plane
     int inflow_side = -1;
@@ -489,7 +497,7 @@ __global__ void __launch_bounds__(128) stage_update(const UpdateArgs A, const __
     if (skip) {
       double *ctp = A.Ct.at(p);
 #pragma unroll
-      for (int k = 0; k < NE; k++) ctp[k] = 0.0;
+      for (int k = 0; k < NE; k++) ctp[k] = A.mode == kStageImplicit ? ct[k] : 0.0;
       continue;
     }
     // T, 1/T and log T of the current state: from the previous stage's
@@ -548,10 +556,15 @@ __global__ void __launch_bounds__(128) stage_update(const UpdateArgs A, const __
         }
       }
     }
+    double *ctp = A.Ct.at(p);
+    if (A.mode == kStageRhsOnly) {
+#pragma unroll
+      for (int k = 0; k < NE; k++) ctp[k] = ct[k];
+      continue;
+    }
     // SSP-RK3 update (prometeo_rk.rg:88-112)
     double *cons = A.C.at(p);
     const double *old = A.Cold.at(p);
-    double *ctp = A.Ct.at(p);
     double u_[NE];
 #pragma unroll
     for (int k = 0; k < NE; k++) {
@@ -674,7 +687,17 @@ cudaError_t launch_stage(const htr_fluid_view &v, const htr_rect3 &my, const htr
   H.s1 = sizeof(double) * dn.n[0];
   H.s2 = sizeof(double) * dn.n[0] * dn.n[1];
   H.b -= (dn.lo[0] * H.s0 + dn.lo[1] * H.s1 + dn.lo[2] * H.s2);
-  if ((e = launch_stage_euler(v, my, fb, mix, w, H, sp, c1, c2, sp.dt * c3, s, ev ? ev + 1 + kKgZ : nullptr)) !=
+  // RK_coeffs and deltaTime of the Euler limiter: the stage's; halved with
+  // implicit chemistry; {0, 1} and dt/2 for the RHS of the implicit pre-step
+  // (src/prometeo.rg:1363-1376, :1406-1419, UpdateDerivatives :498-512)
+  double rk0 = c1, rk1 = c2, sdt = sp.dt * c3;
+  if (sp.mode == kStageImplicit) sdt = (sp.dt * c3) * 0.5;
+  if (sp.mode == kStageRhsOnly) {
+    rk0 = 0.0;
+    rk1 = 1.0;
+    sdt = sp.dt * 0.5;
+  }
+  if ((e = launch_stage_euler(v, my, fb, mix, w, H, sp, rk0, rk1, sdt, s, ev ? ev + 1 + kKgZ : nullptr)) !=
       cudaSuccess)
     return e;
   const htr_field *ms[3] = {&v.dcsi_s, &v.deta_s, &v.dzet_s};
@@ -712,6 +735,7 @@ cudaError_t launch_stage(const htr_fluid_view &v, const htr_rect3 &my, const htr
   U.C = fd<double>(v.Conserved);
   U.Cold = fd<double>(v.Conserved_old);
   U.Ct = fd<double>(v.Conserved_t);
+  U.Ctold = fd<double>(v.Conserved_t_old);
   U.rho = fd<double>(v.rho);
   U.P = fd<double>(v.pressure);
   U.T = fd<double>(v.temperature);
@@ -741,8 +765,10 @@ cudaError_t launch_stage(const htr_fluid_view &v, const htr_rect3 &my, const htr
   U.c1 = c1;
   U.c2 = c2;
   U.c3 = c3;
-  U.dt = sp.dt;
-  U.chemistry = sp.chemistry;
+  // UpdateVars halves the step with implicit chemistry (src/prometeo_rk.rg:95-97)
+  U.dt = sp.mode == kStageImplicit ? sp.dt * 0.5 : sp.dt;
+  U.chemistry = sp.mode == kStageExplicit ? sp.chemistry : 0;
+  U.mode = sp.mode;
   U.status = status;
   U.tcache = w.tcache;
   U.Xp = fd<double>(v.MolarFracs_profile);

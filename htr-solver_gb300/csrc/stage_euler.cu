@@ -202,4 +202,7 @@ template cudaError_t launch_stage_euler<AirDev>(const htr_fluid_view &, const ht
                                                 const StageParams &, double, double, double, cudaStream_t,
                                                 cudaEvent_t *);
 
+// decision counters of this translation unit (htr_decision_counters)
+HTR_DECISION_COUNTERS_ACCESS(decision_counters_stage_euler)
+
 }  // namespace htr

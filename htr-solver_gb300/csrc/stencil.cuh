@@ -15,6 +15,42 @@
 
 namespace htr {
 
+// ---------------------------------------------------------------------------
+// Decision counters (diagnostic, off unless htr_decision_counters enables
+// them): how many selections the single-precision filters decided and how
+// many went to the exact double-precision path, and how many faces the
+// positivity limiter blended.  Every translation unit is its own module, so
+// each holds its own copy; HTR_DECISION_COUNTERS_ACCESS(name) defines the
+// host function through which htr_decision_counters reads, clears and
+// switches the copy of one translation unit.
+// ---------------------------------------------------------------------------
+enum DecisionCounter {
+  kTenoFiltered = 0,  // TENO / TENO-A / TENO-LAD stencil selection taken by fast_mask
+  kTenoExact,         // ... by the exact FP64 expression
+  kSensorFiltered,    // shock-sensor node decided by an FP32 filter
+  kSensorExact,       // ... by the exact FP64 expression
+  kCutFiltered,       // sensor cut-off exponent taken from the FP32 argument
+  kCutExact,          // ... from the exact FP64 argument
+  kLimiterBlend,      // multi-species TENO face blended with the first-order flux
+  kDecisionCounters
+};
+static_assert(kDecisionCounters == HTR_DECISION_COUNTERS, "counter count of the C ABI");
+static __device__ unsigned long long g_decisions[kDecisionCounters];
+static __device__ int g_count_decisions;
+HTR_D void count_decision(int k) {
+  if (g_count_decisions) atomicAdd(&g_decisions[k], 1ull);
+}
+#define HTR_DECISION_COUNTERS_ACCESS(NAME)                                                              \
+  cudaError_t NAME(int enable, unsigned long long *out) {                                             \
+    unsigned long long c[kDecisionCounters];                                                          \
+    cudaError_t e = cudaMemcpyFromSymbol(c, g_decisions, sizeof(c));                                  \
+    if (e != cudaSuccess) return e;                                                                   \
+    for (int k = 0; k < kDecisionCounters; k++) out[k] += c[k];                                       \
+    for (int k = 0; k < kDecisionCounters; k++) c[k] = 0ull;                                          \
+    if ((e = cudaMemcpyToSymbol(g_decisions, c, sizeof(c))) != cudaSuccess) return e;                 \
+    return cudaMemcpyToSymbol(g_count_decisions, &enable, sizeof(int));                               \
+  }
+
 enum NodeType { Std = 0, L_S, Lp1_S, Lp2_S, Rm3_S, Rm2_S, Rm1_S, R_S, L_C, Lp1_C, Rm2_C, Rm1_C, R_C };
 
 // Boundary (ghost) nodes: their state is imposed by the boundary condition,
@@ -303,11 +339,13 @@ HTR_D double teno(double ym2, double ym1, double y, double yp1, double yp2, doub
   }
   int b1, b2, b3, b4;
   if (fmask >= 0) {
+    count_decision(kTenoFiltered);
     b1 = fmask & 1;
     b2 = (fmask >> 1) & 1;
     b3 = (fmask >> 2) & 1;
     b4 = (fmask >> 3) & 1;
   } else {
+  count_decision(kTenoExact);
   const double chi1 = s.tau6 / (s.s1 + eps);
   const double chi2 = s.tau6 / (s.s2 + eps);
   const double chi3 = s.tau6 / (s.s3 + eps);
@@ -537,8 +575,12 @@ HTR_D double sensor_cut_fast(double Phi) {
     const float d = __fmul_rn(w12, __fadd_rn(1.0f, __fmul_rn(12.0f, P)));
     const float z = __fsub_rn(12.5f, __fmul_rn(11.5f, __fsub_rn(1.0f, d)));
     const float fl = floorf(z), fr = z - fl;
-    if (fr > 1e-3f && fr < 1.0f - 1e-3f) return double(kP10[min(max(int(fl), 0), 13)]);
+    if (fr > 1e-3f && fr < 1.0f - 1e-3f) {
+      count_decision(kCutFiltered);
+      return double(kP10[min(max(int(fl), 0), 13)]);
+    }
   }
+  count_decision(kCutExact);
   return sensor_cut(Phi);
 }
 
@@ -557,13 +599,20 @@ HTR_D bool teno_a_sensor(double ym2, double ym1, double y, double yp1, double yp
     return ((1.0 - smin(1.0, Ren_irc * eta)) < 0.5);
   }
   const int pre = sensor_prefilter(ym2, ym1, y, yp1, yp2, yp3, cut);
-  if (pre >= 0) return pre == 1;
+  if (pre >= 0) {
+    count_decision(kSensorFiltered);
+    return pre == 1;
+  }
   const Smooth s = smoothness(ym2, ym1, y, yp1, yp2, yp3);
   const double eps = 1e-8;
   // strict comparison a_k*a > cut: the filter's flag "q >= cut(1+1e-4)"
   // implies it, "q <= cut(1-1e-4)" refutes it
   const int fm = fast_mask(fast_x(s, eps), 15u, cut);
-  if (fm >= 0) return fm == 15;
+  if (fm >= 0) {
+    count_decision(kSensorFiltered);
+    return fm == 15;
+  }
+  count_decision(kSensorExact);
   const double a1 = pow6_exact(1 + s.tau6 / (s.s1 + eps));
   const double a2 = pow6_exact(1 + s.tau6 / (s.s2 + eps));
   const double a3 = pow6_exact(1 + s.tau6 / (s.s3 + eps));

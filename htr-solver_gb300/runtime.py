@@ -19,7 +19,7 @@ _lib = None
 
 class htr_step_params(C.Structure):
     _fields_ = [("scheme", C.c_int), ("vorticityScale", C.c_double), ("cfl", C.c_double),
-                ("deltaTime", C.c_double), ("explicitChemistry", C.c_int)]
+                ("deltaTime", C.c_double), ("explicitChemistry", C.c_int), ("implicitChemistry", C.c_int)]
 
 
 SCHEMES = {"Hybrid": 0, "TENO": 1, "TENOA": 2, "TENOLAD": 3, "SkewSymmetric": 4}
@@ -114,14 +114,16 @@ def workspace_bytes(fluid, mixh, interior=None):
 
 def rk3_step(fluid, mixh, scheme="Hybrid", vorticity_scale=1.0, cfl=0.0, dt=0.0,
              chemistry=True, stream=None, interior=None, status_dev=None, fused=True,
-             workspace=None):
+             workspace=None, implicit=False):
     """One SSP-RK3 step of a device grid; returns the dt used.
 
     fused=True runs htr_rk3_step_ws (fused stage pipeline, periodic grids) on
     `workspace` (a Workspace, default: one cached per process); fused=False
-    runs htr_rk3_step, the composition of the per-task entry points."""
+    runs htr_rk3_step, the composition of the per-task entry points.
+    implicit=True advances the chemistry with the implicit solver
+    (Integrator.implicitChemistry) instead of explicit sources."""
     l = lib()
-    p = htr_step_params(SCHEMES[scheme], vorticity_scale, cfl, dt, 1 if chemistry else 0)
+    p = htr_step_params(SCHEMES[scheme], vorticity_scale, cfl, dt, 1 if chemistry else 0, 1 if implicit else 0)
     v = fluid.view()
     used = C.c_double(0.0)
     inner = fluid.interior() if interior is None else interior

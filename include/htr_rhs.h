@@ -319,6 +319,16 @@ typedef struct {
   double cfl;               /* > 0: CFL-based step size */
   double deltaTime;         /* used when cfl <= 0 */
   int explicitChemistry;    /* add chemistry sources to the RHS */
+  /* Integrator.implicitChemistry (src/prometeo.rg:1360-1398): chemistry is
+   * advanced by the implicit Rosenbrock solver instead of explicit sources.
+   * After the sensors: the transport RHS of the step's start state
+   * (RK_coeffs {0, 1}, deltaTime dt/2), UpdateChemistry over dt with that
+   * RHS frozen, primitive and property refresh, then the three RK stages with
+   * Conserved_t starting from -Conserved_t_old and dt halved
+   * (src/prometeo_rk.rg:59-112).  explicitChemistry is ignored when set.
+   * Supported by htr_rk3_step, htr_rk3_step_ws and htr_rk3_step_static;
+   * htr_rk3_step_bc_ws returns HTR_ERR_UNSUPPORTED. */
+  int implicitChemistry;
 } htr_step_params;
 
 int htr_rk3_step(const htr_fluid_view *view, htr_rect3 interior, htr_rect3 fluid_bounds,
@@ -387,12 +397,17 @@ int htr_rk3_step_bc_ws(const htr_fluid_view *view, htr_rect3 interior, htr_rect3
 
 /* No counterpart in the reference.  The fused step of htr_rk3_step_ws on a
  * fixed scratch that the library owns: a module-scope device array of
- * htr_rk3_static_scratch_bytes() bytes, reserved when the library's module
- * loads, whose address is resolved once per device.  The call allocates no
- * device or host memory.  Grids whose workspace (htr_rk3_workspace_bytes)
- * exceeds the scratch are rejected with HTR_ERR_UNSUPPORTED before any
- * launch.  Calls share the scratch of their device: run them on one stream
- * (or serialise them), never concurrently. */
+ * htr_rk3_static_scratch_bytes() bytes, reserved on a device when the
+ * module holding it loads there and kept until the process exits.
+ * htr_load_mixture loads that module and resolves the array's address for
+ * its current device, so once a mixture was loaded on the device the call
+ * allocates no device or host memory and loads nothing; on a device where
+ * no mixture was loaded, the first call does that set-up (make it before
+ * any stream capture).  After a cudaDeviceReset, load the mixture again.
+ * Grids whose workspace (htr_rk3_workspace_bytes) exceeds the scratch are
+ * rejected with HTR_ERR_UNSUPPORTED before any launch.  Calls share the
+ * scratch of their device: run them on one stream (or serialise them),
+ * never concurrently. */
 int htr_rk3_step_static(const htr_fluid_view *view, htr_rect3 interior, htr_rect3 fluid_bounds,
                         const htr_step_params *params, htr_mixture_t mix, double *dt_used,
                         int *status_dev, htr_stream_t stream);
@@ -418,6 +433,20 @@ int htr_rk3_get_tuning(htr_stage_tuning *tuning);
 int htr_rk3_stage_profile(const htr_fluid_view *view, htr_rect3 interior, htr_rect3 fluid_bounds,
                           const htr_step_params *params, htr_mixture_t mix, void *workspace,
                           size_t workspace_bytes, float *ms_out, htr_stream_t stream);
+
+/* Diagnostic counters, no counterpart in the reference.  The kernels decide
+ * TENO stencil selections and shock sensors first with single-precision
+ * filters and fall back to the exact double-precision expression of the
+ * reference when a value lies within the filter's safety margin; the
+ * multi-species TENO flux may blend with the first-order flux (positivity
+ * limiter).  htr_decision_counters waits for the device, adds the counts
+ * gathered since the previous call to counts[0..6] (TENO selections filtered,
+ * TENO selections exact, sensor nodes filtered, sensor nodes exact, sensor
+ * cut-offs filtered, sensor cut-offs exact, limiter blends), clears them and
+ * switches counting on (enable != 0) or off for later launches.  Counting
+ * costs an atomic per decision: it is off by default. */
+#define HTR_DECISION_COUNTERS 7
+int htr_decision_counters(int enable, unsigned long long counts[HTR_DECISION_COUNTERS]);
 
 #ifdef __cplusplus
 }

@@ -93,18 +93,30 @@ def spectral_dt(lib, fl, mixh, cfl):
     return cfl / r.value
 
 
-def update_derivatives(lib, fl, mixh, stage, dt, scheme="Hybrid", chemistry=True, bnum=(0, 0, 0)):
-    """One explicit RHS evaluation in the reference's order (prometeo.rg:480-606)."""
+def update_derivatives(lib, fl, mixh, stage, dt, scheme="Hybrid", chemistry=True, bnum=(0, 0, 0),
+                       old_derivatives=False, limiter=None):
+    """One RHS evaluation in the reference's order (UpdateDerivatives,
+    prometeo.rg:480-606).  old_derivatives: Conserved_t starts from
+    -Conserved_t_old and the limiter's deltaTime is halved (the RK stages of
+    implicit chemistry).  limiter = (RK_coeffs, deltaTime) overrides the
+    stage's limiter arguments (the implicit pre-step passes ({0, 1}, dt/2))."""
     A = _abi()
     v = fl.view()
     allr = fl.bounds()
     inner = fl.interior(bnum)
     fb = fl.bounds()
-    A.check(lib, lib.htr_InitializeTimeDerivatives(C.byref(v), allr, 0, mixh, None), "init_t")
+    A.check(lib, lib.htr_InitializeTimeDerivatives(C.byref(v), allr, 1 if old_derivatives else 0, mixh, None),
+            "init_t")
     if chemistry:
         A.check(lib, lib.htr_AddChemistrySources(C.byref(v), inner, mixh, None), "chem")
-    rk = (C.c_double * 2)(RK_C[stage - 1][0], RK_C[stage - 1][1])
-    ddt = dt * RK_C[stage - 1][2]
+    if limiter is not None:
+        rk = (C.c_double * 2)(*limiter[0])
+        ddt = limiter[1]
+    else:
+        rk = (C.c_double * 2)(RK_C[stage - 1][0], RK_C[stage - 1][1])
+        ddt = dt * RK_C[stage - 1][2]
+        if old_derivatives:
+            ddt *= 0.5
     for d in "ZYX":
         if scheme == "SkewSymmetric":
             fn = getattr(lib, f"htr_UpdateUsingSkewSymmetricEulerFlux{d}")
@@ -140,23 +152,37 @@ def refresh(lib, fl, mixh, bnum=(0, 0, 0)):
 
 
 def step(lib, fl, mixh, scheme="Hybrid", vorticity_scale=1.0, cfl=0.8, dt=None, chemistry=True,
-         stages=3, hook=None, bnum=(0, 0, 0)):
+         stages=3, hook=None, bnum=(0, 0, 0), implicit=False):
     """One SSP-RK3 time step; returns the dt used.  `bnum` ghost layers per
     side hold Dirichlet states: the RHS, the RK update and the primitive
     recovery run on the interior only (the reference restores ghost
-    conserved variables from their imposed primitives after each update)."""
+    conserved variables from their imposed primitives after each update).
+    implicit: Integrator.implicitChemistry (prometeo.rg:1360-1398): the
+    transport RHS of the start state (RK_coeffs {0, 1}, deltaTime dt/2),
+    UpdateChemistry over dt, the refresh, then the RK stages without
+    chemistry sources, from -Conserved_t_old and with dt halved
+    (prometeo_rk.rg:59-112)."""
     A = _abi()
     if dt is None:
         dt = spectral_dt(lib, fl, mixh, cfl)
     if scheme == "Hybrid":
         update_sensors(lib, fl, mixh, vorticity_scale)
     v = fl.view()
+    if implicit:
+        update_derivatives(lib, fl, mixh, 1, dt, scheme, False, bnum, limiter=((0.0, 1.0), dt * 0.5))
+        status = C.c_int(0)
+        A.check(lib, lib.htr_UpdateChemistry(C.byref(v), fl.interior(bnum), dt, mixh, C.byref(status), None),
+                "UpdateChemistry")
+        if status.value != 0:
+            raise A.HtrError(f"UpdateChemistry status {status.value}")
+        refresh(lib, fl, mixh, bnum)
     A.check(lib, lib.htr_InitializeTemporaries(C.byref(v), fl.bounds(), mixh, None), "tmp")
     for s in range(1, stages + 1):
-        update_derivatives(lib, fl, mixh, s, dt, scheme, chemistry, bnum)
+        update_derivatives(lib, fl, mixh, s, dt, scheme, chemistry and not implicit, bnum, old_derivatives=implicit)
         if hook is not None:
             hook(s, fl)
-        A.check(lib, lib.htr_UpdateVars(C.byref(v), fl.interior(bnum), s, dt, 0, mixh, None), "rk")
+        A.check(lib, lib.htr_UpdateVars(C.byref(v), fl.interior(bnum), s, dt, 1 if implicit else 0, mixh, None),
+                "rk")
         refresh(lib, fl, mixh, bnum)
     return dt
 

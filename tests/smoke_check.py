@@ -38,8 +38,7 @@ def run():
     out = dev.to_host()
     for d in "XYZ":
         assert np.array_equal(out[f"shockSensor{d}"], host[f"shockSensor{d}"]), d
-    err = util.rel_err(out["Conserved_t"], host["Conserved_t"]).max()
-    assert err <= util.RHS_REL_TOL, err
+    err = util.check(out["Conserved_t"], host["Conserved_t"], "Conserved_t")["ratio"]
 
     # boundary layer: the device metrics equal the port's; one fused step
     # equals the oracle's step within the RHS tolerance
@@ -62,9 +61,8 @@ def run():
                                (bc["xPos"][1]["LengthScale"], bc["yPos"][1]["LengthScale"]))
     wall.FusedBoundaryRun(dev, runtime.load_mixture(bl.meta["eos"], mb), bc).step(dt)
     torch.cuda.synchronize()
-    err2 = util.rel_err(dev.to_host()["Conserved"], bl["Conserved"]).max()
-    assert err2 <= util.RHS_REL_TOL, err2
-    print(f"smoke ok: max rel err {err:.3e} (hybrid RHS), {err2:.3e} (boundary-layer step)")
+    err2 = util.check(dev.to_host()["Conserved"], bl["Conserved"], "Conserved")["ratio"]
+    print(f"smoke ok: pointwise error / bound {err:.3e} (hybrid RHS), {err2:.3e} (boundary-layer step)")
 
 
 if __name__ == "__main__":

@@ -5,8 +5,9 @@ Bars (stated per check):
 * shock sensors (booleans) and the Ducros value: bit-exact;
 * Euler fluxes of the single-species gas: bit-exact (every operation on that
   path is correctly rounded on both sides, TENO powers included);
-* everything else: per-component max relative error <= 1e-11
-  (util.RHS_REL_TOL), the bar of the spec for the RHS after one RK3 step.
+* everything else: the pointwise bar of util.check, element by element
+  |gpu - cpu| <= max(1e-11 |cpu|, floor) (the reference's own regression
+  rule, solverTests/testAll.py:22-26, at a ten times tighter tolerance).
 """
 import ctypes as C
 
@@ -21,6 +22,9 @@ from tests import util
 pytestmark = pytest.mark.gpu
 
 CASES = {"tg": (16, 12, 10), "air": (12, 10, 8)}
+# state fields compared after a step
+STEP_FIELDS = ("Conserved", "temperature", "pressure", "Conserved_t", "MolarFracs", "velocity",
+               "rho", "mu", "lam", "Di", "SoS", "MassFracs")
 
 
 @pytest.fixture(scope="module")
@@ -72,10 +76,9 @@ def test_euler_flux(port, gpu, case, scheme, d):
     host, dev = _run_both(port, gpu, fl, h, gh, name, args)
     if kind == "tg":
         assert np.array_equal(dev["Conserved_t"], host["Conserved_t"]), \
-            f"max rel err {util.rel_err(dev['Conserved_t'], host['Conserved_t']).max()}"
+            util.pointwise(dev["Conserved_t"], host["Conserved_t"], "Conserved_t")[1]
     else:
-        err = util.rel_err(dev["Conserved_t"], host["Conserved_t"])
-        assert err.max() <= util.RHS_REL_TOL, err
+        util.check(dev["Conserved_t"], host["Conserved_t"], "Conserved_t")
 
 
 @pytest.mark.parametrize("d", "XYZ")
@@ -83,8 +86,7 @@ def test_diffusion_flux(port, gpu, case, d):
     kind, fl, h, gh = case
     name = f"htr_UpdateUsingDiffusionFlux{d}"
     host, dev = _run_both(port, gpu, fl, h, gh, name, lambda v, f, m, s: (v, f.interior(), f.bounds(), m, s))
-    err = util.rel_err(dev["Conserved_t"], host["Conserved_t"])
-    assert err.max() <= util.RHS_REL_TOL, err
+    util.check(dev["Conserved_t"], host["Conserved_t"], "Conserved_t")
 
 
 def test_sensors_bit_exact(port, gpu, case):
@@ -136,40 +138,100 @@ def test_sensors_bit_exact_large(port, gpu, kind, n, mach):
     for d in "XYZ":
         a, b = out[f"shockSensor{d}"], host[f"shockSensor{d}"]
         assert np.array_equal(a, b), f"{(a != b).sum()} of {a.size} sensor{d} flags differ"
-        assert 0 < b.sum() <= b.size
+        # both outcomes occur (these grids hold 12-50 % false flags)
+        assert 0 < b.sum() < b.size
 
 
 def test_chemistry_sources(port, gpu, case):
     kind, fl, h, gh = case
     host, dev = _run_both(port, gpu, fl, h, gh, "htr_AddChemistrySources",
                           lambda v, f, m, s: (v, f.interior(), m, s))
-    err = util.rel_err(dev["Conserved_t"], host["Conserved_t"])
-    assert err.max() <= util.RHS_REL_TOL, err
+    util.check(dev["Conserved_t"], host["Conserved_t"], "Conserved_t")
+
+
+@pytest.mark.parametrize("state,dt", [("dirichlet", 1e-7), ("air", 1e-6), ("air", 1e-4), ("air", 3e-3)])
+def test_update_chemistry_seeded(port, gpu, state, dt):
+    """Implicit Rosenbrock chemistry (UpdateChemistryTask, src/prometeo_chem.cc:31-68,
+    src/prometeo_chem.hpp:53-93, src/Utils/math_utils.hpp:196-441) with the
+    transport RHS of the state frozen in Conserved_t, over chemical steps
+    from non-stiff to stiff: on the air-box workload's state (T 300-8000 K,
+    p 0.1-10 bar, Dirichlet compositions) at the small step where the
+    reference's solver still converges everywhere, and on near-air
+    compositions (util.make_air_state) up to whole CFL steps.  Conserved,
+    Conserved_t_old and temperature meet the pointwise bar, status 0."""
+    import torch
+    if state == "dirichlet":
+        fl, h, m = util.make_state(port, "air", (12, 10, 8), seed=11)
+    else:
+        fl, h, m = util.make_air_state(port, (12, 10, 8), seed=12)
+    oracle.update_sensors(port, fl, h, 1.0)
+    fl["Conserved_old"] = fl["Conserved"]
+    oracle.update_derivatives(port, fl, h, 1, dt, chemistry=False)
+    gh = runtime.load_mixture(fl.meta["eos"], m)
+    host = fl.copy()
+    st = C.c_int(0)
+    vh = host.view()
+    util.call(port, "htr_UpdateChemistry", C.byref(vh), host.interior(), dt, h, C.byref(st), None)
+    assert st.value == 0 and np.all(np.isfinite(host["Conserved"]))
+    dev = fl.to_device("cuda")
+    sd = torch.zeros(1, dtype=torch.int32, device="cuda")
+    vd = dev.view()
+    util.call(gpu, "htr_UpdateChemistry", C.byref(vd), dev.interior(), dt, gh,
+              C.cast(C.c_void_p(sd.data_ptr()), C.POINTER(C.c_int)), runtime.stream_handle())
+    torch.cuda.synchronize()
+    assert sd.item() == 0
+    out = dev.to_host()
+    # the step changed the state (the comparison is not of an idle solve)
+    assert not np.array_equal(host["Conserved"], fl["Conserved"])
+    util.check_fields(out, host, ("Conserved", "Conserved_t_old", "temperature"))
+
+
+@pytest.mark.parametrize("fused", [False, True], ids=["tasks", "fused"])
+@pytest.mark.parametrize("scheme,cfl", [("Hybrid", 0.8), ("TENOLAD", 0.08)])
+def test_implicit_chemistry_step(port, gpu, scheme, cfl, fused):
+    """One SSP-RK3 step with Integrator.implicitChemistry (src/prometeo.rg:1360-1398,
+    src/prometeo_rk.rg:59-112) on near-air compositions at up to CFL 0.8, far
+    above the explicit chemical limit: the task composition (htr_rk3_step)
+    and the fused pipeline (htr_rk3_step_ws) against the oracle driver's
+    implicit branch on the port; every state field and Conserved_t_old meet
+    the pointwise bar, sensors bit for bit, status 0."""
+    import torch
+    host, h, m = util.make_air_state(port, (12, 10, 8), seed=5)
+    gh = runtime.load_mixture(host.meta["eos"], m)
+    dev = host.to_device("cuda")
+    dt = oracle.spectral_dt(port, host, h, cfl)
+    oracle.step(port, host, h, scheme=scheme, dt=dt, implicit=True)
+    assert np.all(np.isfinite(host["Conserved"]))
+    status = torch.zeros(1, dtype=torch.int32, device="cuda")
+    runtime.rk3_step(dev, gh, scheme=scheme, dt=dt, fused=fused, implicit=True,
+                     status_dev=C.c_void_p(status.data_ptr()))
+    torch.cuda.synchronize()
+    assert status.item() == 0
+    out = dev.to_host()
+    util.check_fields(out, host, STEP_FIELDS + ("Conserved_t_old",))
+    if scheme == "Hybrid":
+        for d in "XYZ":
+            assert np.array_equal(out[f"shockSensor{d}"], host[f"shockSensor{d}"])
 
 
 def test_properties(port, gpu, case):
     kind, fl, h, gh = case
     host, dev = _run_both(port, gpu, fl, h, gh, "htr_UpdatePropertiesFromPrimitive",
                           lambda v, f, m, s: (v, f.bounds(), m, s))
-    for name in ("rho", "mu", "lam", "Di", "SoS", "MassFracs"):
-        err = util.rel_err(dev[name], host[name])
-        assert err.max() <= util.RHS_REL_TOL, (name, err)
+    util.check_fields(dev, host, ("rho", "mu", "lam", "Di", "SoS", "MassFracs"))
 
 
 def test_conserved_and_primitive(port, gpu, case):
     kind, fl, h, gh = case
     host, dev = _run_both(port, gpu, fl, h, gh, "htr_UpdateConservedFromPrimitive",
                           lambda v, f, m, s: (v, f.bounds(), m, s))
-    err = util.rel_err(dev["Conserved"], host["Conserved"])
-    assert err.max() <= util.RHS_REL_TOL, err
+    util.check(dev["Conserved"], host["Conserved"], "Conserved")
     # perturb the temperature guess, then recover primitives with Newton
     fl2 = fl.copy()
     fl2["temperature"] = fl["temperature"] * 1.01
     host, dev = _run_both(port, gpu, fl2, h, gh, "htr_UpdatePrimitiveFromConserved",
                           lambda v, f, m, s: (v, f.bounds(), m, s))
-    for name in ("temperature", "pressure", "MolarFracs", "velocity"):
-        err = util.rel_err(dev[name], host[name])
-        assert err.max() <= util.RHS_REL_TOL, (name, err)
+    util.check_fields(dev, host, ("temperature", "pressure", "MolarFracs", "velocity"))
 
 
 def test_spectral_radius(port, gpu, case):
@@ -206,10 +268,7 @@ def test_rk3_step(port, gpu, case, scheme, fused):
     torch.cuda.synchronize()
     assert status.item() == 0
     out = dev.to_host()
-    for name in ("Conserved", "temperature", "pressure", "Conserved_t", "MolarFracs", "velocity",
-                 "rho", "mu", "lam", "Di", "SoS", "MassFracs"):
-        err = util.rel_err(out[name], host[name])
-        assert err.max() <= util.RHS_REL_TOL, (name, err.max())
+    util.check_fields(out, host, STEP_FIELDS)
     if scheme == "Hybrid":
         for d in "XYZ":
             assert np.array_equal(out[f"shockSensor{d}"], host[f"shockSensor{d}"])
