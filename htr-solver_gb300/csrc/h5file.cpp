@@ -42,10 +42,26 @@ struct Buf {
 
 uint64_t align8(uint64_t v) { return (v + 7) & ~uint64_t(7); }
 
+// a * b, or kOverflow when the product does not fit in 64 bits (a file can
+// declare dimensions whose product wraps; every size derived from them is
+// checked against the bytes actually present, which kOverflow never passes)
+constexpr uint64_t kOverflow = ~uint64_t(0);
+uint64_t mul_checked(uint64_t a, uint64_t b) {
+  if (a == kOverflow || b == kOverflow) return kOverflow;
+  if (a != 0 && b > kOverflow / a) return kOverflow;
+  return a * b;
+}
+
 uint64_t product(const std::vector<uint64_t> &dims) {
   uint64_t n = 1;
-  for (uint64_t d : dims) n *= d;
+  for (uint64_t d : dims) n = mul_checked(n, d);
   return n;
+}
+
+// element `index` of `size` bytes lies inside `bytes` bytes of data
+bool element_inside(uint64_t index, uint64_t size, uint64_t bytes) {
+  const uint64_t end = mul_checked(index + 1 == 0 ? kOverflow : index + 1, size);
+  return end != kOverflow && end <= bytes;
 }
 
 bool has_array_member(const Type &t) {
@@ -494,7 +510,8 @@ bool Type::is_f64_elements(uint64_t *count) const {
   }
   if (cls == kArray && base && base->cls == kFloat && base->ieee64 && !base->big_endian) {
     uint64_t n = 1;
-    for (uint32_t d : dims) n *= d;
+    for (uint32_t d : dims) n = mul_checked(n, d);
+    if (n == kOverflow) return false;
     *count = n;
     return true;
   }
@@ -525,7 +542,7 @@ Status Writer::write(const std::string &path) const {
       return {HTR_ERR_ARGUMENT, "dataset name '" + s.name + "' must be a plain name"};
   for (const auto &a : attrs_) {
     const Value &v = a.second;
-    if (v.data.size() != v.elements() * v.type.size)
+    if (v.data.size() != mul_checked(v.elements(), v.type.size))
       return {HTR_ERR_ARGUMENT, "attribute '" + a.first + "' holds the wrong number of bytes"};
   }
 
@@ -562,7 +579,8 @@ Status Writer::write(const std::string &path) const {
   std::vector<std::vector<Msg>> set_msgs(sets_.size());
   for (size_t k = 0; k < sets_.size(); k++) {
     const auto &s = sets_[k];
-    data_bytes[k] = product(s.dims) * s.type.size;
+    data_bytes[k] = mul_checked(product(s.dims), s.type.size);
+    if (data_bytes[k] == kOverflow) return {HTR_ERR_ARGUMENT, "dataset '" + s.name + "' is too large"};
     Buf fill, dt, ds, layout;
     // fill value message version 1: late allocation, fill written if set,
     // default (zero) fill value, as libhdf5 writes it for a default dataset
@@ -928,7 +946,8 @@ struct Parser {
     }
     c.skip(padded(slen));
     v.dims = s.dims;
-    const uint64_t bytes = s.null ? 0 : v.elements() * v.type.size;
+    const uint64_t bytes = s.null ? 0 : mul_checked(v.elements(), v.type.size);
+    if (bytes == kOverflow) return fail(HTR_ERR_FORMAT, "attribute '" + name + "': size overflows");
     if (!c.need(bytes)) return fail(HTR_ERR_FORMAT, "attribute '" + name + "': data beyond its message");
     v.data.assign(c.p + c.i, c.p + c.i + bytes);
     return true;
@@ -1292,7 +1311,8 @@ const Value *Reader::attribute(const std::string &name) const {
 }
 
 Status Reader::read(const Dataset &d, uint64_t offset, uint64_t bytes, void *dst) const {
-  const uint64_t total = d.elements() * d.type.size;
+  const uint64_t total = mul_checked(d.elements(), d.type.size);
+  if (total == kOverflow) return {HTR_ERR_FORMAT, "dataset '" + d.name + "': size overflows"};
   if (offset > total || bytes > total - offset)
     return {HTR_ERR_ARGUMENT, "read beyond dataset '" + d.name + "'"};
   if (d.filtered) return {HTR_ERR_UNSUPPORTED, "dataset '" + d.name + "' is filtered (compressed)"};
@@ -1317,6 +1337,7 @@ Status Reader::read(const Dataset &d, uint64_t offset, uint64_t bytes, void *dst
 
 bool Reader::as_int64(const Value &v, uint64_t index, int64_t *out) {
   if (v.type.cls != Type::kFixed || v.type.big_endian || v.type.size > 8 || index >= v.elements()) return false;
+  if (!element_inside(index, v.type.size, v.data.size())) return false;
   const uint8_t *p = v.data.data() + index * v.type.size;
   uint64_t u = 0;
   for (uint32_t k = 0; k < v.type.size; k++) u |= uint64_t(p[k]) << (8 * k);
@@ -1327,12 +1348,14 @@ bool Reader::as_int64(const Value &v, uint64_t index, int64_t *out) {
 
 bool Reader::as_double(const Value &v, uint64_t index, double *out) {
   if (v.type.cls != Type::kFloat || !v.type.ieee64 || v.type.big_endian || index >= v.elements()) return false;
+  if (!element_inside(index, 8, v.data.size())) return false;
   std::memcpy(out, v.data.data() + index * 8, 8);
   return true;
 }
 
 bool Reader::as_string(const Value &v, uint64_t index, std::string *out) {
   if (v.type.cls != Type::kString || index >= v.elements()) return false;
+  if (!element_inside(index, v.type.size, v.data.size())) return false;
   const char *p = reinterpret_cast<const char *>(v.data.data() + index * v.type.size);
   size_t n = 0;
   while (n < v.type.size && p[n] != 0) n++;
@@ -1344,6 +1367,7 @@ bool Reader::as_string(const Value &v, uint64_t index, std::string *out) {
 
 bool Reader::as_point3(const Value &v, uint64_t index, const char *member, int64_t out[3]) {
   if (v.type.cls != Type::kCompound || index >= v.elements()) return false;
+  if (!element_inside(index, v.type.size, v.data.size())) return false;
   const Type *t = &v.type;
   uint64_t at = index * v.type.size;
   if (member != nullptr) {

@@ -407,8 +407,12 @@ int htr_restart_write_master(const char *dirname, const htr_restart_info *info, 
     return fail(HTR_ERR_ARGUMENT, "timeStep does not fit the 32-bit attribute");
   if (species_names != nullptr && (nSpec < 1 || nSpec > 1024)) return fail(HTR_ERR_ARGUMENT, "nSpec out of range");
   const uint64_t ntiles = uint64_t(tiles[0]) * tiles[1] * tiles[2];
-  for (uint64_t k = 0; k < ntiles; k++)
+  for (uint64_t k = 0; k < ntiles; k++) {
     if (!rect_ok(partitions[k])) return fail(HTR_ERR_ARGUMENT, "inverted partition rectangle");
+    for (int i = 0; i < 3; i++)
+      if (partitions[k].lo[i] < bounds.lo[i] || partitions[k].hi[i] > bounds.hi[i])
+        return fail(HTR_ERR_ARGUMENT, "a partition lies outside the base index space");
+  }
 
   htr::h5::Writer w;
   {
@@ -478,6 +482,8 @@ int htr_restart_read_master(const char *dirname, htr_restart_info *info, htr_rec
     return fail(HTR_ERR_FORMAT, path + ": channelForcing is not a double");
   if (!bi || !Reader::as_point3(*bi, 0, "lo", bounds->lo) || !Reader::as_point3(*bi, 0, "hi", bounds->hi))
     return fail(HTR_ERR_FORMAT, path + ": no baseIndexSpace rectangle");
+  for (int i = 0; i < 3; i++)
+    if (bounds->lo[i] > bounds->hi[i]) return fail(HTR_ERR_FORMAT, path + ": inverted baseIndexSpace");
   if (!tn || !Reader::as_point3(*tn, 0, nullptr, tiles)) return fail(HTR_ERR_FORMAT, path + ": no tilesNumber");
   for (int i = 0; i < 3; i++)
     if (tiles[i] < 1 || tiles[i] > (int64_t(1) << 20)) return fail(HTR_ERR_FORMAT, path + ": bad tilesNumber");
@@ -487,15 +493,25 @@ int htr_restart_read_master(const char *dirname, htr_restart_info *info, htr_rec
   if (d == nullptr) return fail(HTR_ERR_FORMAT, path + ": no partitions dataset");
   if (d->dims != std::vector<uint64_t>{uint64_t(tiles[2]), uint64_t(tiles[1]), uint64_t(tiles[0])})
     return fail(HTR_ERR_FORMAT, path + ": partitions do not match tilesNumber");
+  // a rectangle of int64 points is 48 bytes; anything far larger is not one
+  if (d->type.cls != Type::kCompound || d->type.size == 0 || d->type.size > 4096)
+    return fail(HTR_ERR_FORMAT, path + ": partitions are not rectangles");
   Value v;
   v.type = d->type;
   v.dims = d->dims;
-  v.data.resize(d->elements() * d->type.size);
+  v.data.resize(ntiles * d->type.size);
   st = r.read(*d, 0, v.data.size(), v.data.data());
   if (!st.ok()) return fail(st);
-  for (uint64_t k = 0; k < ntiles; k++)
+  for (uint64_t k = 0; k < ntiles; k++) {
     if (!Reader::as_point3(v, k, "lo", partitions[k].lo) || !Reader::as_point3(v, k, "hi", partitions[k].hi))
       return fail(HTR_ERR_FORMAT, path + ": partitions are not rectangles");
+    // every tile lies inside baseIndexSpace: a tile file read through a
+    // rectangle reaching past the grid would write outside the fields
+    for (int i = 0; i < 3; i++)
+      if (partitions[k].lo[i] > partitions[k].hi[i] || partitions[k].lo[i] < bounds->lo[i] ||
+          partitions[k].hi[i] > bounds->hi[i])
+        return fail(HTR_ERR_FORMAT, path + ": partition " + std::to_string(k) + " lies outside baseIndexSpace");
+  }
   return HTR_OK;
 }
 

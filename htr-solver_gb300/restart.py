@@ -108,6 +108,26 @@ def read_master(dirname):
     }
 
 
+def check_partitions(dirname, parts, bounds):
+    """The master file's tiles lie inside the grid and cover every point of
+    it exactly once (a restart with overlapping or missing tiles would leave
+    points unloaded or loaded twice)."""
+    import numpy as np
+    lo = [bounds.lo[i] for i in range(3)]
+    ext = [bounds.hi[i] - bounds.lo[i] + 1 for i in range(3)]
+    seen = np.zeros((ext[2], ext[1], ext[0]), dtype=np.uint8)
+    for r in parts:
+        a = [r.lo[i] - lo[i] for i in range(3)]
+        b = [r.hi[i] - lo[i] for i in range(3)]
+        if any(a[i] < 0 or b[i] >= ext[i] or a[i] > b[i] for i in range(3)):
+            raise abi.HtrError(f"{dirname}: tile {list(r.lo)}-{list(r.hi)} lies outside the grid")
+        seen[a[2]:b[2] + 1, a[1]:b[1] + 1, a[0]:b[0] + 1] += 1
+    if seen.max() > 1:
+        raise abi.HtrError(f"{dirname}: tiles overlap")
+    if seen.min() < 1:
+        raise abi.HtrError(f"{dirname}: tiles leave {int((seen == 0).sum())} grid points uncovered")
+
+
 def load(dirname, fluid, profiles=False, stream=None, mixture=None):
     """Fills the restart fields of `fluid` from `dirname`; returns the
     master file's timeStep, simTime and channelForcing.  With `mixture` (a
@@ -121,6 +141,7 @@ def load(dirname, fluid, profiles=False, stream=None, mixture=None):
     if list(b.lo) != list(fb.lo) or list(b.hi) != list(fb.hi):
         raise abi.HtrError(f"{dirname}: baseIndexSpace {list(b.lo)}-{list(b.hi)} does not match the grid "
                            f"{list(fb.lo)}-{list(fb.hi)}")
+    check_partitions(dirname, m["partitions"], fb)
     lib, flags, s = _lib_and_stream(fluid, stream)
     if profiles:
         flags |= abi.HTR_RESTART_PROFILES

@@ -287,6 +287,55 @@ def test_errors(tmp_path):
 
 
 @needs_lib
+def test_master_files_with_bad_sizes_or_tiles_are_rejected(tmp_path):
+    """Attribute dimensions whose byte count overflows 64 bits, partitions
+    reaching outside baseIndexSpace, and tilings that overlap or leave grid
+    points uncovered are refused (HTR_ERR_FORMAT / HtrError), never read."""
+    import struct
+
+    from tests import h5_v2
+    lib = runtime.lib()
+    info, b, t = abi.htr_restart_info(), abi.htr_rect3(), (C.c_int64 * 3)()
+    for name, dtype, dims in (("simTime", h5_v2.F64, [2 ** 61]), ("timeStep", h5_v2.int_type(8), [2 ** 32, 2 ** 32]),
+                              ("timeStep", h5_v2.int_type(8), [2 ** 62, 3])):
+        d = tmp_path / f"ov_{name}_{len(dims)}_{dims[0]}"
+        d.mkdir()
+        w = h5_v2.Writer()
+        w.attribute("timeStep", h5_v2.int_type(8), [1], struct.pack("<q", 1))
+        w.attribute("simTime", h5_v2.F64, [1], struct.pack("<d", 0.5))
+        w.root_msgs = [m for m in w.root_msgs if name.encode() + b"\0" not in m[1]]
+        w.attribute(name, dtype, dims, bytes(8))
+        w.write(str(d / "master.hdf"))
+        assert lib.htr_restart_read_master(str(d).encode(), C.byref(info), C.byref(b), t, None, 0) == \
+            abi.HTR_ERR_FORMAT, name
+    f = random_fluid((4, 3, 2), seed=9)
+    d = str(tmp_path / "tiles")
+    restart.dump(d, f, tiles=(2, 1, 1))
+    master = os.path.join(d, "master.hdf")
+    good = open(master, "rb").read()
+    second = struct.pack("<6q", 2, 0, 0, 3, 2, 1)
+    assert good.count(second) == 1
+    with open(master, "wb") as fh:
+        fh.write(good.replace(second, struct.pack("<6q", 2, 0, 0, 7, 2, 1)))
+    parts = (abi.htr_rect3 * 2)()
+    assert lib.htr_restart_read_master(d.encode(), C.byref(info), C.byref(b), t, parts, 2) == abi.HTR_ERR_FORMAT
+    assert b"outside baseIndexSpace" in lib.htr_last_error()
+    # the writer refuses such a partition too
+    bounds = abi.rect((0, 0, 0), (3, 2, 1))
+    out = (abi.htr_rect3 * 2)(abi.rect((0, 0, 0), (1, 2, 1)), abi.rect((2, 0, 0), (7, 2, 1)))
+    t2 = (C.c_int64 * 3)(2, 1, 1)
+    assert lib.htr_restart_write_master(d.encode(), C.byref(info), bounds, t2, out, 5, None, None) == \
+        abi.HTR_ERR_ARGUMENT
+    # tilings inside the grid that overlap or miss points
+    for rects, msg in (((abi.rect((0, 0, 0), (2, 2, 1)), abi.rect((2, 0, 0), (3, 2, 1))), "overlap"),
+                       ((abi.rect((0, 0, 0), (0, 2, 1)), abi.rect((2, 0, 0), (3, 2, 1))), "uncovered")):
+        arr = (abi.htr_rect3 * 2)(*rects)
+        abi.check(lib, lib.htr_restart_write_master(d.encode(), C.byref(info), bounds, t2, arr, 5, None, None))
+        with pytest.raises(abi.HtrError, match=msg):
+            restart.load(d, fluid.Fluid(f.shape, f.nspec))
+
+
+@needs_lib
 def test_corrupt_files_are_rejected_not_crashed(tmp_path):
     lib = runtime.lib()
     f = random_fluid((4, 3, 2), seed=8)
@@ -382,8 +431,7 @@ def test_run_continues_from_a_restart(tmp_path):
     runtime.rk3_step(b, gh, scheme="Hybrid", dt=dt, chemistry=False)
     torch.cuda.synchronize()
     oa, ob = a.to_host(), b.to_host()
-    for n in ("Conserved", "temperature", "pressure", "velocity", "rho"):
-        assert util.rel_err(ob[n], oa[n]).max() <= util.RHS_REL_TOL, n
+    util.check_fields(ob, oa, ("Conserved", "temperature", "pressure", "velocity", "rho"))
 
 
 # ---------------------------------------------------------------- newer file format

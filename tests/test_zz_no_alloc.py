@@ -46,22 +46,42 @@ def test_static_scratch_equals_workspace_path(kind):
             assert np.array_equal(ha[name], hb[name], equal_nan=True), name
 
 
-def test_static_scratch_allocates_nothing():
+def _measure_in_this_process():
+    """Free device memory around the first two static steps of a process
+    that has loaded its mixture (htr_load_mixture is the set-up point that
+    loads the scratch's module)."""
     import torch
     shape, dt, chem = CASES["air"]
     fl, h, m = util.make_state(oracle.port_lib(), "air", shape, seed=4)
-    gh = runtime.load_mixture(fl.meta["eos"], m)
     dev = fl.to_device("cuda")
-    abi.check(runtime.lib(), _static_step(dev, gh, dt, chem), "first call")
+    gh = runtime.load_mixture(fl.meta["eos"], m)
     torch.cuda.synchronize()
     before_torch = torch.cuda.memory_allocated()
     free_before, _ = torch.cuda.mem_get_info()
-    for _ in range(2):
-        abi.check(runtime.lib(), _static_step(dev, gh, dt, chem), "htr_rk3_step_static")
+    for k in range(2):
+        abi.check(runtime.lib(), _static_step(dev, gh, dt, chem), f"htr_rk3_step_static call {k}")
     torch.cuda.synchronize()
     free_after, _ = torch.cuda.mem_get_info()
-    assert torch.cuda.memory_allocated() == before_torch
-    assert free_after == free_before
+    return before_torch, torch.cuda.memory_allocated(), free_before, free_after
+
+
+def test_static_scratch_allocates_nothing():
+    """In a fresh process (where the scratch's module is not yet loaded) and
+    in this one: once the mixture is loaded, the first static steps change
+    neither torch's allocations nor the device's free memory."""
+    import json
+    import os
+    import subprocess
+    import sys
+    root = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+    code = ("import sys, json; sys.path.insert(0, %r); import __graft_entry__ as g; g.load_package(); "
+            "from tests import test_zz_no_alloc as t; print(json.dumps(t._measure_in_this_process()))" % root)
+    r = subprocess.run([sys.executable, "-c", code], cwd=root, capture_output=True, text=True, timeout=600)
+    assert r.returncode == 0, r.stderr[-2000:]
+    fresh = json.loads(r.stdout.strip().splitlines()[-1])
+    for bt, at, fb, fa in (fresh, _measure_in_this_process()):
+        assert at == bt
+        assert fa == fb
 
 
 def test_static_scratch_rejects_oversize():
