@@ -219,6 +219,86 @@ STATE_FIELDS = ["Conserved", "pressure", "temperature", "MassFracs", "MolarFracs
                 "rho", "mu", "lam", "Di", "SoS"]
 
 
+def fp64_roofline(prof, dominant, fdom, ncell, fp64):
+    """The dominant kernel against the FP64 pipe, the resource that bounds
+    it: FP64 FLOP executed per cell (ncu DADD + DMUL + 2 DFMA counts,
+    profiles/stage_kernels_air96_hybrid.md) x cells / its CUDA-event time,
+    over the FP64 peak measured in this run by the DFMA-chain probe
+    (MEASURED_PEAKS.json has no FP64 figure)."""
+    flops = KERNEL_FP64_FLOPS.get(fdom)
+    t = prof[dominant] * 1e-3
+    achieved = flops * ncell / t / 1e12 if flops else None
+    return {"bound": "fp64", "kernel": dominant, "achieved": achieved, "peak": fp64, "unit": "TFLOP/s",
+            "frac": achieved / fp64 if (achieved and fp64) else None,
+            "peak_source": "DFMA-chain probe run in this benchmark (libhtr_probe.so)",
+            "flops_per_cell": flops, "cells": ncell, "launch_ms": prof[dominant],
+            "flops_source": "ncu smsp__sass_thread_inst_executed_op_d{add,mul,fma} at 96^3, DFMA counted twice",
+            "traffic": KERNEL_DRAM_BYTES[fdom] * ncell if fdom in KERNEL_DRAM_BYTES else None,
+            "traffic_source": "ncu dram__bytes_read.sum + dram__bytes_write.sum per cell at 96^3 x cells"}
+
+
+def teno_face_fraction(dev, gh, lib, runtime):
+    """Faces that the last fused hybrid stage (the kernel profile's)
+    reconstructed with TENO, from the TENO queue counters, over all faces."""
+    from htr_gb300 import runtime as rt
+    inner = dev.interior()
+    nb = lib.htr_rk3_workspace_bytes(inner, gh)
+    ws = rt._workspace.get(nb, dev.device)
+    c = (C.c_ulonglong * 3)()
+    abi.check(lib, lib.htr_rk3_teno_face_counts(inner, gh, C.c_void_p(ws), nb, c, runtime.stream_handle()),
+              "teno counts")
+    n = [inner.hi[i] - inner.lo[i] + 1 for i in range(3)]
+    faces = [(n[0] + (d == 0)) * (n[1] + (d == 1)) * (n[2] + (d == 2)) for d in range(3)]
+    return {"value": sum(c) / sum(faces), "per_direction": [c[d] / faces[d] for d in range(3)],
+            "teno_faces": [int(x) for x in c], "faces": faces,
+            "note": "sensor-rejected faces of one fused hybrid stage of the timed state"}
+
+
+def cpu_full_step(dev, gh, dt, runtime):
+    """The CPU oracle (the port, all host threads) on one whole SSP-RK3 step
+    of the benchmark's own grid and state (copied from the device), timed;
+    the same step on the GPU from the same state is compared with it
+    element by element (pointwise error over the bar max(1e-11 |cpu|,
+    1e-12 max|cpu|))."""
+    import torch
+
+    import oracle
+    port = oracle.port_lib()
+    threads = os.cpu_count() or 1
+    port.htr_oracle_set_threads(threads)
+    host = dev.to_host()
+    eos = abi.HTR_EOS_AIRMIX
+    hp = oracle.load_mixture(port, eos, workloads.make_mixture_struct(port, eos, workloads.AIR_REF))
+    t0 = time.perf_counter()
+    oracle.step(port, host, hp, scheme="Hybrid", dt=dt, chemistry=True)
+    el = time.perf_counter() - t0
+    gpu = dev.copy()
+    runtime.rk3_step(gpu, gh, dt=dt, chemistry=True)
+    torch.cuda.synchronize()
+    ratio = pointwise_ratio(gpu["Conserved"], host["Conserved"])
+    flags = all(torch.equal(gpu[f"shockSensor{d}"].cpu(), torch.from_numpy(host[f"shockSensor{d}"])) for d in "XYZ")
+    del gpu
+    return {"value": 3.0 * dev.ncells / el, "unit": UNIT, "cores": threads, "kind": "port",
+            "seconds": el, "same_config": True,
+            "sample": f"one SSP-RK3 step (3 cell-updates per cell) of the benchmark's full "
+                      f"{dev.nx}x{dev.ny}x{dev.nz} grid and state, OpenMP over all host threads",
+            "parity": {"conserved_pointwise_ratio": ratio, "sensors_bit_exact": flags,
+                       "note": "GPU step from the same state; ratio = max |gpu - cpu| / "
+                               "max(1e-11 |cpu|, 1e-12 max|cpu| per component), <= 1 passes"}}
+
+
+def pointwise_ratio(got, want):
+    """max over elements of |got - want| / max(1e-11 |want|, 1e-12 max|want| of the component)."""
+    import torch
+    a = got.detach().cpu().double() if hasattr(got, "detach") else torch.from_numpy(np.asarray(got))
+    b = want.detach().cpu().double() if hasattr(want, "detach") else torch.from_numpy(np.asarray(want))
+    a = a.reshape(-1, a.shape[-1]) if a.dim() > 3 else a.reshape(-1, 1)
+    b = b.reshape(-1, b.shape[-1]) if b.dim() > 3 else b.reshape(-1, 1)
+    floor = 1e-12 * b.abs().max(dim=0).values
+    bound = torch.maximum(1e-11 * b.abs(), floor[None, :])
+    return float(((a - b).abs() / bound).max())
+
+
 def e2e_pipelined(dev, gh, dt, steps, runtime, barrier, device):
     """End-to-end cell-updates/s through runtime.rk3_step with host state.
 
@@ -291,16 +371,12 @@ def run_batched(args, device, runtime, lib, steps=3):
         del host
         workloads.derive_state(lib, dev, gh, runtime.stream_handle())
         air = eos == abi.HTR_EOS_AIRMIX
-        if air:
-            dt = choose_dt(dev, gh, lib, runtime)
-        else:
-            out = torch.zeros(1, dtype=torch.float64, device=device)
-            v = dev.view()
-            abi.check(lib, lib.htr_CalculateMaxSpectralRadius(
-                C.byref(v), dev.interior(), gh, C.cast(C.c_void_p(out.data_ptr()), C.POINTER(C.c_double)),
-                runtime.stream_handle()), "cfl")
-            dt = 0.8 / out.item()
-        strips.append(dict(dev=dev, gh=gh, dt=dt, offs=offs, L=[i["L"] for i in group], chem=air))
+        L = [i["L"] for i in group]
+        # every tube its own step size: CFL 0.8 over its own spectral radius,
+        # for air also at most half its fastest chemical time scale
+        dts = tubes.strip_dts(dev, offs, [x + 2 for x in L], gh, cfl=0.8, chemistry=air, lib=lib)
+        dt_cell = torch.tensor(tubes.cell_dt(offs, [x + 2 for x in L], dts), dtype=torch.float64, device=device)
+        strips.append(dict(dev=dev, gh=gh, dt=min(dts), dts=dts, dt_cell=dt_cell, offs=offs, L=L, chem=air))
     cells = sum(s["dev"].ncells for s in strips)
     ws = runtime.Workspace()
     ws.get(max(runtime.workspace_bytes(s["dev"], s["gh"]) for s in strips), device)
@@ -313,7 +389,7 @@ def run_batched(args, device, runtime, lib, steps=3):
 
     def step_all(st):
         for s in strips:
-            runtime.rk3_step(s["dev"], s["gh"], dt=s["dt"], chemistry=s["chem"], stream=st, workspace=ws)
+            runtime.rk3_step_cells(s["dev"], s["gh"], s["dt_cell"], chemistry=s["chem"], stream=st, workspace=ws)
 
     log("batched: graph capture")
     side = torch.cuda.Stream()
@@ -340,9 +416,9 @@ def run_batched(args, device, runtime, lib, steps=3):
 
     def loop_all():
         for s in strips:
-            prm = p(runtime.SCHEMES["Hybrid"], 1.0, 0.0, s["dt"], 1 if s["chem"] else 0)
             sv = s["dev"].view()
-            for off, L in zip(s["offs"], s["L"]):
+            for off, L, dt in zip(s["offs"], s["L"], s["dts"]):
+                prm = p(runtime.SCHEMES["Hybrid"], 1.0, 0.0, dt, 1 if s["chem"] else 0)
                 v, fb, inner = tubes.tube_view(sv, int(off), L)
                 st = lib.htr_rk3_step(C.byref(v), inner, fb, C.byref(prm), s["gh"], C.byref(used), None, sh)
                 if st:
@@ -368,8 +444,9 @@ def run_batched(args, device, runtime, lib, steps=3):
             "autotune": {"tuning": tuned, "stage_ms_tuned": t_tuned, "stage_ms_default": t_default},
             "config": {"workload": f"{n} 1-D shock tubes, 128-8192 cells, gamma-1.4 gas or 5-species air "
                                    f"(1/2 each), staggered Dirichlet ends, hybrid scheme, SSP-RK3",
-                       "form": "two strips (one per mixture), one CUDA graph per RK3 step",
-                       "dt": {("air" if s["chem"] else "gas"): s["dt"] for s in strips}}}
+                       "form": "two strips (one per mixture), one CUDA graph per RK3 step, every tube "
+                               "its own step size (htr_rk3_step_cells_ws)",
+                       "dt": {("air" if s["chem"] else "gas"): [min(s["dts"]), max(s["dts"])] for s in strips}}}
     autotune.set_tuning(default)
     return out
 
@@ -461,6 +538,34 @@ def run_wall(args, device, runtime, lib):
     # fused boundary step, for comparison
     hyb = wall.FusedBoundaryRun(dev, gh, bc, scheme="Hybrid", workspace=fused.ws)
     ms_h, fin_h = timed(lambda d: hyb.step(d))
+    cpu = None
+    if args.cpu_baseline:
+        # one step of the full grid on the CPU oracle (the port, all host
+        # threads), from the same start state, against the fused GPU step
+        import oracle
+        log("wall: CPU baseline, one step of the full grid on the port")
+        for k, a_ in dev.arrays.items():
+            a_.copy_(start[k])
+        torch.cuda.synchronize()
+        ref = dev.to_host()
+        port = oracle.port_lib()
+        threads = os.cpu_count() or 1
+        port.htr_oracle_set_threads(threads)
+        eos = abi.HTR_EOS_AIRMIX
+        hp = oracle.load_mixture(port, eos, workloads.make_mixture_struct(port, eos, workloads.AIR_REF))
+        t0 = time.perf_counter()
+        oracle.boundary_layer_step(port, ref, hp, dt, bc["xNeg"][1]["P"], bc["xPos"][1]["P"],
+                                   (bc["xPos"][1]["LengthScale"], bc["yPos"][1]["LengthScale"]))
+        el = time.perf_counter() - t0
+        fused.step(dt)
+        torch.cuda.synchronize()
+        cpu = {"value": 3.0 * cells / el, "unit": UNIT, "cores": threads, "kind": "port", "seconds": el,
+               "same_config": True,
+               "sample": f"one boundary-layer SSP-RK3 step of the full {num[0]}x{num[1]}x{num[2]} interior "
+                         f"(TENO-LAD), the reference driver's task order over its zones",
+               "parity": {"conserved_pointwise_ratio": pointwise_ratio(dev["Conserved"], ref["Conserved"]),
+                          "note": "fused GPU step from the same state"}}
+        del ref
     del start
     # task path kernels per stage: time derivatives, chemistry, 3 Euler, 3
     # diffusion, 2 x (max Mach), 2 outflow, 1 inflow, RK update, primitives,
@@ -488,7 +593,8 @@ def run_wall(args, device, runtime, lib):
                        "interior_cells": list(num), "grid_with_ghosts": list(g.shape), "cells": cells,
                        "tasks": "task entry points in the reference driver's order over its zones",
                        "fused": "htr_rk3_step_bc_ws: fused stage pipeline with the boundary rules"},
-            "gpu_launches": args.wall_steps * (3 * (per_stage_f if best == "fused" else per_stage_t) + 2)}
+            "gpu_launches": args.wall_steps * (3 * (per_stage_f if best == "fused" else per_stage_t) + 2),
+            **({"cpu": cpu} if cpu else {})}
 
 
 def run_restart(dev, device, reps=3):
@@ -531,7 +637,13 @@ def run_restart(dev, device, reps=3):
             "note": "host wall clock, device synchronised on both sides; files in the page cache (no fsync)"}
 
 
-def fp64_peak(lib):
+def fp64_peak(_lib=None):
+    """FP64 TFLOP/s of the device, measured by the DFMA-chain probe of
+    libhtr_probe.so (a benchmark library, not the product)."""
+    from htr_gb300 import build as pkg_build
+    if not os.path.exists(pkg_build.PROBE_LIB):
+        return None
+    lib = C.CDLL(pkg_build.PROBE_LIB)
     lib.htr_probe_fp64_tflops.argtypes = [C.c_int, C.POINTER(C.c_double)]
     lib.htr_probe_fp64_tflops.restype = C.c_int
     t = C.c_double(0)
@@ -588,13 +700,21 @@ def run_gpu(args):
     if rank == 0:
         log("kernel profile")
         prof = kernel_profile(dev, gh, lib, runtime, dt)
+        teno = teno_face_fraction(dev, gh, lib, runtime)
         dominant = max(prof, key=prof.get)
         fdom = dominant.rsplit("_", 1)[0] if dominant[-2:] in ("_x", "_y", "_z") else dominant
         peak, peak_src = hbm_peak()
-        per_cell = KERNEL_BYTES.get(fdom)
-        bytes_launch = per_cell * ncell if per_cell is not None else None
-        achieved = bytes_launch / (prof[dominant] * 1e-3) / 1e9 if bytes_launch else None
         fp64 = fp64_peak(lib)
+        roof = fp64_roofline(prof, dominant, fdom, ncell, fp64)
+        # the step as a whole against HBM, at the reference layout's
+        # compulsory 495 B per cell-update
+        step_gbs = BYTES_PER_CELL_UPDATE_AIR * 3.0 * ncell / (ms_max / args.steps * 1e-3) / 1e9
+        roof["hbm"] = {"bytes_per_cell_update": BYTES_PER_CELL_UPDATE_AIR, "achieved": step_gbs, "peak": peak,
+                       "unit": "GB/s", "frac": step_gbs / peak, "peak_source": peak_src + " (MEASURED_PEAKS.json)",
+                       "of": "whole SSP-RK3 step: 3 cell-updates per cell per step x 495 B / step time",
+                       "kernel_traffic_bytes_per_cell": KERNEL_DRAM_BYTES.get(fdom),
+                       "kernel_hbm_frac": (KERNEL_DRAM_BYTES[fdom] * ncell / (prof[dominant] * 1e-3) / 1e9 / peak
+                                           if fdom in KERNEL_DRAM_BYTES else None)}
         result = {
             "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": ws, "steps": args.steps,
             "warmup": args.warmup, "ms_per_step": ms_max / args.steps, "higher_is_better": True,
@@ -609,21 +729,8 @@ def run_gpu(args):
                     "d2h_bytes_per_step": int(d2h), "steps": e2e_steps,
                     "copies": "11 state fields H2D and Conserved D2H every step, pinned host memory, "
                               "double-buffered on copy streams overlapping the previous step"},
-            "roofline": {"bound": "hbm", "kernel": dominant, "achieved": achieved, "peak": peak,
-                         "unit": "GB/s", "frac": (achieved / peak) if achieved else None,
-                         "peak_source": peak_src,
-                         "traffic": KERNEL_DRAM_BYTES[fdom] * ncell if fdom in KERNEL_DRAM_BYTES else None,
-                         "traffic_source": "ncu DRAM bytes per cell at 96^3 x cells", "bytes_per_launch": bytes_launch,
-                         "bytes_per_cell": per_cell, "launch_ms": prof[dominant]},
-            "fp64": {"peak_tflops_probe": fp64, "note": "measured in this run by a DFMA-chain probe",
-                     "kernel": dominant,
-                     "flops_per_cell": KERNEL_FP64_FLOPS.get(fdom),
-                     "achieved_tflops": (KERNEL_FP64_FLOPS[fdom] * ncell / (prof[dominant] * 1e-3) / 1e12
-                                         if fdom in KERNEL_FP64_FLOPS else None),
-                     "frac": (KERNEL_FP64_FLOPS[fdom] * ncell / (prof[dominant] * 1e-3) / 1e12 / fp64
-                              if fdom in KERNEL_FP64_FLOPS and fp64 else None),
-                     "bound": "fp64 pipe (DADD/DMUL/DFMA plus compares, conversions and the "
-                              "division/sqrt sequences)"},
+            "roofline": roof,
+            "teno_face_fraction": teno,
             "kernel_ms_per_stage": prof,
             # per step: Ducros + shock sensors + Conserved_old copy, then per stage
             # prepass, 3 KG, 3 TENO (one per direction's queue), 3 diffusion, 1 update
@@ -655,107 +762,87 @@ def run_gpu(args):
             except Exception as exc:
                 result["restart"] = {"error": f"{type(exc).__name__}: {exc}"}
         if args.cpu_baseline:
-            log("CPU baseline")
-            result["cpu_baseline"] = cpu_baseline(args.cpu_seconds)
+            log("CPU baseline: one SSP-RK3 step of the full grid on the port")
+            result["cpu_baseline"] = cpu_full_step(dev, gh, dt, runtime)
+            if isinstance(result.get("wall"), dict) and "cpu" in result["wall"]:
+                result["cpu_baseline"]["wall"] = result["wall"].pop("cpu")
     if ws > 1:
         torch.distributed.barrier()
         torch.distributed.destroy_process_group()
     return result
 
 
-def cpu_baseline(budget_s=20.0, n=48, wall_num=(64, 48, 32)):
-    """The CPU oracle (all host threads) on a bounded sample of the same workload:
-    whole SSP-RK3 steps (sensors, 3 x (chemistry, Euler Z/Y/X, diffusion Z/Y/X,
-    RK update, primitive and property refresh)) of an n^3 box, the same work
-    per cell-update as the GPU step."""
+def cpu_choose_dt(lib, fl, h):
+    """choose_dt on a host grid with a CPU library."""
     import oracle
-    lib = oracle.ref_lib(abi.HTR_EOS_AIRMIX)
-    kind = "reference"
-    if lib is None:
-        lib = oracle.port_lib()
-        kind = "port"
-    threads = os.cpu_count() or 1
-    if kind == "port":
-        lib.htr_oracle_set_threads(threads)
-    fl = workloads.air_box(n, seed=1234)
-    m = workloads.make_mixture_struct(lib, abi.HTR_EOS_AIRMIX, fl.meta["mix"])
-    h = oracle.load_mixture(lib, abi.HTR_EOS_AIRMIX, m)
-    workloads.derive_state(lib, fl, h)
-    steps = 0
-    t0 = time.perf_counter()
-    while True:
-        oracle.step(lib, fl, h, dt=1e-9, chemistry=True)
-        steps += 1
-        if time.perf_counter() - t0 > budget_s or steps >= 200:
-            break
-    el = time.perf_counter() - t0
-    out = {"value": 3.0 * steps * fl.ncells / el, "unit": UNIT, "cores": threads, "kind": kind,
-           "sample": f"{steps} SSP-RK3 steps (3 cell-updates per cell each) of a {n}^3 box of the same "
-                     f"workload, {el:.1f} s, OpenMP over all host threads"}
-    if wall_num:
-        out["wall"] = cpu_wall_baseline(lib, kind, wall_num, budget_s=budget_s / 2)
-    return out
-
-
-def cpu_wall_baseline(lib, kind, num, budget_s=10.0):
-    """The boundary-layer step (task composition of wall.BoundaryRun) on the
-    CPU oracle over a bounded sample grid of the same workload; the
-    Regent-defined pieces come from the port when the compiled reference
-    lacks them."""
-    import oracle
-    from htr_gb300 import wall
-    port = oracle.port_lib()
-    fl = wall.boundary_layer(num=num, seed=77)
-    fl.meta["grid"].fill(fl, port)
-    m = workloads.make_mixture_struct(lib, abi.HTR_EOS_AIRMIX, fl.meta["mix"])
-    h = oracle.load_mixture(lib, abi.HTR_EOS_AIRMIX, m)
-    workloads.derive_state(lib, fl, h)
-    bc = fl.meta["bc"]
-    P = bc["xNeg"][1]["P"]
-    Ls = (bc["xPos"][1]["LengthScale"], bc["yPos"][1]["LengthScale"])
-    if kind == "port":
-        run = wall.BoundaryRun(port, fl, h, bc)
-        dt = run.spectral_dt(0.8)
-        step = lambda: run.step(dt)
-    else:
-        hp = oracle.load_mixture(port, abi.HTR_EOS_AIRMIX, workloads.make_mixture_struct(port, abi.HTR_EOS_AIRMIX,
-                                                                                         fl.meta["mix"]))
-        dt = wall.BoundaryRun(port, fl, hp, bc).spectral_dt(0.8)
-        step = lambda: oracle.boundary_layer_step(lib, fl, h, dt, P, P, Ls, regent=port, regent_mix=hp)
-    steps = 0
-    t0 = time.perf_counter()
-    while True:
-        step()
-        steps += 1
-        if time.perf_counter() - t0 > budget_s or steps >= 50:
-            break
-    el = time.perf_counter() - t0
-    cells = num[0] * num[1] * num[2]
-    return {"value": 3.0 * steps * cells / el, "unit": UNIT, "kind": kind,
-            "sample": f"{steps} boundary-layer SSP-RK3 steps of {num[0]}x{num[1]}x{num[2]} interior cells of the "
-                      f"same workload, {el:.1f} s"}
+    dt = oracle.spectral_dt(lib, fl, h, 0.8)
+    v = fl.view()
+    abi.check(lib, lib.htr_InitializeTimeDerivatives(C.byref(v), fl.bounds(), 0, h, None), "init")
+    abi.check(lib, lib.htr_AddChemistrySources(C.byref(v), fl.interior(), h, None), "chem")
+    w = np.abs(fl["Conserved_t"][..., :5])
+    rhoi = fl["Conserved"][..., :5]
+    sig = rhoi > 1e-3 * fl["rho"][..., None]
+    with np.errstate(divide="ignore"):
+        tau = np.where(sig, rhoi / np.maximum(w, 1e-300), np.inf).min()
+    return min(dt, 0.5 * float(tau))
 
 
 def run_reference(args):
+    """Reference arm: the reference's CPU implementation of the path on the
+    host cores, on this benchmark's own grid and seeded state (args.n^3
+    5-species air, the GPU arm's rank-0 seed): the reference's compiled CPU
+    tasks where they were built from the reference sources (oracle/_ref),
+    else their bit-exact restatement, the port (the GPU machine, where the
+    reference sources are not present).  One step of this arm is one SSP-RK3
+    stage over the whole grid, in the reference driver's order: the shock
+    sensors and Conserved_old at the first stage of every three, zeroed time
+    derivatives, chemistry sources, Euler Z, Y, X, diffusion Z, Y, X, the RK
+    update and the primitive / property refresh -- one cell-update of every
+    cell -- so that W + K steps of the full grid fit in a few minutes.
+    value = cells / median stage time."""
     ws, rank, _ = dist_env()
     if rank != 0:
         return None
-    base = cpu_baseline(budget_s=max(5.0, args.cpu_seconds / max(1, args.steps + args.warmup)))
-    # K timed samples after W warm-up samples, each a bounded RHS sample
-    vals = []
+    import oracle
+    eos = abi.HTR_EOS_AIRMIX
+    lib, kind = oracle.ref_lib(eos), "reference"
+    threads = os.cpu_count() or 1
+    if lib is None:
+        lib, kind = oracle.port_lib(), "port"
+        lib.htr_oracle_set_threads(threads)
+    else:
+        os.environ.setdefault("OMP_NUM_THREADS", str(threads))
+    log(f"reference arm ({kind}): building the {args.n}^3 state")
+    fl = workloads.air_box(args.n, seed=1234)
+    h = oracle.load_mixture(lib, eos, workloads.make_mixture_struct(lib, eos, fl.meta["mix"]))
+    workloads.derive_state(lib, fl, h)
+    dt = cpu_choose_dt(lib, fl, h)
+    v = fl.view()
+    times = []
     for i in range(args.warmup + args.steps):
-        b = cpu_baseline(budget_s=max(2.0, args.cpu_seconds / max(1, args.steps + args.warmup)), wall_num=None)
+        stage = i % 3 + 1
+        t0 = time.perf_counter()
+        if stage == 1:
+            oracle.update_sensors(lib, fl, h, 1.0)
+            abi.check(lib, lib.htr_InitializeTemporaries(C.byref(v), fl.bounds(), h, None), "tmp")
+        oracle.update_derivatives(lib, fl, h, stage, dt, "Hybrid", True)
+        abi.check(lib, lib.htr_UpdateVars(C.byref(v), fl.interior(), stage, dt, 0, h, None), "rk")
+        oracle.refresh(lib, fl, h)
+        el = time.perf_counter() - t0
+        log(f"reference arm: step {i} (stage {stage}) {el:.2f} s")
         if i >= args.warmup:
-            vals.append(b["value"])
-    value = float(np.median(vals)) if vals else base["value"]
+            times.append(el)
+    t = float(np.median(times))
+    value = fl.ncells / t
+    sample = (f"{args.steps} timed SSP-RK3 stages (after {args.warmup} untimed) of the full {args.n}^3 grid, "
+              f"one cell-update of every cell each, median {t:.2f} s; OpenMP over {threads} host threads")
     return {"impl": "reference", "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": ws,
-            "steps": args.steps, "warmup": args.warmup, "higher_is_better": True, "scaling": "weak",
-            "vs_baseline": None, "dtype": "f64", "data": "synthetic",
+            "steps": args.steps, "warmup": args.warmup, "ms_per_step": t * 1e3, "higher_is_better": True,
+            "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
             "config": {"workload": f"periodic {args.n}^3 box, 5-species air (AirMix), hybrid TENO/KG + "
                                    f"diffusion + explicit chemistry, SSP-RK3", "grid": [args.n] * 3,
-                       "sample_grid": [48] * 3},
-            "cpu_baseline": {"value": value, "unit": UNIT, "cores": base["cores"], "kind": base["kind"],
-                             "sample": base["sample"], "wall": base.get("wall")},
+                       "cells": fl.ncells, "dt": dt, "step": "one SSP-RK3 stage (1 cell-update per cell)"},
+            "cpu_baseline": {"value": value, "unit": UNIT, "cores": threads, "kind": kind, "sample": sample},
             "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
 
 
@@ -766,7 +853,6 @@ def main():
     p.add_argument("--warmup", type=int, default=3)
     p.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
     p.add_argument("--n", type=int, default=256)
-    p.add_argument("--cpu-seconds", type=float, default=20.0)
     p.add_argument("--no-cpu-baseline", dest="cpu_baseline", action="store_false")
     p.add_argument("--tubes", type=int, default=4096, help="batched shock tubes (0: skip)")
     p.add_argument("--serve", type=int, default=32, help="served requests (0: skip)")

@@ -172,6 +172,7 @@ PROTOTYPES = {
     "htr_InitializeTimeDerivatives": [_V, _R, C.c_int, _M, _S],
     "htr_UpdateVars": [_V, _R, C.c_int, C.c_double, C.c_int, _M, _S],
     "htr_decision_counters": [C.c_int, _P(C.c_ulonglong)],
+    "htr_rk3_teno_face_counts": [_R, _M, C.c_void_p, C.c_size_t, _P(C.c_ulonglong), _S],
 }
 HTR_DECISION_COUNTERS = 7
 # order of the counts of htr_decision_counters

@@ -1,10 +1,10 @@
 """Builds libhtr_gb300.so (CUDA, sm_103a) in-tree under htr-solver_gb300/_build/.
 
 Translation units that evaluate TENO selections or shock sensors
-(euler.cu, sensor.cu, stage_euler.cu) and the grid metrics (metric.cu)
-are compiled with -fmad=false so every floating-point
-operation is rounded exactly as the reference's CPU build rounds it; the
-others keep FMA contraction.
+(euler.cu, sensor.cu, stage_euler.cu), the grid metrics (metric.cu) and the
+implicit chemistry solver (implicit_chem.cu) are compiled with -fmad=false
+so every floating-point operation is rounded exactly as the reference's CPU
+build rounds it; the others keep FMA contraction.
 """
 import concurrent.futures as cf
 import os
@@ -15,9 +15,12 @@ HERE = os.path.dirname(os.path.abspath(__file__))
 CSRC = os.path.join(HERE, "csrc")
 OUT_DIR = os.path.join(HERE, "_build")
 LIB = os.path.join(OUT_DIR, "libhtr_gb300.so")
+# the benchmark's FP64 peak probe, a library of its own (not the product)
+PROBE_SRC = os.path.join(HERE, "probe", "fp64_probe.cu")
+PROBE_LIB = os.path.join(OUT_DIR, "libhtr_probe.so")
 
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
-EXACT_TUS = {"euler.cu", "sensor.cu", "stage_euler.cu", "metric.cu"}
+EXACT_TUS = {"euler.cu", "sensor.cu", "stage_euler.cu", "metric.cu", "implicit_chem.cu"}
 
 
 def nvcc():
@@ -79,9 +82,23 @@ def build(force=False, verbose=False):
     return LIB
 
 
+def build_probe(force=False):
+    """libhtr_probe.so: the benchmark's FP64 rate probe."""
+    os.makedirs(OUT_DIR, exist_ok=True)
+    root = os.path.dirname(HERE)
+    if not force and not _stale(PROBE_LIB, [PROBE_SRC, os.path.abspath(__file__)]):
+        return PROBE_LIB
+    tmp = PROBE_LIB + ".tmp"
+    subprocess.run([nvcc(), *ARCH, "-O3", "-std=c++17", "-Xcompiler", "-fPIC", "-shared",
+                    "-I" + os.path.join(root, "include"), PROBE_SRC, "-o", tmp], check=True)
+    os.replace(tmp, PROBE_LIB)
+    return PROBE_LIB
+
+
 def build_all(root, force=False):
-    """Package library plus the CPU checkers used by the tests."""
+    """Package library, the benchmark's probe, and the CPU checkers used by the tests."""
     build(force=force)
+    build_probe(force=force)
     import importlib.util
     spec = importlib.util.spec_from_file_location("_htr_oracle_build", os.path.join(root, "oracle", "build.py"))
     mod = importlib.util.module_from_spec(spec)

@@ -254,13 +254,20 @@ int step_prologue(const htr_fluid_view *v, htr_rect3 inner, htr_rect3 fb, const 
 // after the transport RHS of the start state is in Conserved_t: UpdateChemistry
 // over dt, then UpdatePrimitivesAndBCsFromConserved (primitives of the
 // interior, properties everywhere) and InitializeTemporaries.
+// skip_ghosts (the fused path, where `inner` is the whole grid): the
+// boundary ghost nodes of packed instances keep their imposed state.
 int implicit_chemistry_block(const htr_fluid_view *v, htr_rect3 inner, htr_rect3 fb, htr_mixture_t m, double dt,
-                             int *status_dev, htr_stream_t s) {
+                             int *status_dev, htr_stream_t s, unsigned skip_ghosts = 0) {
   const cudaStream_t cs = (cudaStream_t)s;
   int st;
-  if ((st = htr_UpdateChemistry(v, inner, dt, m, status_dev, s))) return st;
+  if ((st = check_common(v, m, inner))) return st;
   if ((st = with_mix(m, [&](const auto &mix) {
-         return cuda_status(htr::launch_primitive(*v, inner, mix, status_dev, cs), "primitive");
+         return cuda_status(htr::launch_update_chemistry(*v, inner, dt, mix, status_dev, cs, skip_ghosts),
+                            "UpdateChemistry");
+       })))
+    return st;
+  if ((st = with_mix(m, [&](const auto &mix) {
+         return cuda_status(htr::launch_primitive(*v, inner, mix, status_dev, cs, skip_ghosts), "primitive");
        })))
     return st;
   if ((st = htr_UpdatePropertiesFromPrimitive(v, fb, m, s))) return st;
@@ -270,12 +277,14 @@ int implicit_chemistry_block(const htr_fluid_view *v, htr_rect3 inner, htr_rect3
 // Three stages of the fused pipeline (one prepass, Euler KG + TENO faces,
 // diffusion faces and one per-cell update kernel per stage).
 int fused_step(const htr_fluid_view *v, htr_rect3 inner, htr_rect3 fb, const htr_step_params *p,
-               htr_mixture_t m, const htr::StageWorkspace &w, double *dt_used, int *status_dev, htr_stream_t s) {
+               htr_mixture_t m, const htr::StageWorkspace &w, double *dt_used, int *status_dev, htr_stream_t s,
+               const double *dt_cell = nullptr) {
   double dt = 0.0;
   // the fused stages read the sensors of the active directions only
   if (int st = step_prologue(v, inner, fb, p, m, &dt, s, active_dirs(inner))) return st;
   if (dt_used) *dt_used = dt;
   htr::StageParams sp;
+  sp.dt_cell = dt_cell;
   sp.scheme = p->scheme == HTR_SCHEME_HYBRID ? 0 : (p->scheme == HTR_SCHEME_SKEW ? 1 : 2);
   sp.kind = p->scheme == HTR_SCHEME_TENOA ? htr::kTENOA : (p->scheme == HTR_SCHEME_TENOLAD ? htr::kTENOLAD : htr::kTENO);
   sp.chemistry = p->explicitChemistry ? 1 : 0;
@@ -293,7 +302,7 @@ int fused_step(const htr_fluid_view *v, htr_rect3 inner, htr_rect3 fb, const htr
           return cuda_status(htr::launch_stage(*v, inner, fb, mix, w, sp, status_dev, (cudaStream_t)s), "stage");
         }))
       return st;
-    if (int st = implicit_chemistry_block(v, inner, fb, m, dt, status_dev, s)) return st;
+    if (int st = implicit_chemistry_block(v, inner, fb, m, dt, status_dev, s, active_dirs(inner))) return st;
     sp.mode = htr::kStageImplicit;
   }
   for (int stage = 1; stage <= 3; stage++) {
@@ -666,6 +675,22 @@ int htr_UpdateNSCBCGhostCellTimeDerivatives(const htr_fluid_view *v, htr_rect3 b
   return cuda_status(htr::launch_nscbc_time_derivatives(*v, bc, dt, (cudaStream_t)s), "nscbc time derivatives");
 }
 
+int htr_rk3_teno_face_counts(htr_rect3 inner, htr_mixture_t m, const void *workspace, size_t workspace_bytes,
+                             unsigned long long counts[3], htr_stream_t s) {
+  if (m == nullptr || counts == nullptr || !rect_ok(inner)) return fail(HTR_ERR_ARGUMENT, "null or bad argument%s");
+  htr::StageWorkspace w;
+  if (!htr::stage_workspace_carve(const_cast<void *>(workspace), workspace_bytes, inner, neq_of(m), w))
+    return fail(HTR_ERR_ARGUMENT, "workspace null or smaller than htr_rk3_workspace_bytes%s");
+  unsigned c[3] = {0u, 0u, 0u};
+  const cudaStream_t cs = (cudaStream_t)s;
+  int st;
+  if ((st = cuda_status(cudaMemcpyAsync(c, w.count, sizeof(c), cudaMemcpyDeviceToHost, cs), "teno counts")) ||
+      (st = cuda_status(cudaStreamSynchronize(cs), "teno counts sync")))
+    return st;
+  for (int d = 0; d < 3; d++) counts[d] = c[d];
+  return HTR_OK;
+}
+
 int htr_decision_counters(int enable, unsigned long long counts[HTR_DECISION_COUNTERS]) {
   if (counts == nullptr) return fail(HTR_ERR_ARGUMENT, "null counts%s");
   for (int k = 0; k < HTR_DECISION_COUNTERS; k++) counts[k] = 0ull;
@@ -827,6 +852,27 @@ int htr_rk3_step_ws(const htr_fluid_view *v, htr_rect3 inner, htr_rect3 fb, cons
     return fail(HTR_ERR_ARGUMENT, "workspace null or smaller than htr_rk3_workspace_bytes%s");
   if (reinterpret_cast<uintptr_t>(workspace) % 256 != 0) return fail(HTR_ERR_LAYOUT, "workspace not 256-byte aligned%s");
   return fused_step(v, inner, fb, p, m, w, dt_used, status_dev, s);
+}
+
+int htr_rk3_step_cells_ws(const htr_fluid_view *v, htr_rect3 inner, htr_rect3 fb, const htr_step_params *p,
+                          htr_mixture_t m, const double *dt_cell, void *workspace, size_t workspace_bytes,
+                          int *status_dev, htr_stream_t s) {
+  int st;
+  if (p == nullptr || dt_cell == nullptr) return fail(HTR_ERR_ARGUMENT, "null step parameters or step sizes%s");
+  if (p->cfl > 0.0) return fail(HTR_ERR_ARGUMENT, "per-cell step sizes take no CFL step size%s");
+  if (reinterpret_cast<uintptr_t>(dt_cell) % 8 != 0) return fail(HTR_ERR_LAYOUT, "dt_cell not 8-byte aligned%s");
+  if ((st = check_common(v, m, inner))) return st;
+  if ((st = check_step_fields(v, m))) return st;
+  for (int i = 0; i < 3; i++)
+    if (inner.lo[i] != fb.lo[i] || inner.hi[i] != fb.hi[i])
+      return fail(HTR_ERR_UNSUPPORTED, "the fused step needs a grid periodic in every direction (interior == bounds)%s");
+  htr::StageWorkspace w;
+  if (!htr::stage_workspace_carve(workspace, workspace_bytes, inner, neq_of(m), w))
+    return fail(HTR_ERR_ARGUMENT, "workspace null or smaller than htr_rk3_workspace_bytes%s");
+  if (reinterpret_cast<uintptr_t>(workspace) % 256 != 0) return fail(HTR_ERR_LAYOUT, "workspace not 256-byte aligned%s");
+  htr_step_params q = *p;
+  q.deltaTime = 1.0;  // unused: every cell takes its own step size
+  return fused_step(v, inner, fb, &q, m, w, nullptr, status_dev, s, dt_cell);
 }
 
 static int check_bc_params(const htr_fluid_view *v, htr_rect3 inner, htr_rect3 fb, const htr_bc_params *bc) {

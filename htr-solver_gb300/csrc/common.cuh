@@ -39,6 +39,10 @@ template <> HTR_D bool ld<bool>(const bool *p) {
 struct Box {
   long long lo[3], hi[3];
   HTR_HD long long size(int d) const { return hi[d] - lo[d] + 1; }
+  // dense index of p in the box, x fastest
+  HTR_HD long long dense(const long long *p) const {
+    return (p[0] - lo[0]) + size(0) * ((p[1] - lo[1]) + size(1) * (p[2] - lo[2]));
+  }
 };
 inline Box box(const htr_rect3 &r) {
   Box b;

@@ -14,6 +14,12 @@ struct EulerArgs {
   Fd<bool> sen;
   Box my, fb;
   double rk0, rk1, dt;
+  // per-cell step sizes (batched instances): the limiter's deltaTime of a
+  // face is (dtc[left cell] * dtc_c3) * dtc_h, the stage's dt * RK_C[3]
+  // (halved with implicit chemistry); null: dt above for every face
+  const double *dtc = nullptr;
+  double dtc_c3 = 1.0, dtc_h = 1.0;
+  HTR_D double face_dt(const long long *p) const { return dtc ? (dtc[my.dense(p)] * dtc_c3) * dtc_h : dt; }
 };
 
 enum { kSchemeHybrid = 0, kSchemeSkew = 1, kSchemeTeno = 2 };

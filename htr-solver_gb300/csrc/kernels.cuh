@@ -40,15 +40,17 @@ cudaError_t launch_properties(const htr_fluid_view &v, const htr_rect3 &my, cons
 template <class Mix>
 cudaError_t launch_conserved(const htr_fluid_view &v, const htr_rect3 &my, const Mix &mix,
                              cudaStream_t s);
+// skip_ghosts (bit d: direction d has more than one cell): leave boundary
+// ghost nodes alone (packed instances; 0 = every cell of my)
 template <class Mix>
 cudaError_t launch_primitive(const htr_fluid_view &v, const htr_rect3 &my, const Mix &mix,
-                             int *status, cudaStream_t s);
+                             int *status, cudaStream_t s, unsigned skip_ghosts = 0);
 template <class Mix>
 cudaError_t launch_spectral_radius(const htr_fluid_view &v, const htr_rect3 &my, const Mix &mix,
                                    double *result, cudaStream_t s);
 template <class Mix>
 cudaError_t launch_update_chemistry(const htr_fluid_view &v, const htr_rect3 &my, double dt,
-                                    const Mix &mix, int *status, cudaStream_t s);
+                                    const Mix &mix, int *status, cudaStream_t s, unsigned skip_ghosts = 0);
 
 // NSCBC boundary terms on the plane `bc` (dir 0..2, minus = the "Neg" side)
 template <class Mix>

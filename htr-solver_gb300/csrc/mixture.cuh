@@ -54,6 +54,7 @@ struct ConstPropDev {
   HTR_D double SpeedOfSound(double T, double g, double) const { return sqrt(g * R * T); }
   HTR_HD void Diffusivity(double *D, double, double, double, const double *) const { D[0] = 0.0; }
   HTR_HD void ProductionRates(double *w, double, double, double, const double *) const { w[0] = 0.0; }
+  HTR_HD void ProductionRatesRef(double *w, double, double, double, const double *) const { w[0] = 0.0; }
   HTR_HD double dpde(double rho, double g) const { return rho * (g - 1); }
   HTR_HD void dpdrhoi(double *d, double, double T, const double *) const { d[0] = R * T; }
 };
@@ -551,6 +552,73 @@ struct AirDev {
   }
 
   // --- kinetics (Reaction.inl, MultiComponent.inl:370-415) ------------------
+  // The reference's own operation order and function calls (pow, exp of
+  // -E/RT, the backward rate through exp(-ln Kc), concentrations Y rho / W),
+  // for the implicit solver: its adaptive step control amplifies any
+  // difference of rounding into a different sequence of steps, so the
+  // right-hand side it integrates is evaluated as the reference evaluates it
+  // (in a translation unit without FMA contraction).
+  HTR_D void ProductionRatesRef(double *w, double rhon, double Pn, double Tn, const double *Y) const {
+    const double T = Tn * TRef;
+    const double P = Pn * PRef;
+    const double rho = rhon * rhoRef;
+    double G[NS], C[NS];
+#pragma unroll
+    for (int i = 0; i < NS; i++) {
+      w[i] = 0.0;
+      C[i] = Y[i] * rho / W[i];
+      G[i] = FreeEnthalpy(i, T, 1.0 / T, log(T));
+    }
+#pragma unroll
+    for (int k = 0; k < 5; k++) {
+      const AirReac &r = reac[k];
+      double Kf = r.A;
+      if (r.useN) Kf *= pow(T, r.n);
+      if (r.useE) Kf *= exp(-r.EovR / T);
+      double a = 1.0;
+#pragma unroll
+      for (int i = 0; i < 2; i++)
+        if (i < r.nEd) a *= (r.nuE[i] == 1.0) ? C[r.ed[i]] : pow(C[r.ed[i]], r.nuE[i]);
+      double Kb = 0.0, b = 1.0;
+      if (r.backward) {
+        double sumNu = 0.0, sumNuG = 0.0;
+#pragma unroll
+        for (int i = 0; i < 2; i++)
+          if (i < r.nEd) {
+            sumNu -= r.nuE[i];
+            sumNuG -= r.nuE[i] * G[r.ed[i]];
+          }
+#pragma unroll
+        for (int i = 0; i < 2; i++)
+          if (i < r.nPd) {
+            sumNu += r.nuP[i];
+            sumNuG += r.nuP[i] * G[r.pd[i]];
+          }
+        const double lnKc = -sumNuG - sumNu * (log(T) + log(kRGAS / P));
+        Kb = Kf * exp(-lnKc);
+#pragma unroll
+        for (int i = 0; i < 2; i++)
+          if (i < r.nPd) b *= (r.nuP[i] == 1.0) ? C[r.pd[i]] : pow(C[r.pd[i]], r.nuP[i]);
+      }
+      double R = Kf * a - Kb * b;
+      if (r.nTb > 0) {
+        double c = P / (kRGAS * T);
+#pragma unroll
+        for (int i = 0; i < 5; i++)
+          if (i < r.nTb) c += C[r.tb[i]] * r.effm1[i];
+        R = c * (Kf * a - Kb * b);
+      }
+#pragma unroll
+      for (int i = 0; i < 2; i++)
+        if (i < r.nEd) w[r.ed[i]] -= r.nuE[i] * R;
+#pragma unroll
+      for (int i = 0; i < 2; i++)
+        if (i < r.nPd) w[r.pd[i]] += r.nuP[i] * R;
+    }
+#pragma unroll
+    for (int i = 0; i < NS; i++) w[i] *= W[i] * iwiRef;
+  }
+
   HTR_D void ProductionRates(double *w, double rhon, double Pn, double Tn, const double *Y) const {
     const double T = Tn * TRef;
     ProductionRatesT(w, rhon, Pn, T, 1.0 / T, log(T), Y);

@@ -81,6 +81,12 @@ struct StageParams {
   int stage;   // 1..3
   double dt;   // full step size
   int mode = kStageExplicit;
+  // optional per-cell step sizes (dense over the interior, x fastest) of
+  // independent instances packed into one grid; dt above is then unused.
+  // dtc_c3 / dtc_h: the factors launch_stage derives from the stage and mode
+  // (the limiter's deltaTime is (dt_cell * dtc_c3) * dtc_h)
+  const double *dt_cell = nullptr;
+  double dtc_c3 = 1.0, dtc_h = 1.0;
   // bit D set: direction D has more than one cell.  A one-cell periodic
   // direction contributes exactly zero to every flux difference (both faces
   // see the same cell), so its faces are not computed.

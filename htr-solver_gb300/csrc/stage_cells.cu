@@ -245,6 +245,8 @@ struct UpdateArgs {
   double c1, c2, c3, dt;
   int chemistry;
   int mode;        // StageMode
+  const double *dt_cell;  // per-cell step sizes (dense), or null: dt
+  double dt_h;            // factor of dt_cell (1/2 with implicit chemistry)
   int *status;
   double *tcache;  // [3][ncell]: T, log(T TRef), 1/(T TRef) of the last refresh
   // boundary step only
@@ -566,11 +568,12 @@ __global__ void __launch_bounds__(128) stage_update(const UpdateArgs A, const __
     double *cons = A.C.at(p);
     const double *old = A.Cold.at(p);
     double u_[NE];
+    const double dtu = A.dt_cell ? ld(&A.dt_cell[i]) * A.dt_h : A.dt;
 #pragma unroll
     for (int k = 0; k < NE; k++) {
       ctp[k] = ct[k];
       u_[k] = __dadd_rn(__dadd_rn(__dmul_rn(A.c1, ld(&old[k])), __dmul_rn(A.c2, cons[k])),
-                        __dmul_rn(__dmul_rn(A.c3, ct[k]), A.dt));
+                        __dmul_rn(__dmul_rn(A.c3, ct[k]), dtu));
       cons[k] = u_[k];
     }
     if constexpr (BC) {
@@ -691,13 +694,21 @@ cudaError_t launch_stage(const htr_fluid_view &v, const htr_rect3 &my, const htr
   // implicit chemistry; {0, 1} and dt/2 for the RHS of the implicit pre-step
   // (src/prometeo.rg:1363-1376, :1406-1419, UpdateDerivatives :498-512)
   double rk0 = c1, rk1 = c2, sdt = sp.dt * c3;
-  if (sp.mode == kStageImplicit) sdt = (sp.dt * c3) * 0.5;
+  StageParams ep = sp;
+  ep.dtc_c3 = c3;
+  ep.dtc_h = 1.0;
+  if (sp.mode == kStageImplicit) {
+    sdt = (sp.dt * c3) * 0.5;
+    ep.dtc_h = 0.5;
+  }
   if (sp.mode == kStageRhsOnly) {
     rk0 = 0.0;
     rk1 = 1.0;
     sdt = sp.dt * 0.5;
+    ep.dtc_c3 = 1.0;
+    ep.dtc_h = 0.5;
   }
-  if ((e = launch_stage_euler(v, my, fb, mix, w, H, sp, rk0, rk1, sdt, s, ev ? ev + 1 + kKgZ : nullptr)) !=
+  if ((e = launch_stage_euler(v, my, fb, mix, w, H, ep, rk0, rk1, sdt, s, ev ? ev + 1 + kKgZ : nullptr)) !=
       cudaSuccess)
     return e;
   const htr_field *ms[3] = {&v.dcsi_s, &v.deta_s, &v.dzet_s};
@@ -769,6 +780,8 @@ cudaError_t launch_stage(const htr_fluid_view &v, const htr_rect3 &my, const htr
   U.dt = sp.mode == kStageImplicit ? sp.dt * 0.5 : sp.dt;
   U.chemistry = sp.mode == kStageExplicit ? sp.chemistry : 0;
   U.mode = sp.mode;
+  U.dt_cell = sp.dt_cell;
+  U.dt_h = sp.mode == kStageImplicit ? 0.5 : 1.0;
   U.status = status;
   U.tcache = w.tcache;
   U.Xp = fd<double>(v.MolarFracs_profile);

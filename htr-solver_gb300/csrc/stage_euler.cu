@@ -49,7 +49,7 @@ HTR_D void teno_face_at(const StageTenoArgs &A, const Mix &mix, const long long 
 #pragma unroll
     for (int i = 0; i < NE; i++) F[i] = 0.0;
   } else {
-    const double lim_f = a.dt * (ld(a.me.at(p)) + ld(a.me.at(q)));
+    const double lim_f = a.face_dt(p) * (ld(a.me.at(p)) + ld(a.me.at(q)));
     ef.template teno_flux<KIND>(F, p, t, lim_f);
   }
   const long long nf = A.g.nf[D];
@@ -157,6 +157,9 @@ cudaError_t launch_stage_euler(const htr_fluid_view &v, const htr_rect3 &my, con
   StageTenoArgs T;
   for (int D = 0; D < 3; D++) {
     T.e[D] = euler_args(v, my, fb, D, rk0, rk1, sdt);
+    T.e[D].dtc = p.dt_cell;
+    T.e[D].dtc_c3 = p.dtc_c3;
+    T.e[D].dtc_h = p.dtc_h;
     T.fe[D] = w.fe[D];
   }
   T.g = g;

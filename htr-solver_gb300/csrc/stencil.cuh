@@ -59,6 +59,28 @@ HTR_HD bool ghost_node(int t) { return t == L_S || t == R_S || t == L_C || t == 
 // A face whose left node is a right-boundary ghost lies outside the domain.
 HTR_HD bool outside_face(int t) { return t == R_S || t == R_C; }
 
+// Per-cell kernels run over a whole grid of packed instances skip the
+// boundary ghost nodes (in any direction with more than one cell).
+struct GhostSkip {
+  Fd<int> nt[3];
+  unsigned active = 0;  // 0: skip nothing
+  HTR_D bool at(const long long *p) const {
+    bool g = false;
+#pragma unroll
+    for (int d = 0; d < 3; d++)
+      if (active & (1u << d)) g = g || ghost_node(ld(nt[d].at(p)));
+    return g;
+  }
+};
+inline GhostSkip ghost_skip(const htr_fluid_view &v, unsigned active) {
+  GhostSkip g;
+  g.nt[0] = fd<int>(v.nType_x);
+  g.nt[1] = fd<int>(v.nType_y);
+  g.nt[2] = fd<int>(v.nType_z);
+  g.active = active;
+  return g;
+}
+
 struct NodeDev {
   int8_t off[5];
   int8_t kgOrder;

@@ -1,7 +1,7 @@
-// Device rate probes used by the benchmark to state its FP64 roofline: the
-// GB300 FP64 rate is not a published constant of this pool, so bench.py
-// measures it with a dependent-chain DFMA loop (8 independent chains per
-// thread, enough blocks to fill every SM).
+// FP64 rate probe of the benchmark (not part of the library): the FP64 peak
+// of the device is measured with a dependent-chain DFMA loop (8 independent
+// chains per thread, enough blocks to fill every SM) and used as the
+// denominator of the FP64 roofline fractions.  Built into libhtr_probe.so.
 #include <cuda_runtime.h>
 
 #include "htr_rhs.h"

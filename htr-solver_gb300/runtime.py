@@ -59,6 +59,10 @@ def lib():
                                          C.POINTER(htr_step_params), C.POINTER(htr_bc_params), C.c_void_p,
                                          C.c_void_p, C.c_size_t, C.POINTER(C.c_double), C.c_void_p, C.c_void_p]
         l.htr_rk3_step_bc_ws.restype = C.c_int
+        l.htr_rk3_step_cells_ws.argtypes = [C.POINTER(abi.htr_fluid_view), abi.htr_rect3, abi.htr_rect3,
+                                            C.POINTER(htr_step_params), C.c_void_p, C.c_void_p, C.c_void_p,
+                                            C.c_size_t, C.c_void_p, C.c_void_p]
+        l.htr_rk3_step_cells_ws.restype = C.c_int
         l.htr_rk3_static_scratch_bytes.argtypes = []
         l.htr_rk3_static_scratch_bytes.restype = C.c_size_t
         for name, args in EXTRA_PROTOTYPES.items():
@@ -138,6 +142,25 @@ def rk3_step(fluid, mixh, scheme="Hybrid", vorticity_scale=1.0, cfl=0.0, dt=0.0,
                             status_dev, stream_handle(stream))
         abi.check(l, st, "htr_rk3_step")
     return used.value
+
+
+def rk3_step_cells(fluid, mixh, dt_cell, scheme="Hybrid", vorticity_scale=1.0, chemistry=True, stream=None,
+                   status_dev=None, workspace=None, implicit=False):
+    """One SSP-RK3 step of a device grid of packed independent instances,
+    each cell advancing by its own step size dt_cell (a device float64 tensor
+    of one value per cell, shaped like the grid, x fastest):
+    htr_rk3_step_cells_ws."""
+    l = lib()
+    if dt_cell.dtype.itemsize != 8 or not dt_cell.is_contiguous() or dt_cell.numel() != fluid.ncells:
+        raise abi.HtrError("dt_cell must be a contiguous float64 tensor with one value per cell")
+    p = htr_step_params(SCHEMES[scheme], vorticity_scale, 0.0, 0.0, 1 if chemistry else 0, 1 if implicit else 0)
+    v = fluid.view()
+    inner = fluid.interior()
+    nb = l.htr_rk3_workspace_bytes(inner, mixh)
+    ws = (workspace or _workspace).get(nb, fluid.device)
+    st = l.htr_rk3_step_cells_ws(C.byref(v), inner, fluid.bounds(), C.byref(p), mixh, C.c_void_p(dt_cell.data_ptr()),
+                                 C.c_void_p(ws), nb, status_dev, stream_handle(stream))
+    abi.check(l, st, "htr_rk3_step_cells_ws")
 
 
 def stable_dt(fluid, mixh, cfl=0.8, chemistry=True, stream=None):

@@ -17,6 +17,8 @@ density ratio 1-10, temperatures 300-3000 K, gas at rest.
 """
 import math
 
+import ctypes as C
+
 import numpy as np
 
 from . import abi
@@ -222,6 +224,55 @@ def pack(fluids):
     strip.meta = dict(fluids[0].meta)
     strip.meta.update(workload="shock_tube_strip", bnum=(0, 0, 0), tubes=len(fluids))
     return strip, offs[:-1]
+
+
+def cell_dt(offs, widths, dts):
+    """Step size of every cell of a strip (ghost nodes included): the dt of
+    the tube the cell belongs to.  widths[k] = cells of tube k with its two
+    ghosts."""
+    n = int(offs[-1] + widths[-1])
+    out = np.empty(n)
+    for o, w, d in zip(offs, widths, dts):
+        out[int(o):int(o) + int(w)] = d
+    return out
+
+
+def strip_dts(strip_dev, offs, widths, gh, cfl=0.8, chemistry=False, lib=None):
+    """Each tube's own step size (CFL `cfl` over its own spectral radius;
+    with chemistry also at most half its fastest chemical time scale), as one
+    run of the reference computes it per simulation
+    (src/prometeo.rg:1153-1172).  Device strip in, list of floats out."""
+    import torch
+
+    from . import runtime
+    from .fluid import Fluid
+    l = lib or runtime.lib()
+    dts = []
+    for o, w in zip(offs, widths):
+        L = int(w) - 2
+        v, fb, inner = tube_view(strip_dev.view(), int(o), L)
+        out = torch.zeros(1, dtype=torch.float64, device=strip_dev.device)
+        abi.check(l, l.htr_CalculateMaxSpectralRadius(C.byref(v), inner, gh, C.cast(C.c_void_p(out.data_ptr()),
+                                                                                    C.POINTER(C.c_double)),
+                                                      runtime.stream_handle()), "spectral radius")
+        dts.append(out)
+    torch.cuda.synchronize()
+    dts = [cfl / d.item() for d in dts]
+    if chemistry:
+        v = strip_dev.view()
+        abi.check(l, l.htr_InitializeTimeDerivatives(C.byref(v), strip_dev.bounds(), 0, gh, runtime.stream_handle()),
+                  "init")
+        abi.check(l, l.htr_AddChemistrySources(C.byref(v), strip_dev.interior(), gh, runtime.stream_handle()),
+                  "chem")
+        torch.cuda.synchronize()
+        ns = strip_dev.nspec
+        w_ = strip_dev["Conserved_t"][0, 0, :, :ns].abs()
+        rhoi = strip_dev["Conserved"][0, 0, :, :ns]
+        sig = rhoi > 1e-3 * strip_dev["rho"][0, 0, :, None]
+        tau = torch.where(sig, rhoi / w_.clamp_min(1e-300), torch.full_like(rhoi, float("inf"))).min(dim=1).values
+        tau = tau.cpu().numpy()
+        dts = [min(d, 0.5 * float(tau[int(o) + 1:int(o) + int(w) - 1].min())) for d, o, w in zip(dts, offs, widths)]
+    return dts
 
 
 def unpack(strip, offs, lengths):

@@ -352,6 +352,18 @@ int htr_rk3_step_ws(const htr_fluid_view *view, htr_rect3 interior, htr_rect3 fl
                     const htr_step_params *params, htr_mixture_t mix, void *workspace,
                     size_t workspace_bytes, double *dt_used, int *status_dev, htr_stream_t stream);
 
+/* No reference counterpart: htr_rk3_step_ws with one step size per cell, for
+ * many independent instances packed into one grid (the batched form: tubes
+ * end to end in a strip, separated by their boundary ghost nodes).
+ * `dt_cell` is device memory of one double per interior cell, dense with x
+ * fastest; the cells of one instance share that instance's step size, so
+ * each instance advances exactly as htr_rk3_step_ws would advance it alone
+ * with its own deltaTime (RK update and positivity-limiter deltaTime per
+ * cell).  params->cfl must be <= 0; params->deltaTime is not used. */
+int htr_rk3_step_cells_ws(const htr_fluid_view *view, htr_rect3 interior, htr_rect3 fluid_bounds,
+                          const htr_step_params *params, htr_mixture_t mix, const double *dt_cell,
+                          void *workspace, size_t workspace_bytes, int *status_dev, htr_stream_t stream);
+
 /* --- fused time step of a grid with boundary conditions --------------------
  * Not a reference task.  One SSP-RK3 step of the reference driver
  * (src/prometeo.rg:1342-1486, UpdateDerivatives :480-606,
@@ -401,9 +413,12 @@ int htr_rk3_step_bc_ws(const htr_fluid_view *view, htr_rect3 interior, htr_rect3
  * module holding it loads there and kept until the process exits.
  * htr_load_mixture loads that module and resolves the array's address for
  * its current device, so once a mixture was loaded on the device the call
- * allocates no device or host memory and loads nothing; on a device where
- * no mixture was loaded, the first call does that set-up (make it before
- * any stream capture).  After a cudaDeviceReset, load the mixture again.
+ * allocates no device or host memory; on a device where no mixture was
+ * loaded, the first call does that set-up (make it before any stream
+ * capture).  (Under CUDA's lazy module loading the first launch of each of
+ * the library's kernels in a process loads that kernel's module, whichever
+ * entry point launches it; CUDA_MODULE_LOADING=EAGER loads them all when the
+ * library loads.)  After a cudaDeviceReset, load the mixture again.
  * Grids whose workspace (htr_rk3_workspace_bytes) exceeds the scratch are
  * rejected with HTR_ERR_UNSUPPORTED before any launch.  Calls share the
  * scratch of their device: run them on one stream (or serialise them),
@@ -433,6 +448,14 @@ int htr_rk3_get_tuning(htr_stage_tuning *tuning);
 int htr_rk3_stage_profile(const htr_fluid_view *view, htr_rect3 interior, htr_rect3 fluid_bounds,
                           const htr_step_params *params, htr_mixture_t mix, void *workspace,
                           size_t workspace_bytes, float *ms_out, htr_stream_t stream);
+
+/* Diagnostic, no counterpart in the reference: the numbers of faces of
+ * directions X, Y, Z that the last fused hybrid stage run on `workspace`
+ * (htr_rk3_step_ws, htr_rk3_stage_profile) reconstructed with TENO (the
+ * shock-sensor-rejected faces of its TENO queues); waits for `stream`.
+ * TENO-only schemes reconstruct every face and queue none. */
+int htr_rk3_teno_face_counts(htr_rect3 interior, htr_mixture_t mix, const void *workspace, size_t workspace_bytes,
+                             unsigned long long counts[3], htr_stream_t stream);
 
 /* Diagnostic counters, no counterpart in the reference.  The kernels decide
  * TENO stencil selections and shock sensors first with single-precision

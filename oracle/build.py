@@ -15,7 +15,15 @@ import sys
 
 HERE = os.path.dirname(os.path.abspath(__file__))
 ROOT = os.path.dirname(HERE)
-REF_SRC = "/root/reference/src"
+
+
+def ref_src():
+    """The reference's src/ directory: $HTR_REF_SRC, else src/ of a checkout of
+    the reference named `reference` beside this repository."""
+    env = os.environ.get("HTR_REF_SRC")
+    if env:
+        return env
+    return os.path.join(os.path.dirname(ROOT), "reference", "src")
 
 
 def _newer(target, sources):
@@ -44,10 +52,11 @@ def build_port(force=False):
 
 def build_ref(force=False):
     """Build the reference oracle if its sources are present; return True if built."""
-    if not os.path.isdir(REF_SRC) or shutil.which("make") is None:
+    src = ref_src()
+    if not os.path.isdir(src) or shutil.which("make") is None:
         return False
     jobs = str(max(1, min(16, os.cpu_count() or 1)))
-    cmd = ["make", "-s", "-C", os.path.join(HERE, "ref"), "-j", jobs, "REF_SRC=" + REF_SRC]
+    cmd = ["make", "-s", "-C", os.path.join(HERE, "ref"), "-j", jobs, "REF_SRC=" + os.path.abspath(src)]
     if force:
         cmd.insert(1, "-B")
     subprocess.run(cmd, check=True)

@@ -1,7 +1,12 @@
-"""Size-independent properties of the hot path at the benchmark's full size,
-the 256^3 periodic box of 5-species reacting air, where the CPU oracle is
-too slow to compare point by point (the point-by-point parity runs on the
-smaller grids of the other test files):
+"""The hot path at the benchmark's full sizes.
+
+Point by point against the CPU oracle (the port on all host cores, about 20
+s per step): one fused SSP-RK3 step of the 256^3 periodic box of 5-species
+reacting air (hybrid scheme, diffusion, explicit chemistry) and one fused
+step of the 512 x 192 x 128 TENO-LAD boundary layer, from the same state,
+within the pointwise bar of util.check.
+
+Size-independent properties of the same grids:
 
 - conservation: on a periodic uniform grid every face flux enters its two
   cells with opposite signs, so one RHS evaluation (hybrid Euler flux with
@@ -37,6 +42,89 @@ def box():
     workloads.derive_state(lib, dev, gh, runtime.stream_handle())
     torch.cuda.synchronize()
     return dev, gh
+
+
+def _port():
+    import os
+
+    import oracle
+    port = oracle.port_lib()
+    port.htr_oracle_set_threads(os.cpu_count() or 1)
+    return port
+
+
+STATE = ("Conserved", "temperature", "pressure", "velocity", "MolarFracs", "MassFracs", "rho", "mu", "lam", "Di",
+         "SoS")
+
+
+@pytest.mark.gpu
+def test_fullsize_step_matches_the_oracle(box):
+    """One fused SSP-RK3 step of the 256^3 benchmark box at the benchmark's
+    step size against the oracle driver's step on the port, from the same
+    (device-derived) state: sensors bit for bit, every state field within
+    the pointwise bar."""
+    import numpy as np
+    import torch
+
+    import oracle
+    from htr_gb300 import abi, runtime, workloads
+    from tests import util
+    base, gh = box
+    dev = base.copy()
+    dt = runtime.stable_dt(dev, gh, cfl=0.8, chemistry=True)
+    host = base.to_host()
+    port = _port()
+    eos = abi.HTR_EOS_AIRMIX
+    hp = oracle.load_mixture(port, eos, workloads.make_mixture_struct(port, eos, workloads.AIR_REF))
+    runtime.rk3_step(dev, gh, dt=dt, chemistry=True)
+    oracle.step(port, host, hp, scheme="Hybrid", dt=dt, chemistry=True)
+    torch.cuda.synchronize()
+    out = dev.to_host()
+    for d in "XYZ":
+        a, b = out[f"shockSensor{d}"], host[f"shockSensor{d}"]
+        assert np.array_equal(a, b), f"{(a != b).sum()} sensor{d} flags differ"
+        assert 0 < b.sum() < b.size
+    for name in STATE:
+        info = util.check(out[name], host[name], name)
+        print(f"{name}: pointwise error / bound {info['ratio']:.3e}, normwise {info['normwise']:.3e}")
+
+
+@pytest.mark.gpu
+def test_boundary_layer_fullsize_step_matches_the_oracle():
+    """One fused step of the 512 x 192 x 128 TENO-LAD boundary layer (config
+    3: NSCBC inflow/outflow in x, isothermal wall and outflow in y, periodic
+    z, explicit chemistry) against the oracle's boundary-layer step on the
+    port, from the same state: every state field within the pointwise bar."""
+    import torch
+
+    import oracle
+    from htr_gb300 import runtime, wall, workloads
+    from tests import util
+    lib = runtime.lib()
+    host = wall.boundary_layer(num=(512, 192, 128), seed=77)
+    g, bc = host.meta["grid"], host.meta["bc"]
+    m = workloads.make_mixture_struct(lib, host.meta["eos"], host.meta["mix"])
+    gh = runtime.load_mixture(host.meta["eos"], m)
+    dev = host.to_device("cuda:0")
+    g.fill(dev, lib)
+    workloads.derive_state(lib, dev, gh, runtime.stream_handle())
+    mach = torch.zeros(1, dtype=torch.float64, device="cuda:0")
+    dt = wall.BoundaryRun(lib, dev, gh, bc, stream=runtime.stream_handle(), max_mach_buffer=mach).spectral_dt(0.8)
+    torch.cuda.synchronize()
+    ref = dev.to_host()
+    ref.meta = dict(host.meta)
+    del host
+    port = _port()
+    hp = oracle.load_mixture(port, ref.meta["eos"], workloads.make_mixture_struct(port, ref.meta["eos"],
+                                                                                  ref.meta["mix"]))
+    wall.FusedBoundaryRun(dev, gh, bc).step(dt)
+    oracle.boundary_layer_step(port, ref, hp, dt, bc["xNeg"][1]["P"], bc["xPos"][1]["P"],
+                               (bc["xPos"][1]["LengthScale"], bc["yPos"][1]["LengthScale"]))
+    torch.cuda.synchronize()
+    out = dev.to_host()
+    for name in STATE + ("dudtBoundary", "dTdtBoundary"):
+        info = util.check(out[name], ref[name], name)
+        print(f"{name}: pointwise error / bound {info['ratio']:.3e}, normwise {info['normwise']:.3e}")
 
 
 @pytest.mark.gpu

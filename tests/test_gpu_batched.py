@@ -75,6 +75,59 @@ def test_batched_strip_equals_per_tube_oracle(eos):
 
 
 @pytest.mark.gpu
+@pytest.mark.parametrize("implicit", [False, True], ids=["explicit", "implicit"])
+@pytest.mark.parametrize("eos", [abi.HTR_EOS_CONSTPROPMIX, abi.HTR_EOS_AIRMIX])
+def test_batched_strip_per_tube_dt(eos, implicit):
+    """Each tube with its own step size (CFL 0.8 over its own spectral radius,
+    for air also at most half its fastest chemical time scale, as one run of
+    the reference computes dt per simulation): one fused step of the strip
+    with per-cell step sizes (htr_rk3_step_cells_ws) equals, tube by tube,
+    the oracle's step of that tube alone with its own dt.  With implicit
+    chemistry (air), the tube's whole CFL step, far above its chemical time."""
+    import torch
+    if implicit and eos != abi.HTR_EOS_AIRMIX:
+        pytest.skip("implicit chemistry needs a reacting mixture")
+    port = oracle.port_lib()
+    insts = _groups()[eos]
+    chem = eos == abi.HTR_EOS_AIRMIX
+    fls = [tubes.tube_fluid(i) for i in insts]
+    m = workloads.make_mixture_struct(port, eos, fls[0].meta["mix"])
+    h = oracle.load_mixture(port, eos, m)
+    for f in fls:
+        workloads.derive_state(port, f, h)
+    strip, offs = tubes.pack([f.copy() for f in fls])
+    gh = runtime.load_mixture(eos, m)
+    dev = strip.to_device("cuda")
+    widths = [f.nx for f in fls]
+    dts = tubes.strip_dts(dev, offs, widths, gh, cfl=0.8, chemistry=chem and not implicit)
+    assert len(set(dts)) == len(dts)  # every tube its own step
+    ref, spreads = [], []
+    for f, dt in zip(fls, dts):
+        run = lambda g, dt=dt: oracle.step(port, g, h, dt=dt, chemistry=chem, bnum=(1, 0, 0), implicit=implicit)
+        if implicit:
+            r, sp = util.ulp_spread(run, f, FIELDS)
+        else:
+            r, sp = f.copy(), None
+            run(r)
+        ref.append(r)
+        spreads.append(sp)
+    dt_cell = torch.tensor(tubes.cell_dt(offs, widths, dts), dtype=torch.float64, device="cuda")
+    status = torch.zeros(1, dtype=torch.int32, device="cuda")
+    runtime.rk3_step_cells(dev, gh, dt_cell, chemistry=chem, implicit=implicit,
+                           status_dev=C.c_void_p(status.data_ptr()))
+    torch.cuda.synchronize()
+    assert status.item() == 0
+    out = dev.to_host()
+    for k, (o, f, sp) in enumerate(zip(offs, ref, spreads)):
+        tube = {name: a[:, :, o:o + f.nx] for name, a in out.arrays.items()}
+        if sp is None:
+            _check(tube, f.arrays, f"tube {k}")
+        else:
+            for name in FIELDS:
+                util.check_within_spread(tube[name], f[name], name, sp[name])
+
+
+@pytest.mark.gpu
 @pytest.mark.parametrize("eos", [abi.HTR_EOS_CONSTPROPMIX, abi.HTR_EOS_AIRMIX])
 def test_plain_per_tube_task_path(eos):
     import torch

@@ -49,12 +49,18 @@ def test_static_scratch_equals_workspace_path(kind):
 def _measure_in_this_process():
     """Free device memory around the first two static steps of a process
     that has loaded its mixture (htr_load_mixture is the set-up point that
-    loads the scratch's module)."""
+    loads the scratch's module).  One step through the caller-workspace
+    entry point runs first: under CUDA's lazy module loading the first launch
+    of each kernel in a process loads that kernel's module, whichever entry
+    point launches it."""
     import torch
     shape, dt, chem = CASES["air"]
     fl, h, m = util.make_state(oracle.port_lib(), "air", shape, seed=4)
     dev = fl.to_device("cuda")
     gh = runtime.load_mixture(fl.meta["eos"], m)
+    warm = dev.copy()
+    ws = runtime.Workspace()
+    runtime.rk3_step(warm, gh, dt=dt, chemistry=chem, fused=True, workspace=ws)
     torch.cuda.synchronize()
     before_torch = torch.cuda.memory_allocated()
     free_before, _ = torch.cuda.mem_get_info()

@@ -102,6 +102,52 @@ def check_fields(got, want, names, tol=RHS_REL_TOL):
         check(got[n], want[n], n, tol)
 
 
+def ulp_spread(run, fl, fields, perturb=("Conserved", "Conserved_t")):
+    """The spread of an algorithm's own results under rounding-level changes
+    of its inputs: `run` (an oracle computation, in place on a host Fluid) on
+    `fl` and on copies with each field of `perturb` moved by one ulp
+    (np.nextafter towards +inf).  Returns (the unperturbed result, {field:
+    per-component largest |change|})."""
+    base = fl.copy()
+    run(base)
+    spread = {}
+    for name in perturb:
+        f = fl.copy()
+        f[name] = np.nextafter(fl[name], np.inf)
+        run(f)
+        for out in fields:
+            a, b = np.asarray(f[out], dtype=np.float64), np.asarray(base[out], dtype=np.float64)
+            if a.ndim == 3:
+                a, b = a[..., None], b[..., None]
+            d = np.abs(a - b).reshape(-1, a.shape[-1]).max(axis=0)
+            spread[out] = np.maximum(spread.get(out, 0.0), d)
+    return base, spread
+
+
+def check_within_spread(got, want, name, spread, k=10.0, tol=RHS_REL_TOL):
+    """`check` with the absolute floor raised, per component, to k times the
+    reference algorithm's own one-ulp spread (ulp_spread): for adaptive
+    solvers whose step sequence, and so whose result at the level of their
+    error tolerance, changes with the rounding of their inputs.  Logs the
+    ratio of the largest difference to the spread."""
+    a = np.asarray(got, dtype=np.float64)
+    b = np.asarray(want, dtype=np.float64)
+    if a.ndim == 3:
+        a, b = a[..., None], b[..., None]
+    a2, b2 = a.reshape(-1, a.shape[-1]), b.reshape(-1, b.shape[-1])
+    scale = np.abs(b2).max(axis=0)
+    floor = np.maximum(np.maximum(FLOOR_REL_STATE * scale, k * np.asarray(spread)), 1e-300)
+    d = np.abs(a2 - b2)
+    r = d / np.maximum(tol * np.abs(b2), floor[None, :])
+    dmax = d.max(axis=0)
+    info = dict(field=name, ratio=float(r.max()), max_abs_diff=float(dmax.max()),
+                spread=[float(x) for x in np.atleast_1d(spread)],
+                diff_over_spread=float((dmax / np.maximum(np.asarray(spread), 1e-300)).max()), k=k)
+    log_record(spread_check=info)
+    assert r.max() <= 1.0, f"{name}: beyond {k} x the reference's own one-ulp spread {info}"
+    return info
+
+
 def make_state(lib, kind, n, seed=0):
     """Seeded state built (properties + conserved) by `lib`; returns fluid, mixture handle, struct."""
     if kind == "tg":
