@@ -597,6 +597,76 @@ def run_wall(args, device, runtime, lib):
             **({"cpu": cpu} if cpu else {})}
 
 
+def run_config1(args, device, runtime, lib, steps=200):
+    """The plain small configuration: 32^3 periodic Taylor-Green box of a
+    calorically perfect gas (gamma 1.4, Pr 0.71, power-law viscosity), +-1 %
+    seeded perturbations, hybrid scheme with the Ducros / TENO-A sensor,
+    viscous diffusion, SSP-RK3 at CFL 0.8 (dt fixed from the initial state).
+    GPU: the fused step (a 32^3 grid is launch-latency bound, so the steps
+    are replayed from one CUDA graph) timed over `steps` steps; against HBM
+    at the reference layout's 263 B per single-species cell-update.  CPU:
+    the port on all host threads, one step of the same grid and state, and
+    the pointwise comparison of that step with the GPU's."""
+    import torch
+
+    import oracle
+    fl = workloads.taylor_green(32, seed=0)
+    eos = fl.meta["eos"]
+    m = workloads.make_mixture_struct(lib, eos, fl.meta["mix"])
+    gh = runtime.load_mixture(eos, m)
+    dev = fl.to_device(device)
+    workloads.derive_state(lib, dev, gh, runtime.stream_handle())
+    dt = runtime.stable_dt(dev, gh, cfl=0.8, chemistry=False)
+    start = dev.copy()
+    ws = runtime.Workspace()
+    stream = torch.cuda.current_stream()
+    side = torch.cuda.Stream()
+    side.wait_stream(stream)
+    with torch.cuda.stream(side):
+        runtime.rk3_step(dev, gh, dt=dt, chemistry=False, stream=side, workspace=ws)
+    stream.wait_stream(side)
+    graph = torch.cuda.CUDAGraph()
+    with torch.cuda.graph(graph, stream=side, capture_error_mode="relaxed"):
+        runtime.rk3_step(dev, gh, dt=dt, chemistry=False, stream=side, workspace=ws)
+    for _ in range(3):
+        graph.replay()
+    torch.cuda.synchronize()
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    e0.record(stream)
+    for _ in range(steps):
+        graph.replay()
+    e1.record(stream)
+    e1.synchronize()
+    ms = e0.elapsed_time(e1) / steps
+    value = 3.0 * dev.ncells / (ms * 1e-3)
+    peak, src = hbm_peak()
+    gbs = 263.0 * value / 1e9
+    # one step from the same start state on the GPU and on the port
+    port = oracle.port_lib()
+    threads = os.cpu_count() or 1
+    port.htr_oracle_set_threads(threads)
+    host = start.to_host()
+    hp = oracle.load_mixture(port, eos, workloads.make_mixture_struct(port, eos, fl.meta["mix"]))
+    t0 = time.perf_counter()
+    oracle.step(port, host, hp, scheme="Hybrid", dt=dt, chemistry=False)
+    el = time.perf_counter() - t0
+    runtime.rk3_step(start, gh, dt=dt, chemistry=False)
+    torch.cuda.synchronize()
+    ratio = pointwise_ratio(start["Conserved"], host["Conserved"])
+    flags = all(torch.equal(start[f"shockSensor{d}"].cpu(), torch.from_numpy(host[f"shockSensor{d}"])) for d in "XYZ")
+    return {"metric": METRIC, "value": value, "unit": UNIT, "ms_per_step": ms, "steps": steps, "dt": dt,
+            "roofline": {"bound": "hbm", "achieved": gbs, "peak": peak, "unit": "GB/s", "frac": gbs / peak,
+                         "bytes_per_cell_update": 263, "peak_source": src + " (MEASURED_PEAKS.json)",
+                         "note": "whole step at the reference layout's compulsory bytes; a 32^3 grid "
+                                 "(33k cells) cannot fill 152 SMs, the steps are latency bound"},
+            "cpu_baseline": {"value": 3.0 * host.ncells / el, "unit": UNIT, "cores": threads, "kind": "port",
+                             "seconds": el, "sample": "one SSP-RK3 step of the same 32^3 grid and state"},
+            "parity": {"conserved_pointwise_ratio": ratio, "sensors_bit_exact": flags},
+            "config": {"workload": "32^3 periodic Taylor-Green, calorically perfect gas (ConstPropMix), "
+                                   "hybrid TENO-A/KG + viscous diffusion, SSP-RK3 at CFL 0.8",
+                       "form": "fused step, one CUDA graph replayed per step"}}
+
+
 def run_restart(dev, device, reps=3):
     """Restart dump and load of the benchmark state through
     include/htr_restart.h (2 tiles plus master.hdf in a temporary
@@ -737,6 +807,12 @@ def run_gpu(args):
             "gpu_launches": args.steps * (3 + 3 * 11),
             "clocks": clk,
         }
+        if args.config1:
+            try:
+                log("config 1: 32^3 Taylor-Green")
+                result["config1"] = run_config1(args, device, runtime, lib)
+            except Exception as exc:
+                result["config1"] = {"error": f"{type(exc).__name__}: {exc}"}
         if args.tubes > 0:
             try:
                 log("batched tubes")
@@ -859,6 +935,7 @@ def main():
     p.add_argument("--wall", default="512,192,128", help="boundary-layer interior cells nx,ny,nz ('' skips)")
     p.add_argument("--wall-steps", type=int, default=10)
     p.add_argument("--no-restart", dest="restart", action="store_false", help="skip the restart dump/load timing")
+    p.add_argument("--no-config1", dest="config1", action="store_false", help="skip the 32^3 Taylor-Green case")
     args = p.parse_args()
     res = run_reference(args) if args.impl == "reference" else run_gpu(args)
     if res is not None:

@@ -144,54 +144,46 @@ __global__ void __launch_bounds__(KGTile<D, SX>::THREADS) euler_kg_faces(const S
           }
           const int order = kNode[t].kgOrder;
           const double kgc[3] = {kNode[t].kg[0], kNode[t].kg[1], kNode[t].kg[2]};
-          double rv[3][3];
+          // The split form sums, over the stencil pairs (a, b) of each order
+          // l, kg_l (rho_a + rho_b)(v_a + v_b)(phi_a + phi_b) / 4.  Collected
+          // per stencil point, every transported scalar's flux is one dot
+          // product sum_k cw[k] phi_k, with cw[k] the pair weights
+          // kg_l (rho_a + rho_b)(v_a + v_b) / 4 of the pairs holding point k,
+          // computed once per face (the pressure term likewise with cp[k] =
+          // sum of kg_l).  Same value, regrouped: rounding only.
+          double cw[6] = {0.0, 0.0, 0.0, 0.0, 0.0, 0.0}, cp[6] = {0.0, 0.0, 0.0, 0.0, 0.0, 0.0};
 #pragma unroll
           for (int l2 = 0; l2 < 3; l2++)
 #pragma unroll
             for (int m = 0; m < 3; m++)
-              if (m <= l2 && l2 < order)
-                rv[l2][m] = (r_[2 - m] + r_[2 - m + l2 + 1]) * (v_[2 - m] + v_[2 - m + l2 + 1]);
-          auto triple = [&](int q) {
+              if (m <= l2 && l2 < order) {
+                const int a0 = 2 - m, b0 = 2 - m + l2 + 1;
+                const double w = (0.25 * kgc[l2]) * ((r_[a0] + r_[b0]) * (v_[a0] + v_[b0]));
+                cw[a0] += w;
+                cw[b0] += w;
+                cp[a0] += kgc[l2];
+                cp[b0] += kgc[l2];
+              }
+          auto dot = [&](int q) {
             double flux = 0.0;
 #pragma unroll
-            for (int l2 = 0; l2 < 3; l2++) {
-              if (l2 < order) {
-                double acc = 0.0;
-#pragma unroll
-                for (int m = 0; m <= l2; m++) acc += rv[l2][m] * (V(q, wk[2 - m]) + V(q, wk[2 - m + l2 + 1]));
-                flux += kgc[l2] * acc;
-              }
-            }
-            return flux * 0.25;
+            for (int k = 0; k < 6; k++) flux += cw[k] * V(q, wk[k]);
+            return flux;
           };
 #pragma unroll
-          for (int i = 0; i < NS; i++) F[i] = triple(3 + i);
+          for (int i = 0; i < NS; i++) F[i] = dot(3 + i);
 #pragma unroll
-          for (int cc = 0; cc < 3; cc++) F[iU + cc] = triple(3 + NS + cc);
+          for (int cc = 0; cc < 3; cc++) F[iU + cc] = dot(3 + NS + cc);
           double pflux = 0.0;
 #pragma unroll
-          for (int l2 = 0; l2 < 3; l2++) {
-            if (l2 < order) {
-              double acc = 0.0;
-#pragma unroll
-              for (int m = 0; m <= l2; m++) acc += (pr[2 - m] + pr[2 - m + l2 + 1]);
-              pflux += kgc[l2] * acc;
-            }
-          }
+          for (int k = 0; k < 6; k++) pflux += cp[k] * pr[k];
           F[iU + D] -= pflux;
-          // energy: the same triple product with phi = H
+          // energy: the same dot product with phi = H
           {
             double flux = 0.0;
 #pragma unroll
-            for (int l2 = 0; l2 < 3; l2++) {
-              if (l2 < order) {
-                double acc = 0.0;
-#pragma unroll
-                for (int m = 0; m <= l2; m++) acc += rv[l2][m] * (h[2 - m] + h[2 - m + l2 + 1]);
-                flux += kgc[l2] * acc;
-              }
-            }
-            F[NS + 3] = flux * 0.25;
+            for (int k = 0; k < 6; k++) flux += cw[k] * h[k];
+            F[NS + 3] = flux;
           }
         }
 #pragma unroll

@@ -314,6 +314,132 @@ HTR_D int fast_mask(const FastX &f, unsigned used, double cut) {
 
 
 
+// ---------------------------------------------------------------------------
+// Smoothness measures in single precision with a rigorous bound on their
+// absolute error, from six point values v[] already converted to float
+// (conversion error at most u |v| <= uM): every stencil difference with
+// integer coefficients c_i and k rounded operations is within (k + 2) u C M
+// of its exact value (C = sum |c_i|; the +2 covers the conversion), squares
+// and sums add at most a few u relative to the (positive) terms.  Used by
+// the shock-sensor and TENO interval filters below.
+// ---------------------------------------------------------------------------
+struct SmoothF {
+  float s[4], e[4];  // s_k and the bound on its error
+  float tau, et;     // tau6 and its bound
+};
+HTR_D SmoothF smooth_f32(float v0, float v1, float v2, float v3, float v4, float v5, float uM) {
+  const float u = 5.9604645e-08f;
+  // s = A a^2 + B b^2 and the bound on its error
+  auto sq2 = [&](float A, float a, float ea, float B, float b, float eb, float &e) {
+    const float t = __fadd_rn(__fmul_rn(__fmul_rn(A, a), a), __fmul_rn(__fmul_rn(B, b), b));
+    e = A * ea * (2.0f * fabsf(a) + ea) + B * eb * (2.0f * fabsf(b) + eb) + 8.0f * u * t;
+    return t;
+  };
+  const float C13 = 13.0f / 12.0f, C23 = 3.0f / 12.0f, C14 = 1.0f / 36.0f, C24 = 13.0f / 12.0f,
+              C34 = 781.0f / 720.0f;
+  SmoothF r;
+  // s1: a = ym1 - 2y + yp1 (C 4, 2 ops), b = ym1 - yp1 (C 2, 1 op)
+  r.s[0] = sq2(C13, __fadd_rn(__fsub_rn(v1, 2.0f * v2), v3), 4.0f * 4.0f * uM, C23, __fsub_rn(v1, v3),
+               3.0f * 2.0f * uM, r.e[0]);
+  // s2: a = y - 2yp1 + yp2 (C 4, 2), b = 3y - 4yp1 + yp2 (C 8, 3)
+  r.s[1] = sq2(C13, __fadd_rn(__fsub_rn(v2, 2.0f * v3), v4), 4.0f * 4.0f * uM, C23,
+               __fadd_rn(__fsub_rn(__fmul_rn(3.0f, v2), 4.0f * v3), v4), 5.0f * 8.0f * uM, r.e[1]);
+  // s3: a = ym2 - 2ym1 + y (C 4, 2), b = 3y - 4ym1 + ym2 (C 8, 3)
+  r.s[2] = sq2(C13, __fadd_rn(__fsub_rn(v0, 2.0f * v1), v2), 4.0f * 4.0f * uM, C23,
+               __fadd_rn(__fsub_rn(__fmul_rn(3.0f, v2), 4.0f * v1), v0), 5.0f * 8.0f * uM, r.e[2]);
+  // s4: a = -11y + 18yp1 - 9yp2 + 2yp3 (C 40, 6), b = 2y - 5yp1 + 4yp2 - yp3 (C 12, 4),
+  //     c = -y + 3yp1 - 3yp2 + yp3 (C 8, 5)
+  const float a4 = __fadd_rn(__fsub_rn(__fadd_rn(__fmul_rn(-11.0f, v2), __fmul_rn(18.0f, v3)), __fmul_rn(9.0f, v4)),
+                             2.0f * v5);
+  const float b4 = __fsub_rn(__fadd_rn(__fsub_rn(2.0f * v2, __fmul_rn(5.0f, v3)), 4.0f * v4), v5);
+  const float c4 = __fadd_rn(__fsub_rn(__fadd_rn(-v2, __fmul_rn(3.0f, v3)), __fmul_rn(3.0f, v4)), v5);
+  const float ea4 = 8.0f * 40.0f * uM, eb4 = 6.0f * 12.0f * uM, ec4 = 7.0f * 8.0f * uM;
+  r.s[3] = __fadd_rn(__fadd_rn(__fmul_rn(__fmul_rn(C14, a4), a4), __fmul_rn(__fmul_rn(C24, b4), b4)),
+                     __fmul_rn(__fmul_rn(C34, c4), c4));
+  r.e[3] = C14 * ea4 * (2.0f * fabsf(a4) + ea4) + C24 * eb4 * (2.0f * fabsf(b4) + eb4) +
+           C34 * ec4 * (2.0f * fabsf(c4) + ec4) + 10.0f * u * r.s[3];
+  const float comb = __fdiv_rn(__fadd_rn(__fadd_rn(r.s[2], r.s[1]), 4.0f * r.s[0]), 6.0f);
+  r.tau = fabsf(__fsub_rn(r.s[3], comb));
+  r.et = r.e[3] + (r.e[2] + r.e[1] + 4.0f * r.e[0]) / 6.0f + 6.0f * u * (r.s[3] + comb);
+  return r;
+}
+
+// Interval decision of the TENO / TENO-A (non-standard node) / TENO-LAD
+// stencil selection, before any double-precision smoothness measure is
+// evaluated.  The six values are scaled by a power of two (exact) so that
+// the largest has magnitude in [1/2, 1), converted to float, and the
+// smoothness measures bounded with smooth_f32 (eps scaled by the square of
+// the same power of two).  From the resulting intervals of
+// chi_k = tau6/(s_k + eps) it bounds q_k = (1 + chi_k)^6 / sum_j (1 + chi_j)^6
+// over the used candidates and, for TENO-LAD, the cut-off exponent
+// floor(3 + 9.5 / (1 + chi_max / 10)); it returns the flags (bit k = stencil
+// k kept) only when the exponent is determined and every q_k clears the
+// cut-off by 1e-3 of it -- far above the relative rounding of this interval
+// arithmetic (below 1e-5) -- and -1 otherwise, or for values whose scaling
+// leaves the float range.  Its decisions therefore equal the exact
+// double-precision ones.
+template <int KIND>
+HTR_D int teno_interval_mask(double ym2, double ym1, double y0, double yp1, double yp2, double yp3, unsigned used,
+                             double eps, double cut) {
+  const double M = fmax(fmax(fmax(fabs(ym2), fabs(ym1)), fmax(fabs(y0), fabs(yp1))), fmax(fabs(yp2), fabs(yp3)));
+  if (!(M > 1e-30 && M < 1e30) || used == 0u) return -1;
+  int ex;
+  frexp(M, &ex);
+  const float epsS = __double2float_rn(scalbn(eps, -2 * ex));
+  if (!(epsS >= 1e-30f && epsS <= 1e30f)) return -1;
+  const float u = 5.9604645e-08f;
+  const SmoothF sm = smooth_f32(__double2float_rn(scalbn(ym2, -ex)), __double2float_rn(scalbn(ym1, -ex)),
+                                __double2float_rn(scalbn(y0, -ex)), __double2float_rn(scalbn(yp1, -ex)),
+                                __double2float_rn(scalbn(yp2, -ex)), __double2float_rn(scalbn(yp3, -ex)), u);
+  const float tlo = fmaxf(sm.tau - sm.et, 0.0f), thi = sm.tau + sm.et;
+  float xl[4], xh[4], m = 1.0f, cmax_lo = 0.0f, cmax_hi = 0.0f;
+#pragma unroll
+  for (int k = 0; k < 4; k++) {
+    const float clo = tlo / (sm.s[k] + sm.e[k] + epsS);
+    const float chi = thi / (fmaxf(sm.s[k] - sm.e[k], 0.0f) + epsS);
+    cmax_lo = fmaxf(cmax_lo, clo);
+    cmax_hi = fmaxf(cmax_hi, chi);
+    xl[k] = 1.0f + clo;
+    xh[k] = 1.0f + chi;
+    if (used & (1u << k)) m = fmaxf(m, xh[k]);
+  }
+  if (!(m < 1e30f)) return -1;
+  float c = (float)cut;
+  if (KIND == kTENOLAD) {
+    // the exponent argument decreases with chi_max; the exact one lies in (3, 12.5]
+    const float argHi = 3.0f + 9.5f / (1.0f + cmax_lo * 0.1f);
+    const float argLo = 3.0f + 9.5f / (1.0f + cmax_hi * 0.1f);
+    const float fhi = floorf(argHi + 1e-3f), flo = floorf(argLo - 1e-3f);
+    int power;
+    if (fhi == flo) power = (int)fhi;
+    else if (fhi <= 3.0f) power = 3;
+    else return -1;
+    c = kP10[min(max(power, 0), 13)];
+  }
+  float pl[4], ph[4], Sl = 0.0f, Sh = 0.0f;
+#pragma unroll
+  for (int k = 0; k < 4; k++) {
+    const bool on = used & (1u << k);
+    pl[k] = on ? pow6f(xl[k] / m) : 0.0f;
+    ph[k] = on ? pow6f(xh[k] / m) : 0.0f;
+    Sl += pl[k];
+    Sh += ph[k];
+  }
+  const float hi = c * 1.001f, lo = c * 0.999f;
+  int mask = 0;
+#pragma unroll
+  for (int k = 0; k < 4; k++) {
+    if (!(used & (1u << k))) continue;
+    const float qlo = pl[k] / (pl[k] + (Sh - ph[k]));
+    const float qhi = ph[k] / (ph[k] + (Sl - pl[k]));
+    if (qlo >= hi)
+      mask |= 1 << k;
+    else if (!(qhi <= lo))
+      return -1;
+  }
+  return mask;
+}
+
 // One TENO reconstruction at face c+1/2 from y = (c-2 .. c+3); MINUS gives
 // the right-biased value (metric.inl:431-1038).  Returns the 4 selection
 // flags in *mask (bit k = stencil k kept).
@@ -327,14 +453,24 @@ HTR_D double teno(double ym2, double ym1, double y, double yp1, double yp2, doub
   const double W1 = MINUS ? kNode[t].cm[1] : kNode[t].cp[1];
   const double W2 = MINUS ? kNode[t].cm[2] : kNode[t].cp[2];
   const double W3 = MINUS ? kNode[t].cm[3] : kNode[t].cp[3];
-  const Smooth s = MINUS ? smoothness(yp3, yp2, yp1, y, ym1, ym2) : smoothness(ym2, ym1, y, yp1, yp2, yp3);
   const double eps = KIND == kTENO ? 1e-10 : (KIND == kTENOA ? 1e-8 : 1e-16);
   int fmask = -1;
-  if (KIND != kTENOA || t != Std) {
-    // cheap exact-decision filter (see fast_mask); TENO-A on standard nodes
-    // adapts its cut-off to a Ren sensor and always takes the exact path
-    const unsigned used = (W0 < 1e-10 ? 0u : 1u) | (W1 < 1e-10 ? 0u : 2u) | (W2 < 1e-10 ? 0u : 4u) |
-                          (W3 < 1e-10 ? 0u : 8u);
+  const unsigned used_all = (W0 < 1e-10 ? 0u : 1u) | (W1 < 1e-10 ? 0u : 2u) | (W2 < 1e-10 ? 0u : 4u) |
+                            (W3 < 1e-10 ? 0u : 8u);
+  // interval filter on the point values: most faces are decided without
+  // evaluating the smoothness measures in double precision
+  if (KIND != kTENOA || t != Std)
+    fmask = MINUS ? teno_interval_mask<KIND>(yp3, yp2, yp1, y, ym1, ym2, used_all, eps,
+                                             KIND == kTENOA ? double(kP10[4]) : 1e-6)
+                  : teno_interval_mask<KIND>(ym2, ym1, y, yp1, yp2, yp3, used_all, eps,
+                                             KIND == kTENOA ? double(kP10[4]) : 1e-6);
+  Smooth s;
+  if (fmask < 0) s = MINUS ? smoothness(yp3, yp2, yp1, y, ym1, ym2) : smoothness(ym2, ym1, y, yp1, yp2, yp3);
+  if (fmask < 0 && (KIND != kTENOA || t != Std)) {
+    // second filter on the double-precision smoothness measures (see
+    // fast_mask); TENO-A on standard nodes adapts its cut-off to a Ren
+    // sensor and always takes the exact path
+    const unsigned used = used_all;
     const FastX fx = fast_x(s, eps);
     double fcut = 1e-6;
     bool cut_ok = true;
@@ -515,39 +651,10 @@ HTR_D int sensor_prefilter(double ym2, double ym1, double y0, double yp1, double
               v3 = __double2float_rn(yp1), v4 = __double2float_rn(yp2), v5 = __double2float_rn(yp3);
   float M = fmaxf(fmaxf(fmaxf(fabsf(v0), fabsf(v1)), fmaxf(fabsf(v2), fabsf(v3))), fmaxf(fabsf(v4), fabsf(v5)));
   if (!(M < 1e6f)) return -1;
-  const float uM = u * M;
-  // s = A a^2 + B b^2 (+ C c^2) and the bound on its error
-  auto sq2 = [&](float A, float a, float ea, float B, float b, float eb, float &e) {
-    const float t = __fadd_rn(__fmul_rn(__fmul_rn(A, a), a), __fmul_rn(__fmul_rn(B, b), b));
-    e = A * ea * (2.0f * fabsf(a) + ea) + B * eb * (2.0f * fabsf(b) + eb) + 8.0f * u * t;
-    return t;
-  };
-  const float C13 = 13.0f / 12.0f, C23 = 3.0f / 12.0f, C14 = 1.0f / 36.0f, C24 = 13.0f / 12.0f,
-              C34 = 781.0f / 720.0f;
-  float e1, e2, e3, e4;
-  // s1: a = ym1 - 2y + yp1 (C 4, 2 ops), b = ym1 - yp1 (C 2, 1 op)
-  const float s1 = sq2(C13, __fadd_rn(__fsub_rn(v1, 2.0f * v2), v3), 4.0f * 4.0f * uM, C23, __fsub_rn(v1, v3),
-                       3.0f * 2.0f * uM, e1);
-  // s2: a = y - 2yp1 + yp2 (C 4, 2), b = 3y - 4yp1 + yp2 (C 8, 3)
-  const float s2 = sq2(C13, __fadd_rn(__fsub_rn(v2, 2.0f * v3), v4), 4.0f * 4.0f * uM, C23,
-                       __fadd_rn(__fsub_rn(__fmul_rn(3.0f, v2), 4.0f * v3), v4), 5.0f * 8.0f * uM, e2);
-  // s3: a = ym2 - 2ym1 + y (C 4, 2), b = 3y - 4ym1 + ym2 (C 8, 3)
-  const float s3 = sq2(C13, __fadd_rn(__fsub_rn(v0, 2.0f * v1), v2), 4.0f * 4.0f * uM, C23,
-                       __fadd_rn(__fsub_rn(__fmul_rn(3.0f, v2), 4.0f * v1), v0), 5.0f * 8.0f * uM, e3);
-  // s4: a = -11y + 18yp1 - 9yp2 + 2yp3 (C 40, 6), b = 2y - 5yp1 + 4yp2 - yp3 (C 12, 4),
-  //     c = -y + 3yp1 - 3yp2 + yp3 (C 8, 5)
-  const float a4 = __fadd_rn(__fsub_rn(__fadd_rn(__fmul_rn(-11.0f, v2), __fmul_rn(18.0f, v3)), __fmul_rn(9.0f, v4)),
-                             2.0f * v5);
-  const float b4 = __fsub_rn(__fadd_rn(__fsub_rn(2.0f * v2, __fmul_rn(5.0f, v3)), 4.0f * v4), v5);
-  const float c4 = __fadd_rn(__fsub_rn(__fadd_rn(-v2, __fmul_rn(3.0f, v3)), __fmul_rn(3.0f, v4)), v5);
-  const float ea4 = 8.0f * 40.0f * uM, eb4 = 6.0f * 12.0f * uM, ec4 = 7.0f * 8.0f * uM;
-  const float s4 = __fadd_rn(__fadd_rn(__fmul_rn(__fmul_rn(C14, a4), a4), __fmul_rn(__fmul_rn(C24, b4), b4)),
-                             __fmul_rn(__fmul_rn(C34, c4), c4));
-  e4 = C14 * ea4 * (2.0f * fabsf(a4) + ea4) + C24 * eb4 * (2.0f * fabsf(b4) + eb4) +
-       C34 * ec4 * (2.0f * fabsf(c4) + ec4) + 10.0f * u * s4;
-  const float comb = __fdiv_rn(__fadd_rn(__fadd_rn(s3, s2), 4.0f * s1), 6.0f);
-  const float tau = fabsf(__fsub_rn(s4, comb));
-  const float et = e4 + (e3 + e2 + 4.0f * e1) / 6.0f + 6.0f * u * (s4 + comb);
+  const SmoothF sm = smooth_f32(v0, v1, v2, v3, v4, v5, u * M);
+  const float tau = sm.tau, et = sm.et;
+  const float s1 = sm.s[0], s2 = sm.s[1], s3 = sm.s[2], s4 = sm.s[3];
+  const float e1 = sm.e[0], e2 = sm.e[1], e3 = sm.e[2], e4 = sm.e[3];
   const float eps = 1e-8f;
   const float tlo = fmaxf(tau - et, 0.0f), thi = tau + et;
   const float sv[4] = {s1, s2, s3, s4}, ev[4] = {e1, e2, e3, e4};

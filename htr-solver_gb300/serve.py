@@ -4,9 +4,12 @@ A request asks for a number of SSP-RK3 steps of one seeded grid: a 1-D shock
 tube, a 2-D vortex-advection box or a 3-D reacting-air box.  The server
 keeps every admitted request's state resident on the device and advances
 all of them round by round: each round issues one step of every active
-request, each as the replay of that request's CUDA graph of one fused step
-(htr_rk3_step_ws on the request's own workspace) on a stream of a small
-pool, so the steps of different requests overlap on the GPU.  Requests are
+request.  Shock tubes of one mixture are stepped together: packed into one
+strip (TubeGroup), all of them advance in one fused step of the strip, each
+by its own step size.  Each 2-D and 3-D box steps as the replay of its own
+CUDA graph of one fused step (htr_rk3_step_ws on the request's own
+workspace); the groups and the boxes run on the streams of a small pool, so
+the steps of different requests overlap on the GPU.  Requests are
 admitted in arrival order while their device memory (state + workspace) fits
 the HBM budget; a finished request's result (Conserved) is copied to the host
 and its memory released, which lets the next request in.  At most two rounds
@@ -126,6 +129,114 @@ class Instance:
         self.graph = None
 
 
+class TubeGroup:
+    """Every admitted shock-tube request of one mixture, stepped together:
+    the tubes are packed end to end into one device strip (their boundary
+    ghost nodes keep each tube's stencils to itself) and advanced by one
+    fused step of the strip per round, every tube by its own step size
+    (htr_rk3_step_cells_ws), replayed from one CUDA graph.  The strip is
+    rebuilt, and the graph captured again, when tubes join or leave; a tube's
+    cells go through the same arithmetic in any strip, so its result does
+    not depend on the other members."""
+
+    def __init__(self, eos, device, stream, graphs=True):
+        self.eos = eos
+        self.device = device
+        self.stream = stream
+        self.graphs = graphs
+        self.chem = eos == abi.HTR_EOS_AIRMIX
+        l = runtime.lib()
+        mix = tubes.AIR_REF if self.chem else tubes.GAS_PARAMS
+        self.gh = runtime.load_mixture(eos, workloads.make_mixture_struct(l, eos, mix))
+        self.members = []   # dicts: req, dev (the tube's Fluid, a view into the strip once packed), dt, remaining
+        self.done = []      # members whose last step ran: (member, pinned host result, event)
+        self.strip = None
+        self.dt_cell = None
+        self.ws = runtime.Workspace()
+        self.graph = None
+        self.dirty = False
+
+    def admit(self, req):
+        """Derive the tube's state and its own step size on the group's stream."""
+        import torch
+        host = host_fluid(req)
+        l = runtime.lib()
+        with torch.cuda.stream(self.stream):
+            dev = host.to_device(self.device)
+            workloads.derive_state(l, dev, self.gh, runtime.stream_handle(self.stream))
+            dt = runtime.stable_dt(dev, self.gh, chemistry=self.chem, stream=self.stream)
+        self.members.append(dict(req=req, dev=dev, dt=dt, remaining=req.steps))
+        self.dirty = True
+        return sum(a.numel() * a.element_size() for a in dev.arrays.values())
+
+    def rebuild(self):
+        """Pack the current members into a new strip and capture its step."""
+        import torch
+
+        from .fluid import Fluid
+        self.stream.synchronize()
+        self.graph = None
+        if not self.members:
+            self.strip = self.dt_cell = None
+            self.dirty = False
+            return
+        nsp = self.members[0]["dev"].nspec
+        widths = [m["dev"].nx for m in self.members]
+        names = list(self.members[0]["dev"].arrays)
+        with torch.cuda.stream(self.stream):
+            strip = Fluid((sum(widths), 1, 1), nsp, device=self.device, fields=names)
+            for name in names:
+                torch.cat([m["dev"].arrays[name] for m in self.members], dim=2, out=strip.arrays[name])
+            self.dt_cell = torch.cat([torch.full((w,), m["dt"], dtype=torch.float64, device=self.device)
+                                      for w, m in zip(widths, self.members)])
+            off = 0
+            for w, m in zip(widths, self.members):
+                view = Fluid((w, 1, 1), nsp, device=self.device, fields=[])
+                view.arrays = {n: strip.arrays[n][:, :, off:off + w] for n in names}
+                m["dev"] = view
+                off += w
+            self.ws.get(runtime.workspace_bytes(strip, self.gh), self.device)
+        self.strip = strip
+        if self.graphs:
+            g = torch.cuda.CUDAGraph()
+            self.stream.synchronize()
+            with torch.cuda.stream(self.stream):
+                g.capture_begin(capture_error_mode="relaxed")
+                self._step()
+                g.capture_end()
+            self.graph = g
+        self.dirty = False
+
+    def _step(self):
+        runtime.rk3_step_cells(self.strip, self.gh, self.dt_cell, chemistry=self.chem, stream=self.stream,
+                               workspace=self.ws)
+
+    def step(self):
+        """One step of every member; members that took their last step have
+        their result copied to pinned host memory on the group's stream and
+        leave the strip at the next rebuild."""
+        import torch
+        with torch.cuda.stream(self.stream):
+            if self.graph is not None:
+                self.graph.replay()
+            else:
+                self._step()
+            keep = []
+            for m in self.members:
+                m["remaining"] -= 1
+                if m["remaining"] == 0:
+                    c = m["dev"]["Conserved"]
+                    out = torch.empty(c.shape, dtype=c.dtype, device="cpu").pin_memory()
+                    out.copy_(c, non_blocking=True)
+                    ev = torch.cuda.Event()
+                    ev.record(self.stream)
+                    self.done.append((m, out, ev))
+                    self.dirty = True
+                else:
+                    keep.append(m)
+            self.members = keep
+
+
 def _grid(req):
     """(nx, ny, nz, nspec) of a request's grid."""
     if req.kind == "tube":
@@ -181,13 +292,17 @@ def admissible(queue, now, used, budget, size=estimate_bytes):
 class Server:
     """Continuous batching under an HBM budget (bytes)."""
 
-    def __init__(self, device="cuda", hbm_budget=150e9, streams=8, graphs=True, admit_per_round=2):
+    def __init__(self, device="cuda", hbm_budget=150e9, streams=8, graphs=True, admit_per_round=2,
+                 batch_tubes=True):
         import torch
         self.device = device
         self.admit_per_round = admit_per_round  # admissions between rounds (keeps the device busy)
         self.budget = hbm_budget
         self.pool = [torch.cuda.Stream() for _ in range(streams)]
         self.graphs = graphs
+        # shock tubes of one mixture are stepped together in one strip
+        self.batch_tubes = batch_tubes
+        self.groups = {}
         self.used = 0          # bytes reserved by admitted requests
         self.peak = 0
         self.rounds = 0
@@ -199,22 +314,45 @@ class Server:
         active, finishing = [], []
         t0 = clock()
         prev_round, next_stream = [], 0
-        while queue or active or finishing:
+        while queue or active or finishing or any(g.members or g.done for g in self.groups.values()):
             now = clock() - t0
             # admission in arrival order while the budget allows
             admitted_now = 0
+            grouped = sum(len(g.members) for g in self.groups.values())
             while queue and admissible(queue[:1], now, self.used, self.budget) and \
-                    (admitted_now < self.admit_per_round or not active):
+                    (admitted_now < self.admit_per_round or not (active or grouped)):
                 admitted_now += 1
                 req = queue.pop(0)
-                inst = Instance(req, self.device, self.pool[next_stream % len(self.pool)], self.graphs)
-                next_stream += 1
+                reserved = estimate_bytes(req)
+                if self.batch_tubes and req.kind == "tube":
+                    eos = abi.HTR_EOS_AIRMIX if _grid(req)[3] == 5 else abi.HTR_EOS_CONSTPROPMIX
+                    if eos not in self.groups:
+                        self.groups[eos] = TubeGroup(eos, self.device, self.pool[next_stream % len(self.pool)],
+                                                     self.graphs)
+                        next_stream += 1
+                    nbytes = self.groups[eos].admit(req)
+                    self.over_estimate = max(self.over_estimate, nbytes / reserved)
+                    grouped += 1
+                else:
+                    inst = Instance(req, self.device, self.pool[next_stream % len(self.pool)], self.graphs)
+                    next_stream += 1
+                    inst.reserved = reserved
+                    self.over_estimate = max(self.over_estimate, inst.bytes / inst.reserved)
+                    active.append(inst)
                 req.admitted = clock() - t0
-                inst.reserved = estimate_bytes(req)
-                self.over_estimate = max(self.over_estimate, inst.bytes / inst.reserved)
-                self.used += inst.reserved
+                req.reserved = reserved
+                self.used += reserved
                 self.peak = max(self.peak, self.used)
-                active.append(inst)
+            # tubes that took their last step: results, then the strip without them
+            for g in self.groups.values():
+                for m, out, ev in list(g.done):
+                    if ev.query():
+                        m["req"].result = out.numpy()
+                        m["req"].done = clock() - t0
+                        self.used -= m["req"].reserved
+                        g.done.remove((m, out, ev))
+                if g.dirty:
+                    g.rebuild()
             # retire requests whose last step completed
             for inst in list(finishing):
                 if inst.done_event.query():
@@ -222,8 +360,10 @@ class Server:
                     inst.req.done = clock() - t0
                     self.used -= inst.reserved
                     finishing.remove(inst)
-            if not active:
-                if finishing:
+            stepping = [g for g in self.groups.values() if g.members]
+            pending = any(g.done for g in self.groups.values())
+            if not active and not stepping:
+                if finishing or pending:
                     time.sleep(1e-4)
                 elif queue:
                     time.sleep(max(0.0, min(queue[0].arrival - (clock() - t0), 0.01)))
@@ -232,6 +372,11 @@ class Server:
             for ev in prev_round:
                 ev.synchronize()
             cur = []
+            for g in stepping:
+                g.step()
+                ev = torch.cuda.Event()
+                ev.record(g.stream)
+                cur.append(ev)
             for inst in active:
                 inst.step()
                 ev = torch.cuda.Event()
