@@ -372,9 +372,9 @@ def run_batched(args, device, runtime, lib, steps=3):
         workloads.derive_state(lib, dev, gh, runtime.stream_handle())
         air = eos == abi.HTR_EOS_AIRMIX
         L = [i["L"] for i in group]
-        # every tube its own step size: CFL 0.8 over its own spectral radius,
+        # every tube its own step size: CFL 0.4 over its own spectral radius,
         # for air also at most half its fastest chemical time scale
-        dts = tubes.strip_dts(dev, offs, [x + 2 for x in L], gh, cfl=0.8, chemistry=air, lib=lib)
+        dts = tubes.strip_dts(dev, offs, [x + 2 for x in L], gh, cfl=tubes.TUBE_CFL, chemistry=air, lib=lib)
         dt_cell = torch.tensor(tubes.cell_dt(offs, [x + 2 for x in L], dts), dtype=torch.float64, device=device)
         strips.append(dict(dev=dev, gh=gh, dt=min(dts), dts=dts, dt_cell=dt_cell, offs=offs, L=L, chem=air))
     cells = sum(s["dev"].ncells for s in strips)
@@ -451,15 +451,80 @@ def run_batched(args, device, runtime, lib, steps=3):
     return out
 
 
-def run_served(args, device):
-    """Served mix: Poisson arrivals (200/s) of 1-D tubes (256-8192 cells), 2-D
-    vortex boxes (64^2-512^2) and 3-D reacting-air boxes (32^3-96^3), each
-    submitted with its initial state (generated before the session) and
-    asking for 20-100 RK3 steps (the served configuration's 100-2000 scaled by
-    1/20 so the run stays bounded).  The server (continuous batching,
-    per-request CUDA graphs on 8 streams, 150 GB budget) against the plain
-    per-request path (one request at a time, task kernels)."""
-    mix = serve.prepare(serve.request_mix(args.serve, rate=200.0, seed=777, steps=(20, 100), tube=(256, 8192),
+def run_batched_mixed(device, runtime, lib, steps=5, seed=99):
+    """Batched form with uneven shapes of both mixtures (batch.Batch): 512
+    shock tubes (128-2048 cells, gas or air), 8 2-D vortex boxes (64^2 -
+    256^2), 4 3-D Taylor-Green boxes (24^3 - 48^3) and 4 3-D reacting-air
+    boxes (24^3 - 48^3), every instance its own step size, one CUDA graph
+    launch per step; against the plain drop-in (htr_rk3_step, task kernels)
+    looped over the instances.  A solve is one SSP-RK3 step of one
+    instance."""
+    import torch
+
+    from htr_gb300 import batch
+    rng = np.random.default_rng(seed)
+    insts = [batch.tube_instance(i, device, lib) for i in tubes.instances(512, seed=seed, length=(128, 2048))]
+    boxes = [workloads.vortex2d(int(rng.integers(64, 257)), seed=int(rng.integers(1 << 30))) for _ in range(8)]
+    boxes += [workloads.taylor_green(int(rng.integers(24, 49)), seed=int(rng.integers(1 << 30))) for _ in range(4)]
+    boxes += [workloads.air_box(int(rng.integers(24, 49)), seed=int(rng.integers(1 << 30))) for _ in range(4)]
+    insts += [batch.box_instance(b, device, lib) for b in boxes]
+    cells = sum(i["fluid"].ncells for i in insts)
+    bt = batch.Batch(insts, device)
+    stream = torch.cuda.current_stream()
+    bt.step()
+    torch.cuda.synchronize()
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    e0.record(stream)
+    for _ in range(steps):
+        bt.step()
+    e1.record(stream)
+    e1.synchronize()
+    t_batch = e0.elapsed_time(e1) / steps
+    p = runtime.htr_step_params
+    used = C.c_double(0.0)
+    sh = runtime.stream_handle()
+
+    def loop_all():
+        for i in insts:
+            f = i["fluid"]
+            prm = p(runtime.SCHEMES["Hybrid"], 1.0, 0.0, i["dt"], 1 if i["chemistry"] else 0)
+            v = f.view()
+            inner = f.interior((1, 0, 0)) if i["tube"] else f.interior()
+            abi.check(lib, lib.htr_rk3_step(C.byref(v), inner, f.bounds(), C.byref(prm), i["gh"], C.byref(used),
+                                            None, sh), "htr_rk3_step")
+
+    loop_all()
+    torch.cuda.synchronize()
+    f0, f1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    f0.record(stream)
+    loop_all()
+    f1.record(stream)
+    f1.synchronize()
+    t_plain = f0.elapsed_time(f1)
+    n = len(insts)
+    return {"metric": "batched solves/s", "unit": "instance RK3 steps/s", "instances": n, "cells": int(cells),
+            "value": n / (t_batch * 1e-3), "ms_per_step": t_batch,
+            "cell_updates_per_s": 3.0 * cells / (t_batch * 1e-3),
+            "plain": {"value": n / (t_plain * 1e-3), "ms_per_step": t_plain,
+                      "cell_updates_per_s": 3.0 * cells / (t_plain * 1e-3)},
+            "speedup_vs_plain": t_plain / t_batch, "gpu_launches_per_step": bt.launches_per_step(),
+            "config": {"workload": "512 shock tubes (128-2048 cells, gas or air) + 8 vortex boxes (64^2-256^2) + "
+                                   "4 Taylor-Green boxes (24^3-48^3) + 4 reacting-air boxes (24^3-48^3)",
+                       "form": "tubes in one strip per mixture, boxes as their own fused steps, one CUDA graph "
+                               "with one branch per strip and box, one launch per step, per-instance dt"}}
+
+
+def run_served(args, device, rate=200.0):
+    """Served mix: Poisson arrivals (`rate` per s) of 1-D tubes (256-8192
+    cells), 2-D vortex boxes (64^2-512^2) and 3-D reacting-air boxes
+    (32^3-96^3), each submitted with its initial state (generated before the
+    session) and asking for 20-100 RK3 steps (the served configuration's
+    100-2000 scaled by 1/20 so the run stays bounded).  The server
+    (continuous batching: the tubes of one mixture stepped together in one
+    strip, the boxes as per-request CUDA graphs, on 8 streams; 150 GB budget)
+    against the plain per-request path (one request at a time, task
+    kernels)."""
+    mix = serve.prepare(serve.request_mix(args.serve, rate=rate, seed=777, steps=(20, 100), tube=(256, 8192),
                                           vortex=(64, 512), box=(32, 96)))
     # warm the library, the allocator and the host-state generators
     warm = serve.request_mix(3, rate=1e6, seed=1, steps=(1, 1), tube=(64, 64), vortex=(16, 16), box=(8, 8))
@@ -483,7 +548,7 @@ def run_served(args, device):
             "plain": {"value": b["solves_per_s"], "tts_p50_s": b["tts_p50_s"], "tts_p99_s": b["tts_p99_s"],
                       "cell_updates_per_s": cells / t_plain},
             "speedup_vs_plain": t_plain / t_srv,
-            "config": {"requests": len(mix), "arrival_rate_per_s": 200.0, "steps": [20, 100],
+            "config": {"requests": len(mix), "arrival_rate_per_s": rate, "steps": [20, 100],
                        "kinds": {k: sum(r.kind == k for r in mix) for k in ("tube", "vortex", "box")},
                        "sizes": {"tube": [256, 8192], "vortex": [64, 512], "box": [32, 96]},
                        "note": "steps scaled by 1/20 from the served configuration to bound the run; "
@@ -819,10 +884,23 @@ def run_gpu(args):
                 result["batched"] = run_batched(args, device, runtime, lib)
             except Exception as exc:  # the headline line must still print
                 result["batched"] = {"error": f"{type(exc).__name__}: {exc}"}
-        if args.serve > 0:
             try:
-                log("served mix")
-                result["served"] = run_served(args, device)
+                log("batched mixed shapes")
+                result["batched"]["mixed"] = run_batched_mixed(device, runtime, lib)
+            except Exception as exc:
+                result["batched"]["mixed"] = {"error": f"{type(exc).__name__}: {exc}"}
+        if args.serve > 0:
+            rates = [float(r) for r in args.serve_rates.split(",")]
+            try:
+                log(f"served mix at {rates[0]}/s")
+                result["served"] = run_served(args, device, rates[0])
+                if len(rates) > 1:
+                    result["served"]["rates"] = {}
+                    for r in rates[1:]:
+                        log(f"served mix at {r}/s")
+                        res = run_served(args, device, r)
+                        result["served"]["rates"][str(r)] = {k: res[k] for k in ("value", "tts_p50_s", "tts_p99_s",
+                                                                                 "speedup_vs_plain", "plain")}
             except Exception as exc:
                 result["served"] = {"error": f"{type(exc).__name__}: {exc}"}
         if args.wall:
@@ -932,6 +1010,7 @@ def main():
     p.add_argument("--no-cpu-baseline", dest="cpu_baseline", action="store_false")
     p.add_argument("--tubes", type=int, default=4096, help="batched shock tubes (0: skip)")
     p.add_argument("--serve", type=int, default=32, help="served requests (0: skip)")
+    p.add_argument("--serve-rates", default="200", help="Poisson arrival rates per s of the served mix, first reported")
     p.add_argument("--wall", default="512,192,128", help="boundary-layer interior cells nx,ny,nz ('' skips)")
     p.add_argument("--wall-steps", type=int, default=10)
     p.add_argument("--no-restart", dest="restart", action="store_false", help="skip the restart dump/load timing")

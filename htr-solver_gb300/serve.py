@@ -93,7 +93,8 @@ class Instance:
         with torch.cuda.stream(stream):
             self.dev = host.to_device(device)
             workloads.derive_state(l, self.dev, self.gh, runtime.stream_handle(stream))
-            self.dt = runtime.stable_dt(self.dev, self.gh, chemistry=self.chem, stream=stream)
+            cfl = tubes.TUBE_CFL if req.kind == "tube" else 0.8
+            self.dt = runtime.stable_dt(self.dev, self.gh, cfl=cfl, chemistry=self.chem, stream=stream)
             self.ws = runtime.Workspace()
             self.ws.get(runtime.workspace_bytes(self.dev, self.gh), device)
         self.bytes = sum(a.numel() * a.element_size() for a in self.dev.arrays.values()) + self.ws.nbytes
@@ -164,7 +165,7 @@ class TubeGroup:
         with torch.cuda.stream(self.stream):
             dev = host.to_device(self.device)
             workloads.derive_state(l, dev, self.gh, runtime.stream_handle(self.stream))
-            dt = runtime.stable_dt(dev, self.gh, chemistry=self.chem, stream=self.stream)
+            dt = runtime.stable_dt(dev, self.gh, cfl=tubes.TUBE_CFL, chemistry=self.chem, stream=self.stream)
         self.members.append(dict(req=req, dev=dev, dt=dt, remaining=req.steps))
         self.dirty = True
         return sum(a.numel() * a.element_size() for a in dev.arrays.values())
@@ -408,7 +409,7 @@ def run_plain(requests, device="cuda", clock=time.perf_counter):
         gh = runtime.load_mixture(eos, m)
         dev = host.to_device(device)
         workloads.derive_state(l, dev, gh, runtime.stream_handle())
-        dt = runtime.stable_dt(dev, gh, chemistry=chem)
+        dt = runtime.stable_dt(dev, gh, cfl=tubes.TUBE_CFL if req.kind == "tube" else 0.8, chemistry=chem)
         req.admitted = clock() - t0
         inner = dev.interior(host.meta.get("bnum", (0, 0, 0)))
         for _ in range(req.steps):

@@ -3,8 +3,11 @@
 Point by point against the CPU oracle (the port on all host cores, about 20
 s per step): one fused SSP-RK3 step of the 256^3 periodic box of 5-species
 reacting air (hybrid scheme, diffusion, explicit chemistry) and one fused
-step of the 512 x 192 x 128 TENO-LAD boundary layer, from the same state,
-within the pointwise bar of util.check.
+step of the 512 x 192 x 128 TENO-LAD boundary layer, from the same state:
+Conserved within the pointwise bar of util.check everywhere, the primitive
+and property fields too except in the rare cells where the two sides'
+Newton solves for T stop one iteration apart at the reference's tolerance
+(util.check_state_after_step).
 
 Size-independent properties of the same grids:
 
@@ -85,8 +88,9 @@ def test_fullsize_step_matches_the_oracle(box):
         assert np.array_equal(a, b), f"{(a != b).sum()} sensor{d} flags differ"
         assert 0 < b.sum() < b.size
     for name in STATE:
-        info = util.check(out[name], host[name], name)
-        print(f"{name}: pointwise error / bound {info['ratio']:.3e}, normwise {info['normwise']:.3e}")
+        ratio, info = util.pointwise(out[name], host[name], name)
+        print(f"{name}: pointwise error / bound {ratio:.3e}, normwise {info['normwise']:.3e}")
+    util.check_state_after_step(out, host, STATE)
 
 
 @pytest.mark.gpu
@@ -123,8 +127,9 @@ def test_boundary_layer_fullsize_step_matches_the_oracle():
     torch.cuda.synchronize()
     out = dev.to_host()
     for name in STATE + ("dudtBoundary", "dTdtBoundary"):
-        info = util.check(out[name], ref[name], name)
-        print(f"{name}: pointwise error / bound {info['ratio']:.3e}, normwise {info['normwise']:.3e}")
+        ratio, info = util.pointwise(out[name], ref[name], name)
+        print(f"{name}: pointwise error / bound {ratio:.3e}, normwise {info['normwise']:.3e}")
+    util.check_state_after_step(out, ref, STATE + ("dudtBoundary", "dTdtBoundary"))
 
 
 @pytest.mark.gpu
