@@ -469,7 +469,7 @@ def run_batched_mixed(device, runtime, lib, steps=5, seed=99):
     boxes += [workloads.air_box(int(rng.integers(24, 49)), seed=int(rng.integers(1 << 30))) for _ in range(4)]
     insts += [batch.box_instance(b, device, lib) for b in boxes]
     cells = sum(i["fluid"].ncells for i in insts)
-    bt = batch.Batch(insts, device)
+    bt = batch.Batch(insts, device, tune=True)
     stream = torch.cuda.current_stream()
     bt.step()
     torch.cuda.synchronize()
@@ -508,6 +508,7 @@ def run_batched_mixed(device, runtime, lib, steps=5, seed=99):
             "plain": {"value": n / (t_plain * 1e-3), "ms_per_step": t_plain,
                       "cell_updates_per_s": 3.0 * cells / (t_plain * 1e-3)},
             "speedup_vs_plain": t_plain / t_batch, "gpu_launches_per_step": bt.launches_per_step(),
+            "autotune": bt.tunings,
             "config": {"workload": "512 shock tubes (128-2048 cells, gas or air) + 8 vortex boxes (64^2-256^2) + "
                                    "4 Taylor-Green boxes (24^3-48^3) + 4 reacting-air boxes (24^3-48^3)",
                        "form": "tubes in one strip per mixture, boxes as their own fused steps, one CUDA graph "

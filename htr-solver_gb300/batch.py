@@ -13,7 +13,9 @@ independent, so the GPU runs them concurrently and the host issues one
 launch per step.  Every instance keeps its own step size (the CFL step of
 its own grid, as each run of the reference computes it), and its result
 does not depend on the other members: the same cells go through the same
-arithmetic in any batch.
+arithmetic in any batch.  With tune=True the launch shapes (KG x tile, TENO
+blocks per SM, block sizes) are chosen per size class of branch by the
+autotuner and captured into each branch.
 """
 from . import abi, runtime, tubes
 
@@ -25,7 +27,7 @@ class Batch:
     strip).  After construction the instances' fluids are views into the
     batch's storage (tubes: into their strip)."""
 
-    def __init__(self, instances, device="cuda", graph=True):
+    def __init__(self, instances, device="cuda", graph=True, tune=False):
         import torch
 
         from .fluid import Fluid
@@ -59,19 +61,52 @@ class Batch:
         self.workspaces = [runtime.Workspace() for _ in self.branches]
         for (kind, b), ws in zip(self.branches, self.workspaces):
             ws.get(runtime.workspace_bytes(b["fluid"], b["gh"]), device)
+        self.tunings = {}  # size class -> launch shapes chosen for it
+        if tune:
+            self.autotune()
         self.graph = None
         if graph:
             self.capture()
+
+    @staticmethod
+    def size_class(kind, fluid):
+        """Size class of a branch for launch-shape tuning: the strips of each
+        mixture, and small (below 64 k cells) or large boxes of each mixture."""
+        if kind == "strip":
+            return f"strip, {fluid.nspec} species"
+        return f"{'small' if fluid.ncells < 65536 else 'large'} box, {fluid.nspec} species"
+
+    def autotune(self, reps=3):
+        """Launch shapes per size class (autotune.autotune on that class's
+        grids: KG x tile, TENO blocks per SM, block sizes).  The shapes are
+        captured into the graph branch by branch; they never change the
+        arithmetic."""
+        from . import autotune as at
+        default = at.get_tuning()
+        classes = {}
+        for (kind, b), ws in zip(self.branches, self.workspaces):
+            classes.setdefault(self.size_class(kind, b["fluid"]), []).append((b, ws))
+        for cls, items in classes.items():
+            at.set_tuning(default)
+            grids = [(b["fluid"], b["gh"], b["dt"] if "dt" in b else float(b["dt_cell"].min()), b["chemistry"])
+                     for b, _ in items]
+            best, t_best, t0, _ = at.autotune(grids, reps=reps, workspace=items[0][1])
+            self.tunings[cls] = dict(tuning=best, stage_ms=t_best, stage_ms_default=t0)
+        at.set_tuning(default)
 
     def _issue(self, stream):
         """One step of every branch, each on its own stream forked from and
         joined back to `stream`."""
         import torch
+        from . import autotune as at
+        default = at.get_tuning() if self.tunings else None
         fork = torch.cuda.Event()
         fork.record(stream)
         joins = []
         for (kind, b), s, ws in zip(self.branches, self.streams, self.workspaces):
             s.wait_event(fork)
+            if self.tunings:
+                at.set_tuning(at.htr_stage_tuning(**self.tunings[self.size_class(kind, b["fluid"])]["tuning"]))
             if kind == "strip":
                 runtime.rk3_step_cells(b["fluid"], b["gh"], b["dt_cell"], chemistry=b["chemistry"], stream=s,
                                        workspace=ws)
@@ -81,6 +116,8 @@ class Batch:
             ev = torch.cuda.Event()
             ev.record(s)
             joins.append(ev)
+        if default is not None:
+            at.set_tuning(default)
         for ev in joins:
             stream.wait_event(ev)
 

@@ -379,8 +379,13 @@ struct AirDev {
   // With `have`, Td = T * TRef, Tinv and logT = log(Td) of the initial T are
   // supplied; later iterates take log T from the previous one through a
   // log1p series when they moved by less than 2^-10 (|r|^7/7 < 1e-22).
+  // With h0 / cp0, the species enthalpies and heat capacities at the initial
+  // T (computed by the previous refresh that ended on this very T) replace
+  // its evaluation; hout (optional) receives the enthalpies at the returned T.
   HTR_D double TFromInternalEnergyCp(double e0, double T, const double *Y, int *its, double *cpk,
-                                     double &Td, double &Tinv, double &logT, bool have = false) const {
+                                     double &Td, double &Tinv, double &logT, bool have = false,
+                                     const double *h0 = nullptr, const double *cp0 = nullptr,
+                                     double *hout = nullptr) const {
     const int MAXITS = 1000;
     const double TOL = 1e-8;
     double dfdT = 1.0, h[NS];
@@ -402,7 +407,15 @@ struct AirDev {
         Td = Tn;
         Tinv = 1.0 / Td;
       }
-      EnthalpyCp(Td, Tinv, logT, h, cpk);
+      if (j == 0 && h0 != nullptr) {
+#pragma unroll
+        for (int i = 0; i < NS; i++) {
+          h[i] = h0[i];
+          cpk[i] = cp0[i];
+        }
+      } else {
+        EnthalpyCp(Td, Tinv, logT, h, cpk);
+      }
       double e = 0.0;
 #pragma unroll
       for (int i = 0; i < NS; i++) e += Y[i] * (h[i] - rOvW[i] * Td);
@@ -419,6 +432,10 @@ struct AirDev {
       Tinv = 1.0 / Td;
       logT = log(Td);
       EnthalpyCp(Td, Tinv, logT, h, cpk);
+    }
+    if (hout != nullptr) {
+#pragma unroll
+      for (int i = 0; i < NS; i++) hout[i] = h[i];
     }
     if (its) *its = j;
     return T;

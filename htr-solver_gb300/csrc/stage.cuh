@@ -54,7 +54,7 @@ struct StageWorkspace {
   TenoEntry *queue; // capacity nf[0]+nf[1]+nf[2]: the faces of direction D from offset nf[0]+..+nf[D-1]
   unsigned *count;  // queue lengths of the three directions
   double *prep;     // per-cell prepass values, [kPrepVals][ncell]
-  double *tcache;   // per cell: T it was computed for, log(T TRef), 1/(T TRef); [3][ncell]
+  double *tcache;   // per cell: T it was computed for, log(T TRef), 1/(T TRef), species h and c_p; [3 + 2 NS][ncell]
   double *scalars;  // 3 doubles in the counters' 256-byte block (maximum Mach number per direction)
 };
 

@@ -31,7 +31,7 @@ size_t stage_workspace_bytes(const htr_rect3 &r, int neq) {
   b += align256(sizeof(TenoEntry) * (g.nf[0] + g.nf[1] + g.nf[2]));
   b += align256(sizeof(unsigned));
   b += align256(sizeof(double) * kPrepVals * ncell);
-  b += align256(sizeof(double) * 3 * ncell);
+  b += align256(sizeof(double) * (3 + 2 * (neq - 4)) * ncell);
   return b;
 }
 
@@ -248,7 +248,9 @@ struct UpdateArgs {
   const double *dt_cell;  // per-cell step sizes (dense), or null: dt
   double dt_h;            // factor of dt_cell (1/2 with implicit chemistry)
   int *status;
-  double *tcache;  // [3][ncell]: T, log(T TRef), 1/(T TRef) of the last refresh
+  // [3 + 2 NS][ncell] of the last refresh: T, log(T TRef), 1/(T TRef), the
+  // species enthalpies and heat capacities at that T
+  double *tcache;
   // boundary step only
   Fd<double> Xp, Tp, up;  // NSCBC inflow profiles
   int bc[6];
@@ -259,9 +261,11 @@ struct UpdateArgs {
 // conserved vector u_.  Single-species gas: the task kernels' arithmetic.
 // Air: the fused thermo/transport of the mixture (one Newton pass that also
 // yields the species c_p of the final temperature, batched inversions).
+// cached: the cache holds this cell's species enthalpies and heat
+// capacities at the current T (the Newton's first evaluation is skipped).
 template <class Mix>
 HTR_D void refresh_cell(const UpdateArgs &A, const Mix &mix, const long long *p, const double *u_, long long i,
-                        double Td, double Tinv, double logT) {
+                        double Td, double Tinv, double logT, bool cached = false) {
   constexpr int NS = Mix::NS;
   double rhoYi[NS], Yi[NS], x[NS], vel[3], d[NS], y2[NS];
 #pragma unroll
@@ -282,12 +286,25 @@ HTR_D void refresh_cell(const UpdateArgs &A, const Mix &mix, const long long *p,
 #pragma unroll
     for (int k = 0; k < 3; k++) vel[k] = u_[NS + k] * rhoInv;
     const double e = u_[NS + 3] * rhoInv - 0.5 * mod2(vel);
-    double cpk[NS];
-    const double Tn = mix.TFromInternalEnergyCp(e, *A.T.at(p), Yi, &its, cpk, Td, Tinv, logT, true);
+    double cpk[NS], hk[NS], h0[NS], cp0[NS];
     const long long n = A.dn.count();
+    if (cached) {
+#pragma unroll
+      for (int k = 0; k < NS; k++) {
+        h0[k] = A.tcache[(3 + k) * n + i];
+        cp0[k] = A.tcache[(3 + NS + k) * n + i];
+      }
+    }
+    const double Tn = mix.TFromInternalEnergyCp(e, *A.T.at(p), Yi, &its, cpk, Td, Tinv, logT, true,
+                                                cached ? h0 : nullptr, cp0, hk);
     A.tcache[i] = Tn;
     A.tcache[n + i] = logT;
     A.tcache[2 * n + i] = Tinv;
+#pragma unroll
+    for (int k = 0; k < NS; k++) {
+      A.tcache[(3 + k) * n + i] = hk[k];
+      A.tcache[(3 + NS + k) * n + i] = cpk[k];
+    }
     const double Pn = rho * Tn * s / mix.iMixWRef;
     *A.T.at(p) = Tn;
     *A.P.at(p) = Pn;
@@ -435,7 +452,7 @@ __device__ __noinline__ void outflow_refresh(const UpdateArgs &A, const Mix &mix
       Ti = A.tcache[2 * n + i];
       lT = A.tcache[n + i];
     }
-    refresh_cell(A, mix, p, u_, i, Td, Ti, lT);
+    refresh_cell(A, mix, p, u_, i, Td, Ti, lT, NS > 1);
   }
   double x[NS], vel[3];
   const double *xp = A.X.at(p), *vp = A.u.at(p);
@@ -505,12 +522,14 @@ __global__ void __launch_bounds__(128) stage_update(const UpdateArgs A, const __
     // T, 1/T and log T of the current state: from the previous stage's
     // refresh when it computed them for this very T, else evaluated here
     double Td0 = 0.0, Tinv0 = 0.0, logT0 = 0.0;
+    bool cached = false;
     if constexpr (NS > 1) {
       const double Tn0 = *A.T.at(p);
       Td0 = Tn0 * mix.TRef;
       if (__double_as_longlong(A.tcache[i]) == __double_as_longlong(Tn0)) {
         logT0 = A.tcache[n + i];
         Tinv0 = A.tcache[2 * n + i];
+        cached = true;
       } else {
         Tinv0 = 1.0 / Td0;
         logT0 = log(Td0);
@@ -540,7 +559,7 @@ __global__ void __launch_bounds__(128) stage_update(const UpdateArgs A, const __
         const double *F = pass == 0 ? A.fe[dd] : A.fd[dd];
         const double m = pass == 0 ? ld(A.me[dd].at(p)) : ld(A.md[dd].at(p));
 #pragma unroll
-        for (int k = 0; k < NE; k++) ct[k] = __dadd_rn(ct[k], __dmul_rn(m, __dsub_rn(F[k * nf + fp], F[k * nf + fm])));
+        for (int k = 0; k < NE; k++) ct[k] = __fma_rn(m, __dsub_rn(F[k * nf + fp], F[k * nf + fm]), ct[k]);
       }
     }
     if constexpr (BC) {
@@ -583,7 +602,7 @@ __global__ void __launch_bounds__(128) stage_update(const UpdateArgs A, const __
     }
     // primitive recovery (variables.hpp:163-193) and property refresh
     // (variables.hpp:62-89) of the new state
-    refresh_cell(A, mix, p, u_, i, Td0, Tinv0, logT0);
+    refresh_cell(A, mix, p, u_, i, Td0, Tinv0, logT0, cached);
   }
 }
 
@@ -633,18 +652,20 @@ __global__ void boundary_refresh(const UpdateArgs A, const __grid_constant__ Mix
     }
     const long long i = A.dn.idx(p);
     double Td0 = 0.0, Tinv0 = 0.0, logT0 = 0.0;
+    bool cached = false;
     if constexpr (NS > 1) {
       const double Tn0 = *A.T.at(p);
       Td0 = Tn0 * mix.TRef;
       if (__double_as_longlong(A.tcache[i]) == __double_as_longlong(Tn0)) {
         logT0 = A.tcache[n + i];
         Tinv0 = A.tcache[2 * n + i];
+        cached = true;
       } else {
         Tinv0 = 1.0 / Td0;
         logT0 = log(Td0);
       }
     }
-    refresh_cell(A, mix, p, u_, i, Td0, Tinv0, logT0);
+    refresh_cell(A, mix, p, u_, i, Td0, Tinv0, logT0, cached);
     outflow_refresh(A, mix, p, u_, i, n_out);
   }
 }

@@ -273,7 +273,7 @@ def estimate_bytes(req):
     n = (nx, ny, nz)
     nf = [(n[0] + (d == 0)) * (n[1] + (d == 1)) * (n[2] + (d == 2)) for d in range(3)]
     work = (sum(2 * a256(8 * neq * f) for f in nf) + a256(16 * sum(nf)) + a256(4) + a256(8 * 11 * cells) +
-            a256(8 * 3 * cells))
+            a256(8 * (3 + 2 * nsp) * cells))
     return int(state + work + 256)
 
 

@@ -174,9 +174,9 @@ def test_mixed_batch_equals_each_instance_alone():
     """A batch of uneven instances of both mixtures -- shock tubes of gas and
     of air (packed into one strip per mixture), 2-D vortex boxes, 3-D
     Taylor-Green and reacting-air boxes of different sizes -- advanced by
-    one CUDA graph launch per step (batch.Batch), each with its own step
-    size: after two steps every instance equals, bit for bit, the same two
-    steps of that instance alone."""
+    one CUDA graph launch per step (batch.Batch, launch shapes tuned per
+    size class), each with its own step size: after two steps every instance
+    equals, bit for bit, the same two steps of that instance alone."""
     import torch
 
     from htr_gb300 import batch
@@ -191,7 +191,8 @@ def test_mixed_batch_equals_each_instance_alone():
         f = inst["fluid"].copy()
         f.meta = dict(inst["fluid"].meta)
         alone.append(f)
-    bt = batch.Batch(insts, "cuda")
+    bt = batch.Batch(insts, "cuda", tune=True)
+    assert len(bt.tunings) >= 3  # strips and boxes are tuned per size class
     for _ in range(2):
         bt.step()
     torch.cuda.synchronize()
