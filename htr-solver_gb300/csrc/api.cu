@@ -256,14 +256,18 @@ int step_prologue(const htr_fluid_view *v, htr_rect3 inner, htr_rect3 fb, const 
 // interior, properties everywhere) and InitializeTemporaries.
 // skip_ghosts (the fused path, where `inner` is the whole grid): the
 // boundary ghost nodes of packed instances keep their imposed state.
+// dt_cell (the per-cell step sizes of packed instances, dense over `inner`)
+// replaces dt where given.
 int implicit_chemistry_block(const htr_fluid_view *v, htr_rect3 inner, htr_rect3 fb, htr_mixture_t m, double dt,
-                             int *status_dev, htr_stream_t s, unsigned skip_ghosts = 0) {
+                             int *status_dev, htr_stream_t s, unsigned skip_ghosts = 0,
+                             const double *dt_cell = nullptr) {
   const cudaStream_t cs = (cudaStream_t)s;
   int st;
   if ((st = check_common(v, m, inner))) return st;
   if ((st = with_mix(m, [&](const auto &mix) {
-         return cuda_status(htr::launch_update_chemistry(*v, inner, dt, mix, status_dev, cs, skip_ghosts),
-                            "UpdateChemistry");
+         return cuda_status(
+             htr::launch_update_chemistry(*v, inner, dt, mix, status_dev, cs, skip_ghosts, dt_cell),
+             "UpdateChemistry");
        })))
     return st;
   if ((st = with_mix(m, [&](const auto &mix) {
@@ -302,7 +306,8 @@ int fused_step(const htr_fluid_view *v, htr_rect3 inner, htr_rect3 fb, const htr
           return cuda_status(htr::launch_stage(*v, inner, fb, mix, w, sp, status_dev, (cudaStream_t)s), "stage");
         }))
       return st;
-    if (int st = implicit_chemistry_block(v, inner, fb, m, dt, status_dev, s, active_dirs(inner))) return st;
+    if (int st = implicit_chemistry_block(v, inner, fb, m, dt, status_dev, s, active_dirs(inner), dt_cell))
+      return st;
     sp.mode = htr::kStageImplicit;
   }
   for (int stage = 1; stage <= 3; stage++) {

@@ -232,8 +232,8 @@ template <class Mix> struct Rosen {
 
 template <class Mix>
 __global__ void update_chemistry_kernel(CellRange R, Fd<double> Ct, Fd<double> C, Fd<double> Ctold,
-                                        Fd<double> T, double dt, int *status, const GhostSkip G,
-                                        const __grid_constant__ Mix mix) {
+                                        Fd<double> T, double dt, const double *dt_cell, int *status,
+                                        const GhostSkip G, const __grid_constant__ Mix mix) {
   constexpr int N = Mix::NS + 4;
   HTR_FOR_CELLS(R, idx) {
     long long p[3];
@@ -249,7 +249,9 @@ __global__ void update_chemistry_kernel(CellRange R, Fd<double> Ct, Fd<double> C
     }
     Rosen<Mix> rb{mix, old};
     rb.T = *T.at(p);
-    const int st = rb.solve(x, dt, dt);
+    // per-cell step sizes are indexed densely over the range (x fastest)
+    const double h = dt_cell ? dt_cell[idx] : dt;
+    const int st = rb.solve(x, h, h);
     if (st != HTR_OK) flag_status(status, st);
     for (int i = 0; i < N; i++) c[i] = x[i];
     *T.at(p) = rb.T;
@@ -258,17 +260,19 @@ __global__ void update_chemistry_kernel(CellRange R, Fd<double> Ct, Fd<double> C
 
 template <class Mix>
 cudaError_t launch_update_chemistry(const htr_fluid_view &v, const htr_rect3 &my, double dt,
-                                    const Mix &mix, int *status, cudaStream_t s, unsigned skip_ghosts) {
+                                    const Mix &mix, int *status, cudaStream_t s, unsigned skip_ghosts,
+                                    const double *dt_cell) {
   const CellRange R = cells(my);
   update_chemistry_kernel<Mix><<<grid_for(R.n, 64), 64, 0, s>>>(
       R, fd<double>(v.Conserved_t), fd<double>(v.Conserved), fd<double>(v.Conserved_t_old),
-      fd<double>(v.temperature), dt, status, ghost_skip(v, skip_ghosts), mix);
+      fd<double>(v.temperature), dt, dt_cell, status, ghost_skip(v, skip_ghosts), mix);
   return cudaGetLastError();
 }
 
 template cudaError_t launch_update_chemistry<ConstPropDev>(const htr_fluid_view &, const htr_rect3 &, double,
-                                                          const ConstPropDev &, int *, cudaStream_t, unsigned);
+                                                          const ConstPropDev &, int *, cudaStream_t, unsigned,
+                                                          const double *);
 template cudaError_t launch_update_chemistry<AirDev>(const htr_fluid_view &, const htr_rect3 &, double,
-                                                    const AirDev &, int *, cudaStream_t, unsigned);
+                                                    const AirDev &, int *, cudaStream_t, unsigned, const double *);
 
 }  // namespace htr

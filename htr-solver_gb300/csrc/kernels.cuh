@@ -49,8 +49,11 @@ template <class Mix>
 cudaError_t launch_spectral_radius(const htr_fluid_view &v, const htr_rect3 &my, const Mix &mix,
                                    double *result, cudaStream_t s);
 template <class Mix>
+// dt_cell (optional): one step size per cell of `my`, dense with x fastest,
+// replacing dt
 cudaError_t launch_update_chemistry(const htr_fluid_view &v, const htr_rect3 &my, double dt,
-                                    const Mix &mix, int *status, cudaStream_t s, unsigned skip_ghosts = 0);
+                                    const Mix &mix, int *status, cudaStream_t s, unsigned skip_ghosts = 0,
+                                    const double *dt_cell = nullptr);
 
 // NSCBC boundary terms on the plane `bc` (dir 0..2, minus = the "Neg" side)
 template <class Mix>
