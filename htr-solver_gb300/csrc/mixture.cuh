@@ -10,6 +10,7 @@
 #pragma once
 
 #include "common.cuh"
+#include "fastexp.cuh"
 
 namespace htr {
 
@@ -658,10 +659,11 @@ struct AirDev {
     for (int k = 0; k < 5; k++) {
       const AirReac &r = reac[k];
       // A T^n exp(-E/RT) and its backward partner as single exponentials
+      // (table-driven exp: fastexp.cuh)
       double arg = 0.0;
       if (r.useN) arg += r.n * logT;
       if (r.useE) arg -= r.EovR * Tinv;
-      const double Kf = r.A * exp(arg);
+      const double Kf = r.A * exp_table(arg);
       double a = 1.0;
 #pragma unroll
       for (int i = 0; i < 2; i++)
@@ -682,7 +684,7 @@ struct AirDev {
             sumNuG += r.nuP[i] * G[r.pd[i]];
           }
         const double lnKc = -sumNuG - sumNu * (logT + lnRP);
-        Kb = r.A * exp(arg - lnKc);
+        Kb = r.A * exp_table(arg - lnKc);
 #pragma unroll
         for (int i = 0; i < 2; i++)
           if (i < r.nPd) b *= (r.nuP[i] == 1.0) ? C[r.pd[i]] : ((r.nuP[i] == 2.0) ? C[r.pd[i]] * C[r.pd[i]] : pow(C[r.pd[i]], r.nuP[i]));

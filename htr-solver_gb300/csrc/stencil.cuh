@@ -321,7 +321,7 @@ HTR_D int fast_mask(const FastX &f, unsigned used, double cut) {
 // integer coefficients c_i and k rounded operations is within (k + 2) u C M
 // of its exact value (C = sum |c_i|; the +2 covers the conversion), squares
 // and sums add at most a few u relative to the (positive) terms.  Used by
-// the shock-sensor and TENO interval filters below.
+// the shock sensor's interval filter below.
 // ---------------------------------------------------------------------------
 struct SmoothF {
   float s[4], e[4];  // s_k and the bound on its error
@@ -364,82 +364,6 @@ HTR_D SmoothF smooth_f32(float v0, float v1, float v2, float v3, float v4, float
   return r;
 }
 
-// Interval decision of the TENO / TENO-A (non-standard node) / TENO-LAD
-// stencil selection, before any double-precision smoothness measure is
-// evaluated.  The six values are scaled by a power of two (exact) so that
-// the largest has magnitude in [1/2, 1), converted to float, and the
-// smoothness measures bounded with smooth_f32 (eps scaled by the square of
-// the same power of two).  From the resulting intervals of
-// chi_k = tau6/(s_k + eps) it bounds q_k = (1 + chi_k)^6 / sum_j (1 + chi_j)^6
-// over the used candidates and, for TENO-LAD, the cut-off exponent
-// floor(3 + 9.5 / (1 + chi_max / 10)); it returns the flags (bit k = stencil
-// k kept) only when the exponent is determined and every q_k clears the
-// cut-off by 1e-3 of it -- far above the relative rounding of this interval
-// arithmetic (below 1e-5) -- and -1 otherwise, or for values whose scaling
-// leaves the float range.  Its decisions therefore equal the exact
-// double-precision ones.
-template <int KIND>
-HTR_D int teno_interval_mask(double ym2, double ym1, double y0, double yp1, double yp2, double yp3, unsigned used,
-                             double eps, double cut) {
-  const double M = fmax(fmax(fmax(fabs(ym2), fabs(ym1)), fmax(fabs(y0), fabs(yp1))), fmax(fabs(yp2), fabs(yp3)));
-  if (!(M > 1e-30 && M < 1e30) || used == 0u) return -1;
-  int ex;
-  frexp(M, &ex);
-  const float epsS = __double2float_rn(scalbn(eps, -2 * ex));
-  if (!(epsS >= 1e-30f && epsS <= 1e30f)) return -1;
-  const float u = 5.9604645e-08f;
-  const SmoothF sm = smooth_f32(__double2float_rn(scalbn(ym2, -ex)), __double2float_rn(scalbn(ym1, -ex)),
-                                __double2float_rn(scalbn(y0, -ex)), __double2float_rn(scalbn(yp1, -ex)),
-                                __double2float_rn(scalbn(yp2, -ex)), __double2float_rn(scalbn(yp3, -ex)), u);
-  const float tlo = fmaxf(sm.tau - sm.et, 0.0f), thi = sm.tau + sm.et;
-  float xl[4], xh[4], m = 1.0f, cmax_lo = 0.0f, cmax_hi = 0.0f;
-#pragma unroll
-  for (int k = 0; k < 4; k++) {
-    const float clo = tlo / (sm.s[k] + sm.e[k] + epsS);
-    const float chi = thi / (fmaxf(sm.s[k] - sm.e[k], 0.0f) + epsS);
-    cmax_lo = fmaxf(cmax_lo, clo);
-    cmax_hi = fmaxf(cmax_hi, chi);
-    xl[k] = 1.0f + clo;
-    xh[k] = 1.0f + chi;
-    if (used & (1u << k)) m = fmaxf(m, xh[k]);
-  }
-  if (!(m < 1e30f)) return -1;
-  float c = (float)cut;
-  if (KIND == kTENOLAD) {
-    // the exponent argument decreases with chi_max; the exact one lies in (3, 12.5]
-    const float argHi = 3.0f + 9.5f / (1.0f + cmax_lo * 0.1f);
-    const float argLo = 3.0f + 9.5f / (1.0f + cmax_hi * 0.1f);
-    const float fhi = floorf(argHi + 1e-3f), flo = floorf(argLo - 1e-3f);
-    int power;
-    if (fhi == flo) power = (int)fhi;
-    else if (fhi <= 3.0f) power = 3;
-    else return -1;
-    c = kP10[min(max(power, 0), 13)];
-  }
-  float pl[4], ph[4], Sl = 0.0f, Sh = 0.0f;
-#pragma unroll
-  for (int k = 0; k < 4; k++) {
-    const bool on = used & (1u << k);
-    pl[k] = on ? pow6f(xl[k] / m) : 0.0f;
-    ph[k] = on ? pow6f(xh[k] / m) : 0.0f;
-    Sl += pl[k];
-    Sh += ph[k];
-  }
-  const float hi = c * 1.001f, lo = c * 0.999f;
-  int mask = 0;
-#pragma unroll
-  for (int k = 0; k < 4; k++) {
-    if (!(used & (1u << k))) continue;
-    const float qlo = pl[k] / (pl[k] + (Sh - ph[k]));
-    const float qhi = ph[k] / (ph[k] + (Sl - pl[k]));
-    if (qlo >= hi)
-      mask |= 1 << k;
-    else if (!(qhi <= lo))
-      return -1;
-  }
-  return mask;
-}
-
 // One TENO reconstruction at face c+1/2 from y = (c-2 .. c+3); MINUS gives
 // the right-biased value (metric.inl:431-1038).  Returns the 4 selection
 // flags in *mask (bit k = stencil k kept).
@@ -457,16 +381,8 @@ HTR_D double teno(double ym2, double ym1, double y, double yp1, double yp2, doub
   int fmask = -1;
   const unsigned used_all = (W0 < 1e-10 ? 0u : 1u) | (W1 < 1e-10 ? 0u : 2u) | (W2 < 1e-10 ? 0u : 4u) |
                             (W3 < 1e-10 ? 0u : 8u);
-  // interval filter on the point values: most faces are decided without
-  // evaluating the smoothness measures in double precision
-  if (KIND != kTENOA || t != Std)
-    fmask = MINUS ? teno_interval_mask<KIND>(yp3, yp2, yp1, y, ym1, ym2, used_all, eps,
-                                             KIND == kTENOA ? double(kP10[4]) : 1e-6)
-                  : teno_interval_mask<KIND>(ym2, ym1, y, yp1, yp2, yp3, used_all, eps,
-                                             KIND == kTENOA ? double(kP10[4]) : 1e-6);
-  Smooth s;
-  if (fmask < 0) s = MINUS ? smoothness(yp3, yp2, yp1, y, ym1, ym2) : smoothness(ym2, ym1, y, yp1, yp2, yp3);
-  if (fmask < 0 && (KIND != kTENOA || t != Std)) {
+  const Smooth s = MINUS ? smoothness(yp3, yp2, yp1, y, ym1, ym2) : smoothness(ym2, ym1, y, yp1, yp2, yp3);
+  if (KIND != kTENOA || t != Std) {
     // second filter on the double-precision smoothness measures (see
     // fast_mask); TENO-A on standard nodes adapts its cut-off to a Ren
     // sensor and always takes the exact path
