@@ -10,6 +10,7 @@
 #pragma once
 
 #include "common.cuh"
+#include "dfloat.cuh"
 #include "fastexp.cuh"
 
 namespace htr {
@@ -111,6 +112,11 @@ struct AirDev {
   double CvVoff[NS];     // 3.5 R (linear) or 4 R (non-linear)
   double lamB0[NS];      // 2/PI * 5/3 * CvROvR
   double lamK5[NS];      // 5 CvR / (PI CvT)
+  // double-float copies of the transport factors (TransportDF)
+  dfloat xkbOveps[NS], xmuC[NS], xfvK[NS], xiKbOveps[NS], xisqKbOveps[NS], xzrot298[NS], xlamB0[NS],
+      xlamK5[NS], xlamMono[NS], xCvRot[NS], xCvVoff[NS], xW[NS], xiW[NS];
+  dfloat xwilkeA[NS][NS], xwilkeBi[NS][NS], xdifEps[NS][NS], xdifK[NS][NS];
+  dfloat xpi15, xPRef, ximuRef, xilamRef, xiDiRef;
   // kinetics (2 standard + 3 third-body)
   AirReac reac[5];
   // reference scales
@@ -566,6 +572,147 @@ struct AirDev {
       for (int j = 0; j < NS; j++)
         if (j != i) num += X[j] * W[j];
       D[i] = num * den[i] * iDiRef;
+    }
+  }
+
+  // The same viscosity, conductivity and diffusivities in double-float
+  // arithmetic (dfloat.cuh) on the FP32 pipe, whose rate on this part is
+  // ~70 times the FP64 rate: every factor is a T- or pair-dependent quantity
+  // of bounded range, so about 48 significant bits carry the formulas of
+  // TransportFast to a relative error of a few 1e-14 (measured), against the
+  // 1e-11 bar.  Inputs and outputs cross between double and double-float on
+  // the integer pipe.  Mole fractions below 2^-74 lose bits and below 2^-126
+  // vanish; their terms are negligible in every sum as long as each
+  // species' diffusion partner sum keeps a partner of mole fraction >= 1e-20,
+  // i.e. at least two species have such a mole fraction.  A (near) pure
+  // mixture takes the FP64 TransportFast.
+  static HTR_D dfloat df_poly(dfloat t, const dfloat *c, int n) {
+    dfloat r = c[n - 1];
+    for (int k = n - 2; k >= 0; k--) r = df_add(df_mul(r, t), c[k]);
+    return r;
+  }
+  // omega_mu and omega_D as numerator / denominator (the fits of
+  // Species.inl:198-239; constants split at compile time)
+  static HTR_D void omega_mu_df(dfloat t, dfloat &n, dfloat &d) {
+    const dfloat cn[4] = {HTR_DF_CONST(3.3530622607), HTR_DF_CONST(2.53272006), HTR_DF_CONST(2.9024238575),
+                          HTR_DF_CONST(0.11186138893)};
+    const dfloat cd[5] = {HTR_DF_CONST(0.8662326188), HTR_DF_CONST(1.3913958626), HTR_DF_CONST(3.158490576),
+                          HTR_DF_CONST(0.18973411754), HTR_DF_CONST(0.00018682962894)};
+    n = df_poly(t, cn, 4);
+    d = df_poly(t, cd, 5);
+  }
+  static HTR_D void omega_D_df(dfloat t, dfloat &n, dfloat &d) {
+    const dfloat cn[4] = {HTR_DF_CONST(6.8728271691), HTR_DF_CONST(9.4122316321), HTR_DF_CONST(7.7442359037),
+                          HTR_DF_CONST(0.23424661229)};
+    const dfloat cd[5] = {HTR_DF_CONST(1.45337701568), HTR_DF_CONST(5.2269794238), HTR_DF_CONST(9.7108519575),
+                          HTR_DF_CONST(0.46539437353), HTR_DF_CONST(0.00041908394781)};
+    n = df_poly(t, cn, 4);
+    d = df_poly(t, cd, 5);
+  }
+  HTR_D void TransportDF(double Td, double Tinv_d, double Pn, double MixW_d, const double *X,
+                         const double *cpk, double &mu, double &lam, double *D) const {
+    // mole fractions are non-negative: their bit patterns order like them
+    const unsigned long long kTiny = 0x3bc79ca10c924223ULL;  // 1e-20
+    int big = 0;
+#pragma unroll
+    for (int i = 0; i < NS; i++) big += (df_bits(X[i]) >= kTiny) ? 1 : 0;
+    if (big < 2) {
+      TransportFast(Td, Tinv_d, Pn, MixW_d, X, cpk, mu, lam, D);
+      return;
+    }
+    const dfloat T = df_from_bits(Td);
+    const dfloat Tinv = df_from_bits(Tinv_d);
+    const dfloat sT = df_sqrt(T);
+    const dfloat isT = df_rcp(sT);
+    const dfloat P = df_mul(df_from_bits(Pn), xPRef);
+    dfloat x[NS];
+#pragma unroll
+    for (int i = 0; i < NS; i++) x[i] = df_from_bits(X[i]);
+    // species viscosities and the collision integrals of self diffusion
+    dfloat muk[NS], smu[NS], ismu[NS], nmu[NS], dmu[NS], nD[NS], dD[NS];
+#pragma unroll
+    for (int i = 0; i < NS; i++) {
+      const dfloat ts = df_mul(T, xkbOveps[i]);
+      omega_mu_df(ts, nmu[i], dmu[i]);
+      muk[i] = df_div(df_mul(df_mul(xmuC[i], sT), dmu[i]), nmu[i]);
+      smu[i] = df_sqrt(muk[i]);
+      ismu[i] = df_rcp(smu[i]);
+      if (geom[i] != 0) {
+        omega_D_df(ts, nD[i], dD[i]);
+      } else {
+        nD[i] = dD[i] = df_from(1.0f);
+      }
+    }
+    // Wilke's mixing rule (Phi_ii = 1)
+    dfloat m = df_from(0.0f);
+#pragma unroll
+    for (int i = 0; i < NS; i++) {
+      dfloat den = x[i];
+#pragma unroll
+      for (int j = 0; j < NS; j++) {
+        if (j == i) continue;
+        dfloat phi = df_add(df_mul(df_mul(smu[i], ismu[j]), xwilkeA[i][j]), 1.0f);
+        phi = df_mul(df_mul(phi, phi), xwilkeBi[i][j]);
+        den = df_add(den, df_mul(x[j], phi));
+      }
+      m = df_add(m, df_div(df_mul(x[i], muk[i]), den));
+    }
+    mu = df_to_double_bits(df_mul(m, ximuRef));
+    // species conductivities (Eucken with the rotational and vibrational
+    // relaxation of the polyatomic species) and the mixing rule
+    // lam = (sum X l + 1 / sum X / l) / 2
+    const dfloat twoOvPi = HTR_DF_CONST(2 / 3.1415926535898);
+    const dfloat fzK = HTR_DF_CONST(2 + 0.25 * 3.1415926535898 * 3.1415926535898);
+    const dfloat CvT = HTR_DF_CONST(1.5 * kRGAS);
+    dfloat a = df_from(0.0f), sxl = df_from(0.0f);
+#pragma unroll
+    for (int i = 0; i < NS; i++) {
+      dfloat l;
+      if (geom[i] == 0) {
+        l = df_mul(muk[i], xlamMono[i]);
+      } else {
+        const dfloat fV = df_div(df_mul(df_mul(xfvK[i], nmu[i]), dD[i]), df_mul(dmu[i], nD[i]));  // Dkk / mu_k
+        const dfloat tmp = df_mul(Tinv, xiKbOveps[i]);
+        const dfloat st = df_mul(isT, xisqKbOveps[i]);
+        const dfloat hp = df_mul(xpi15, st);
+        dfloat fz = df_add(df_mul(hp, 0.5f), 1.0f);
+        fz = df_add(fz, df_mul(fzK, tmp));
+        fz = df_add(fz, df_mul(hp, tmp));
+        const dfloat Bd = df_add(xzrot298[i], df_mul(fz, df_add(xlamB0[i], df_mul(twoOvPi, fV))));
+        const dfloat AiB = df_div(df_mul(df_add(df_neg(fV), 2.5f), fz), Bd);  // A / B
+        const dfloat fT = df_add(df_neg(df_mul(xlamK5[i], AiB)), 2.5f);
+        const dfloat fR = df_mul(fV, df_add(df_mul(twoOvPi, AiB), 1.0f));
+        const dfloat CvV = df_sub(df_mul(df_from_bits(cpk[i]), xW[i]), xCvVoff[i]);
+        const dfloat s = df_add(df_add(df_mul(fT, CvT), df_mul(fR, xCvRot[i])), df_mul(fV, CvV));
+        l = df_mul(df_mul(muk[i], xiW[i]), s);
+      }
+      a = df_add(a, df_mul(x[i], l));
+      sxl = df_add(sxl, df_div(x[i], l));
+    }
+    lam = df_to_double_bits(df_mul(df_mul(df_add(a, df_rcp(sxl)), 0.5f), xilamRef));
+    // binary diffusion coefficients: 1 / D_ij = difK P omega_D(T kb/eps_ij) / T^1.5
+    const dfloat PisT3 = df_mul(df_mul(P, Tinv), isT);
+    dfloat Ds[NS];
+#pragma unroll
+    for (int i = 0; i < NS; i++) Ds[i] = df_from(0.0f);
+#pragma unroll
+    for (int i = 0; i < NS; i++)
+#pragma unroll
+      for (int j = 0; j < i; j++) {
+        dfloat nb, db;
+        omega_D_df(df_mul(T, xdifEps[i][j]), nb, db);
+        const dfloat inv = df_div(df_mul(df_mul(xdifK[i][j], PisT3), nb), db);
+        Ds[i] = df_add(Ds[i], df_mul(x[j], inv));
+        Ds[j] = df_add(Ds[j], df_mul(x[i], inv));
+      }
+    const dfloat MixW = df_from_bits(MixW_d);
+#pragma unroll
+    for (int i = 0; i < NS; i++) {
+      dfloat num = df_from(0.0f);
+#pragma unroll
+      for (int j = 0; j < NS; j++)
+        if (j != i) num = df_add(num, df_mul(x[j], xW[j]));
+      D[i] = df_to_double_bits(df_mul(df_div(num, df_mul(MixW, Ds[i])), xiDiRef));
     }
   }
 

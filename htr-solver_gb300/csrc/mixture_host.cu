@@ -318,6 +318,33 @@ bool derive(const htr_airmix_t &s, AirDev &d) {
   d.ilamRef = s.ilamRef;
   d.iDiRef = s.iDiRef;
   d.iwiRef = s.iwiRef;
+  // double-float copies for TransportDF
+  for (int i = 0; i < 5; i++) {
+    d.xkbOveps[i] = df_from(d.kbOveps[i]);
+    d.xmuC[i] = df_from(d.muC[i]);
+    d.xfvK[i] = df_from(d.fvK[i]);
+    d.xiKbOveps[i] = df_from(d.iKbOveps[i]);
+    d.xisqKbOveps[i] = df_from(d.isqKbOveps[i]);
+    d.xzrot298[i] = df_from(d.zrot298[i]);
+    d.xlamB0[i] = df_from(d.lamB0[i]);
+    d.xlamK5[i] = df_from(d.lamK5[i]);
+    d.xlamMono[i] = df_from(d.lamMono[i]);
+    d.xCvRot[i] = df_from(d.CvRot[i]);
+    d.xCvVoff[i] = df_from(d.CvVoff[i]);
+    d.xW[i] = df_from(d.W[i]);
+    d.xiW[i] = df_from(d.iW[i]);
+    for (int j = 0; j < 5; j++) {
+      d.xwilkeA[i][j] = df_from(d.wilkeA[i][j]);
+      d.xwilkeBi[i][j] = df_from(d.wilkeBi[i][j]);
+      d.xdifEps[i][j] = df_from(d.difEps[i][j]);
+      d.xdifK[i][j] = df_from(d.difK[i][j]);
+    }
+  }
+  d.xpi15 = df_from(d.pi15);
+  d.xPRef = df_from(d.PRef);
+  d.ximuRef = df_from(d.imuRef);
+  d.xilamRef = df_from(d.ilamRef);
+  d.xiDiRef = df_from(d.iDiRef);
   return s.TRef > 0 && s.PRef > 0;
 }
 

@@ -318,7 +318,7 @@ HTR_D void refresh_cell(const UpdateArgs &A, const Mix &mix, const long long *p,
     const double iTn = Tinv * mix.TRef;
     *A.rho.at(p) = Pn * Wr * iTn;
     double m_, l_;
-    mix.TransportFast(Td, Tinv, Pn, MixWx, x, cpk, m_, l_, d);
+    mix.TransportDF(Td, Tinv, Pn, MixWx, x, cpk, m_, l_, d);
     *A.mu.at(p) = m_;
     *A.lam.at(p) = l_;
     const double iMixWx = 1.0 / MixWx;
