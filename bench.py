@@ -162,7 +162,7 @@ def choose_dt(dev, gh, lib, runtime):
 
 
 STAGE_KERNELS = ["prepass", "kg_faces_z", "kg_faces_y", "kg_faces_x", "teno_faces",
-                 "diffusion_faces_z", "diffusion_faces_y", "diffusion_faces_x", "stage_update"]
+                 "diffusion_faces_z", "diffusion_faces_y", "diffusion_faces_x", "stage_update", "stage_transport"]
 
 
 def kernel_profile(dev, gh, lib, runtime, dt, reps=3):
@@ -532,7 +532,8 @@ def run_served(args, device, rate=200.0):
     serve.Server(device=device, streams=2).run(warm)
     serve.run_plain([serve.Request(r.rid, r.kind, r.size, r.seed, r.steps, 0.0) for r in warm], device=device)
     log("served: server")
-    server = serve.Server(device=device, hbm_budget=150e9, streams=8)
+    rc = args.serve_round_cells if args.serve_round_cells > 0 else None
+    server = serve.Server(device=device, hbm_budget=150e9, streams=8, round_cells=rc)
     t0 = time.perf_counter()
     server.run(mix)
     t_srv = time.perf_counter() - t0
@@ -549,7 +550,7 @@ def run_served(args, device, rate=200.0):
             "plain": {"value": b["solves_per_s"], "tts_p50_s": b["tts_p50_s"], "tts_p99_s": b["tts_p99_s"],
                       "cell_updates_per_s": cells / t_plain},
             "speedup_vs_plain": t_plain / t_srv,
-            "config": {"requests": len(mix), "arrival_rate_per_s": rate, "steps": [20, 100],
+            "config": {"requests": len(mix), "arrival_rate_per_s": rate, "steps": [20, 100], "round_cells": rc,
                        "kinds": {k: sum(r.kind == k for r in mix) for k in ("tube", "vortex", "box")},
                        "sizes": {"tube": [256, 8192], "vortex": [64, 512], "box": [32, 96]},
                        "note": "steps scaled by 1/20 from the served configuration to bound the run; "
@@ -1012,6 +1013,8 @@ def main():
     p.add_argument("--tubes", type=int, default=4096, help="batched shock tubes (0: skip)")
     p.add_argument("--serve", type=int, default=32, help="served requests (0: skip)")
     p.add_argument("--serve-rates", default="200", help="Poisson arrival rates per s of the served mix, first reported")
+    p.add_argument("--serve-round-cells", type=float, default=0,
+                   help="cells of the boxes stepped per server round, least remaining work first (0: all)")
     p.add_argument("--wall", default="512,192,128", help="boundary-layer interior cells nx,ny,nz ('' skips)")
     p.add_argument("--wall-steps", type=int, default=10)
     p.add_argument("--no-restart", dest="restart", action="store_false", help="skip the restart dump/load timing")

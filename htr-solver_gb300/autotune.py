@@ -75,7 +75,7 @@ def stage_ms(grids, reps=3, workspace=None, originals=None):
             if originals is not None:
                 for name, a in fl.arrays.items():
                     a.copy_(originals[k].arrays[name])
-            out = (C.c_float * 9)()
+            out = (C.c_float * 10)()  # htr_rk3_stage_profile writes 10 kernel times
             abi.check(l, l.htr_rk3_stage_profile(C.byref(v), fl.interior(), fl.bounds(), C.byref(p), gh,
                                                  C.c_void_p(ptr), nb, out, runtime.stream_handle()), "profile")
             runs.append(sum(out))

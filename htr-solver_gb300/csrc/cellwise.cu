@@ -93,7 +93,7 @@ __global__ void properties_kernel(CellRange R, Fd<double> P, Fd<double> T, Fd<do
     *rho.at(p) = mix.Rho(Pp, Tp, MixW);
     if constexpr (NS > 1) {
       double m, l;
-      mix.Transport(Tp, Pp, MixW, x, m, l, d);
+      mix.TransportAt(Tp, Pp, MixW, x, m, l, d);
       *mu.at(p) = m;
       *lam.at(p) = l;
     } else {

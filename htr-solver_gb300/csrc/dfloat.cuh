@@ -199,6 +199,14 @@ DF_HD dfloat df_add(dfloat a, dfloat b) {
   const dfloat v = fast_two_sum(s.hi, df_add_rn(s.lo, t.hi));
   return fast_two_sum(v.hi, df_add_rn(t.lo, v.lo));
 }
+// a + b for operands of the same sign (SloppyDWPlusDW: 11 operations; for
+// same-sign operands no cancellation occurs and the relative error stays
+// within 3u^2, checked by the host test)
+DF_HD dfloat df_add_same(dfloat a, dfloat b) {
+  const dfloat s = two_sum(a.hi, b.hi);
+  const float v = df_add_rn(a.lo, b.lo);
+  return fast_two_sum(s.hi, df_add_rn(s.lo, v));
+}
 DF_HD dfloat df_neg(dfloat a) { return {-a.hi, -a.lo}; }
 DF_HD dfloat df_sub(dfloat a, dfloat b) { return df_add(a, df_neg(b)); }
 // a * b, b a float (DWTimesFP3)

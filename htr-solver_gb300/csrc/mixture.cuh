@@ -251,19 +251,6 @@ struct AirDev {
   }
 
   // --- transport (Species.inl:145-351, MultiComponent.inl:231-311) ----------
-  static HTR_D double omega_mu(double T) {
-    const double num = 3.3530622607 + T * (2.53272006 + T * (2.9024238575 + T * 0.11186138893));
-    const double den = 0.8662326188 + T * (1.3913958626 + T * (3.158490576 + T * (0.18973411754 + T * 0.00018682962894)));
-    return num / den;
-  }
-  static HTR_D double omega_D(double T) {
-    const double num = 6.8728271691 + T * (9.4122316321 + T * (7.7442359037 + T * 0.23424661229));
-    const double den = 1.45337701568 + T * (5.2269794238 + T * (9.7108519575 + T * (0.46539437353 + T * 0.00041908394781)));
-    return num / den;
-  }
-  HTR_D double Mu(int i, double T) const {
-    return 5 * sqrt(muNum[i] * T) / (muDen[i] * omega_mu(T * kbOveps[i]));
-  }
   // rational fits as numerator / denominator pairs (one division saved per use)
   static HTR_D void omega_mu_nd(double T, double &n, double &d) {
     n = 3.3530622607 + T * (2.53272006 + T * (2.9024238575 + T * 0.11186138893));
@@ -273,92 +260,6 @@ struct AirDev {
     n = 6.8728271691 + T * (9.4122316321 + T * (7.7442359037 + T * 0.23424661229));
     d = 1.45337701568 + T * (5.2269794238 + T * (9.7108519575 + T * (0.46539437353 + T * 0.00041908394781)));
   }
-  // Viscosity, conductivity and mixture-averaged diffusivities in one pass.
-  // Species values are regrouped around shared sqrt(T), 1/sqrt(T), 1/T and
-  // T^1.5 so that each needs about one division; the results differ from the
-  // reference's operation order only by rounding (<= 1e-15 relative).
-  HTR_D void Transport(double Tn, double Pn, double MixW, const double *X, double &mu, double &lam,
-                       double *D) const {
-    const double PI = 3.1415926535898;
-    const double T = Tn * TRef;
-    const double P = Pn * PRef;
-    const double Tinv = 1.0 / T;
-    const double sT = sqrt(T);
-    const double isT = 1.0 / sT;
-    double muk[NS], smu[NS], ismu[NS];
-#pragma unroll
-    for (int i = 0; i < NS; i++) {
-      double n, d;
-      omega_mu_nd(T * kbOveps[i], n, d);
-      const double om_inv = d / n;  // 1/omega_mu
-      muk[i] = muC[i] * sT * om_inv;
-      smu[i] = sqrt(muk[i]);
-      ismu[i] = 1.0 / smu[i];
-    }
-    double m = 0.0;
-#pragma unroll
-    for (int i = 0; i < NS; i++) {
-      double den = 0.0;
-#pragma unroll
-      for (int j = 0; j < NS; j++) {
-        double Phi = 1 + smu[i] * ismu[j] * wilkeA[i][j];
-        Phi *= Phi * wilkeBi[i][j];
-        den += X[j] * Phi;
-      }
-      m += X[i] * muk[i] / den;
-    }
-    mu = m * imuRef;
-    double a = 0.0, b = 0.0;
-#pragma unroll
-    for (int i = 0; i < NS; i++) {
-      double l;
-      if (geom[i] == 0) {
-        l = 15.0 / 4 * muk[i] * kRGAS * iW[i];
-      } else {
-        const double CvROvR = (geom[i] == 1) ? 1.0 : 1.5;
-        const double CvT = 1.5 * kRGAS;
-        const double CvR = CvROvR * kRGAS;
-        const double CvV = Cp(i, T, Tinv) * W[i] - ((geom[i] == 1) ? 3.5 : 4.0) * kRGAS;
-        double n, d;
-        omega_D_nd(T * kbOveps[i], n, d);
-        const double fV = sdC[i] * sT * d / (n * muk[i]);  // Dkk / mu
-        const double tmp = Tinv / kbOveps[i];
-        const double st = isT * isqKbOveps[i];               // sqrt(tmp)
-        const double fz = 1 + 0.5 * pi15 * st + (2 + 0.25 * PI * PI) * tmp + pi15 * (tmp * st);
-        const double A = 2.5 - fV;
-        const double B = zrot298[i] / fz + 2 / PI * (5. / 3 * CvROvR + fV);
-        const double iB = 1.0 / B;
-        const double fT = 2.5 * (1. - 2 * CvR * A * iB / (PI * CvT));
-        const double fR = fV * (1. + 2 * A * iB / PI);
-        l = muk[i] * iW[i] * (fT * CvT + fR * CvR + fV * CvV);
-      }
-      a += X[i] * l;
-      b += X[i] / l;
-    }
-    lam = 0.5 * (a + 1.0 / b) * ilamRef;
-    const double PisT3 = P * Tinv * isT;  // P / T^1.5
-#pragma unroll
-    for (int i = 0; i < NS; i++) D[i] = 0.0;
-#pragma unroll
-    for (int i = 0; i < NS; i++)
-#pragma unroll
-      for (int j = 0; j < i; j++) {
-        double n, d;
-        omega_D_nd(T * difEps[i][j], n, d);
-        const double inv = difK[i][j] * PisT3 * n / d;  // 1 / D_ij
-        D[i] += X[j] * inv;
-        D[j] += X[i] * inv;
-      }
-#pragma unroll
-    for (int i = 0; i < NS; i++) {
-      double num = 0.0;
-#pragma unroll
-      for (int j = 0; j < NS; j++)
-        if (j != i) num += X[j] * W[j];
-      D[i] = num / (MixW * D[i]) * iDiRef;
-    }
-  }
-
   // --- fused per-cell refresh (the update kernel of the fused stage) -------
   // The same physics as TFromInternalEnergy / Transport / HeatCapacity, with
   // the arithmetic regrouped for fewer FP64 operations: species enthalpies
@@ -586,9 +487,11 @@ struct AirDev {
   // species' diffusion partner sum keeps a partner of mole fraction >= 1e-20,
   // i.e. at least two species have such a mole fraction.  A (near) pure
   // mixture takes the FP64 TransportFast.
+  // Horner with positive coefficients at t > 0: every partial sum adds
+  // operands of one sign
   static HTR_D dfloat df_poly(dfloat t, const dfloat *c, int n) {
     dfloat r = c[n - 1];
-    for (int k = n - 2; k >= 0; k--) r = df_add(df_mul(r, t), c[k]);
+    for (int k = n - 2; k >= 0; k--) r = df_add_same(df_mul(r, t), c[k]);
     return r;
   }
   // omega_mu and omega_D as numerator / denominator (the fits of
@@ -653,9 +556,9 @@ struct AirDev {
         if (j == i) continue;
         dfloat phi = df_add(df_mul(df_mul(smu[i], ismu[j]), xwilkeA[i][j]), 1.0f);
         phi = df_mul(df_mul(phi, phi), xwilkeBi[i][j]);
-        den = df_add(den, df_mul(x[j], phi));
+        den = df_add_same(den, df_mul(x[j], phi));
       }
-      m = df_add(m, df_div(df_mul(x[i], muk[i]), den));
+      m = df_add_same(m, df_div(df_mul(x[i], muk[i]), den));
     }
     mu = df_to_double_bits(df_mul(m, ximuRef));
     // species conductivities (Eucken with the rotational and vibrational
@@ -676,9 +579,9 @@ struct AirDev {
         const dfloat st = df_mul(isT, xisqKbOveps[i]);
         const dfloat hp = df_mul(xpi15, st);
         dfloat fz = df_add(df_mul(hp, 0.5f), 1.0f);
-        fz = df_add(fz, df_mul(fzK, tmp));
-        fz = df_add(fz, df_mul(hp, tmp));
-        const dfloat Bd = df_add(xzrot298[i], df_mul(fz, df_add(xlamB0[i], df_mul(twoOvPi, fV))));
+        fz = df_add_same(fz, df_mul(fzK, tmp));
+        fz = df_add_same(fz, df_mul(hp, tmp));
+        const dfloat Bd = df_add_same(xzrot298[i], df_mul(fz, df_add_same(xlamB0[i], df_mul(twoOvPi, fV))));
         const dfloat AiB = df_div(df_mul(df_add(df_neg(fV), 2.5f), fz), Bd);  // A / B
         const dfloat fT = df_add(df_neg(df_mul(xlamK5[i], AiB)), 2.5f);
         const dfloat fR = df_mul(fV, df_add(df_mul(twoOvPi, AiB), 1.0f));
@@ -686,10 +589,10 @@ struct AirDev {
         const dfloat s = df_add(df_add(df_mul(fT, CvT), df_mul(fR, xCvRot[i])), df_mul(fV, CvV));
         l = df_mul(df_mul(muk[i], xiW[i]), s);
       }
-      a = df_add(a, df_mul(x[i], l));
-      sxl = df_add(sxl, df_div(x[i], l));
+      a = df_add_same(a, df_mul(x[i], l));
+      sxl = df_add_same(sxl, df_div(x[i], l));
     }
-    lam = df_to_double_bits(df_mul(df_mul(df_add(a, df_rcp(sxl)), 0.5f), xilamRef));
+    lam = df_to_double_bits(df_mul(df_mul(df_add_same(a, df_rcp(sxl)), 0.5f), xilamRef));
     // binary diffusion coefficients: 1 / D_ij = difK P omega_D(T kb/eps_ij) / T^1.5
     const dfloat PisT3 = df_mul(df_mul(P, Tinv), isT);
     dfloat Ds[NS];
@@ -702,8 +605,8 @@ struct AirDev {
         dfloat nb, db;
         omega_D_df(df_mul(T, xdifEps[i][j]), nb, db);
         const dfloat inv = df_div(df_mul(df_mul(xdifK[i][j], PisT3), nb), db);
-        Ds[i] = df_add(Ds[i], df_mul(x[j], inv));
-        Ds[j] = df_add(Ds[j], df_mul(x[i], inv));
+        Ds[i] = df_add_same(Ds[i], df_mul(x[j], inv));
+        Ds[j] = df_add_same(Ds[j], df_mul(x[i], inv));
       }
     const dfloat MixW = df_from_bits(MixW_d);
 #pragma unroll
@@ -711,9 +614,20 @@ struct AirDev {
       dfloat num = df_from(0.0f);
 #pragma unroll
       for (int j = 0; j < NS; j++)
-        if (j != i) num = df_add(num, df_mul(x[j], xW[j]));
+        if (j != i) num = df_add_same(num, df_mul(x[j], xW[j]));
       D[i] = df_to_double_bits(df_mul(df_div(num, df_mul(MixW, Ds[i])), xiDiRef));
     }
+  }
+
+  // TransportDF at a nondimensional temperature and pressure whose species
+  // heat capacities are not at hand (the task kernels' property refresh)
+  HTR_D void TransportAt(double Tn, double Pn, double MixW, const double *X, double &mu, double &lam,
+                         double *D) const {
+    const double Td = Tn * TRef, Tinv = 1.0 / Td;
+    double cpk[NS];
+#pragma unroll
+    for (int i = 0; i < NS; i++) cpk[i] = Cp(i, Td, Tinv);
+    TransportDF(Td, Tinv, Pn, MixW, X, cpk, mu, lam, D);
   }
 
   // --- kinetics (Reaction.inl, MultiComponent.inl:370-415) ------------------

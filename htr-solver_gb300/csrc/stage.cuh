@@ -133,6 +133,6 @@ cudaError_t launch_stage(const htr_fluid_view &v, const htr_rect3 &interior, con
                          cudaStream_t s, cudaEvent_t *ev = nullptr);
 
 // Events of a profiled stage: start, then one after each kernel.
-enum StageKernel { kPrepass, kKgZ, kKgY, kKgX, kTeno, kDiffZ, kDiffY, kDiffX, kUpdate, kStageKernels };
+enum StageKernel { kPrepass, kKgZ, kKgY, kKgX, kTeno, kDiffZ, kDiffY, kDiffX, kUpdate, kTransport, kStageKernels };
 
 }  // namespace htr

@@ -317,10 +317,8 @@ HTR_D void refresh_cell(const UpdateArgs &A, const Mix &mix, const long long *p,
     const double Wr = MixWx * mix.iMixWRef;
     const double iTn = Tinv * mix.TRef;
     *A.rho.at(p) = Pn * Wr * iTn;
-    double m_, l_;
-    mix.TransportDF(Td, Tinv, Pn, MixWx, x, cpk, m_, l_, d);
-    *A.mu.at(p) = m_;
-    *A.lam.at(p) = l_;
+    // viscosity, conductivity and diffusivities: stage_transport, from the
+    // T, P, X and cached c_p written here
     const double iMixWx = 1.0 / MixWx;
     double c = 0.0;
 #pragma unroll
@@ -359,11 +357,45 @@ HTR_D void refresh_cell(const UpdateArgs &A, const Mix &mix, const long long *p,
     *A.SoS.at(p) = mix.SpeedOfSound(Tn, gamma, MixWx);
   }
   if (its >= 1000 && A.status) atomicMax(A.status, (int)HTR_ERR_ITERATION_CAP);
-  double *dp = A.Di.at(p), *yp = A.Y.at(p);
+  double *yp = A.Y.at(p);
 #pragma unroll
-  for (int k = 0; k < NS; k++) {
-    dp[k] = d[k];
-    yp[k] = y2[k];
+  for (int k = 0; k < NS; k++) yp[k] = y2[k];
+  if constexpr (NS == 1) A.Di.at(p)[0] = d[0];
+}
+
+// Viscosity, conductivity and mixture-averaged diffusivities of the cells
+// that refresh_cell just refreshed (multi-species mixtures): those whose
+// temperature cache entry holds their current temperature.  The inputs are
+// the values refresh_cell wrote and used (T, P, X, 1/T and the species c_p
+// of the final Newton temperature), so the results are those it would have
+// computed.  A kernel of its own because the double-float transport
+// (TransportDF) runs on the FP32 pipe in long dependent chains that the
+// FP64-bound update kernel, at its register count, has too few warps to
+// hide (inside the update kernel: 52.2 ms per 256^3 stage; split: 36.1 ms
+// update + 6.7 ms here).  Five blocks per SM (96 registers, a few hundred
+// bytes of spills) run it 9 % faster than four without spills.
+template <class Mix>
+__global__ void __launch_bounds__(128, 5) stage_transport(const UpdateArgs A, const __grid_constant__ Mix mix) {
+  constexpr int NS = Mix::NS;
+  const long long n = A.dn.count();
+  for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n; i += (long long)gridDim.x * blockDim.x) {
+    long long p[3];
+    A.dn.point(i, p);
+    const double Tn = *A.T.at(p);
+    if (__double_as_longlong(A.tcache[i]) != __double_as_longlong(Tn)) continue;
+    double x[NS], cpk[NS], d[NS], m_, l_;
+    const double *xp = A.X.at(p);
+#pragma unroll
+    for (int k = 0; k < NS; k++) {
+      x[k] = xp[k];
+      cpk[k] = A.tcache[(3 + NS + k) * n + i];
+    }
+    mix.TransportDF(Tn * mix.TRef, A.tcache[2 * n + i], *A.P.at(p), mix.MolarWeightFromXi(x), x, cpk, m_, l_, d);
+    *A.mu.at(p) = m_;
+    *A.lam.at(p) = l_;
+    double *dp = A.Di.at(p);
+#pragma unroll
+    for (int k = 0; k < NS; k++) dp[k] = d[k];
   }
 }
 
@@ -380,7 +412,7 @@ __device__ __noinline__ void boundary_properties(const UpdateArgs &A, const Mix 
   *A.rho.at(p) = r;
   if constexpr (NS > 1) {
     double m, l;
-    mix.Transport(Tp, Pp, MixW, x, m, l, d);
+    mix.TransportAt(Tp, Pp, MixW, x, m, l, d);
     *A.mu.at(p) = m;
     *A.lam.at(p) = l;
   } else {
@@ -825,7 +857,14 @@ cudaError_t launch_stage(const htr_fluid_view &v, const htr_rect3 &my, const htr
     stage_update<Mix, false><<<grid_for(n, ub), ub, 0, s>>>(U, mix);
   }
   if ((e = cudaGetLastError()) != cudaSuccess) return e;
-  return mark(1 + kUpdate);
+  if ((e = mark(1 + kUpdate)) != cudaSuccess) return e;
+  if constexpr (Mix::NS > 1) {
+    if (sp.mode != kStageRhsOnly) {
+      stage_transport<Mix><<<grid_for(n, 128), 128, 0, s>>>(U, mix);
+      if ((e = cudaGetLastError()) != cudaSuccess) return e;
+    }
+  }
+  return mark(1 + kTransport);
 }
 
 template cudaError_t launch_stage<ConstPropDev>(const htr_fluid_view &, const htr_rect3 &, const htr_rect3 &,

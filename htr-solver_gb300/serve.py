@@ -98,6 +98,7 @@ class Instance:
             self.ws = runtime.Workspace()
             self.ws.get(runtime.workspace_bytes(self.dev, self.gh), device)
         self.bytes = sum(a.numel() * a.element_size() for a in self.dev.arrays.values()) + self.ws.nbytes
+        self.cells = self.dev.ncells
         self.remaining = req.steps
         self.graph = None
         if graphs:
@@ -294,9 +295,14 @@ class Server:
     """Continuous batching under an HBM budget (bytes)."""
 
     def __init__(self, device="cuda", hbm_budget=150e9, streams=8, graphs=True, admit_per_round=2,
-                 batch_tubes=True):
+                 batch_tubes=True, round_cells=None):
         import torch
         self.device = device
+        # cells of the boxes stepped per round (None: every active box): the
+        # boxes with the least remaining work (steps left x cells) go first
+        # until their cells reach round_cells, so short requests finish early
+        # (shortest remaining work first) while the round still fills the GPU
+        self.round_cells = round_cells
         self.admit_per_round = admit_per_round  # admissions between rounds (keeps the device busy)
         self.budget = hbm_budget
         self.pool = [torch.cuda.Stream() for _ in range(streams)]
@@ -378,7 +384,7 @@ class Server:
                 ev = torch.cuda.Event()
                 ev.record(g.stream)
                 cur.append(ev)
-            for inst in active:
+            for inst in self.select(active):
                 inst.step()
                 ev = torch.cuda.Event()
                 ev.record(inst.stream)
@@ -391,6 +397,27 @@ class Server:
             self.rounds += 1
         torch.cuda.synchronize()
         return requests
+
+
+    def select(self, active):
+        return round_selection(active, self.round_cells)
+
+
+def round_selection(active, round_cells):
+    """The boxes stepped in one round, in the order they were admitted: all
+    of them without a cell budget, else those with the least remaining work
+    (steps left x cells; ties by admission) until their cells reach
+    round_cells.  Items need `remaining` and `cells`."""
+    if round_cells is None or len(active) <= 1:
+        return list(active)
+    order = sorted(range(len(active)), key=lambda k: (active[k].remaining * active[k].cells, k))
+    chosen, cells = set(), 0
+    for k in order:
+        chosen.add(k)
+        cells += active[k].cells
+        if cells >= round_cells:
+            break
+    return [inst for k, inst in enumerate(active) if k in chosen]
 
 
 def run_plain(requests, device="cuda", clock=time.perf_counter):

@@ -442,8 +442,9 @@ int htr_rk3_get_tuning(htr_stage_tuning *tuning);
 /* Profiling aid, no counterpart in the reference: copies Conserved to
  * Conserved_old, runs stage 1 of the fused pipeline once (deltaTime, no
  * sensor update) with CUDA events between its kernels, waits for it, and
- * writes the milliseconds of each kernel to ms_out[9]: prepass, KG faces Z,
- * Y, X, TENO faces, diffusion faces Z, Y, X, per-cell update.  The state
+ * writes the milliseconds of each kernel to ms_out[10]: prepass, KG faces Z,
+ * Y, X, TENO faces, diffusion faces Z, Y, X, per-cell update, transport
+ * properties (multi-species mixtures; 0 for a single species).  The state
  * advances by that forward-Euler stage. */
 int htr_rk3_stage_profile(const htr_fluid_view *view, htr_rect3 interior, htr_rect3 fluid_bounds,
                           const htr_step_params *params, htr_mixture_t mix, void *workspace,

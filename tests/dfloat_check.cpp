@@ -26,7 +26,7 @@ static dfloat rnd(double lo_exp, double hi_exp, bool sign) {
 int main() {
   const double u2 = std::ldexp(1.0, -48);
   double e_add = 0, e_addpos = 0, e_mul = 0, e_mulf = 0, e_div = 0, e_rcp = 0, e_sqrt = 0, e_conv = 0;
-  double e_bits = 0, e_bits_small = 0;
+  double e_bits = 0, e_bits_small = 0, e_same = 0;
   long bits_back_mismatch = 0;
   for (int k = 0; k < 2000000; k++) {
     const dfloat a = rnd(-20, 20, true), b = rnd(-20, 20, true);
@@ -41,6 +41,8 @@ int main() {
     const double es = std::fabs(htr::df_to_double(htr::df_add(a, b)) - s) / (std::fabs(A) + std::fabs(B));
     e_add = std::fmax(e_add, es / u2);
     e_addpos = std::fmax(e_addpos, rel(htr::df_add(p, q), P + Q) / u2);
+    e_same = std::fmax(e_same, rel(htr::df_add_same(p, q), P + Q) / u2);
+    e_same = std::fmax(e_same, rel(htr::df_add_same(htr::df_neg(p), htr::df_neg(q)), -(P + Q)) / u2);
     e_mul = std::fmax(e_mul, rel(htr::df_mul(a, b), A * B) / u2);
     e_mulf = std::fmax(e_mulf, rel(htr::df_mul(a, b.hi), A * (double)b.hi) / u2);
     e_div = std::fmax(e_div, rel(htr::df_div(a, b), A / B) / u2);
@@ -57,6 +59,7 @@ int main() {
     const double z = std::exp2(-126 + 52 * uniform()) * (1.0 + uniform());
     e_bits_small = std::fmax(e_bits_small, std::fabs(htr::df_to_double(htr::df_from_bits(z)) - z) / z);
   }
+  std::printf("same %.3f ", e_same);
   std::printf("add %.3f addpos %.3f mul %.3f mulf %.3f div %.3f rcp %.3f sqrt %.3f conv %.3f bits %.3f "
               "bits_small %.3e bits_back_mismatch %ld zero %d\n", e_add, e_addpos, e_mul, e_mulf, e_div, e_rcp, e_sqrt,
               e_conv, e_bits, e_bits_small, bits_back_mismatch,

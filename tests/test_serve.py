@@ -29,6 +29,18 @@ def test_admission_is_fifo_under_budget():
     assert serve.admissible(big, now=1.0, used=0, budget=serve.estimate_bytes(big[0]) - 1) == 0
 
 
+def test_round_selection_is_shortest_remaining_work_first():
+    from types import SimpleNamespace as NS
+    active = [NS(remaining=r, cells=c) for r, c in ((100, 1000), (5, 1000), (50, 10), (1, 5000), (5, 1000))]
+    assert serve.round_selection(active, None) == active
+    # least remaining work first: #2 (500), then #1, #3, #4 (5000 each, in
+    # admission order), then #0
+    assert serve.round_selection(active, 1) == [active[2]]
+    assert serve.round_selection(active, 1010) == [active[1], active[2]]
+    assert serve.round_selection(active, 2010) == [active[1], active[2], active[3]]
+    assert serve.round_selection(active, 10 ** 9) == active
+
+
 def test_estimate_covers_sizes():
     sizes = [serve.estimate_bytes(serve.Request(0, k, n, 0, 1, 0.0))
              for k, n in (("tube", 256), ("tube", 8192), ("vortex", 64), ("vortex", 512), ("box", 32), ("box", 96))]
