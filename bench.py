@@ -206,13 +206,15 @@ KERNEL_BYTES = {
 # Executed FP64 floating-point operations per cell (per face for the face
 # kernels) of the same kernels: DADD + DMUL + 2 x DFMA thread instructions
 # counted by ncu on the 96^3 case of this workload (profiles/
-# stage_kernels_air96_hybrid.md).  The kernels are bound by the FP64 pipe;
+# stage_kernels_air96_hybrid.md, profiles/stage_update_transport_air96.md).  The kernels are bound by the FP64 pipe;
 # this gives their achieved FP64 rate next to the memory roofline.
-KERNEL_FP64_FLOPS = {"prepass": 80.0, "kg_faces": 259.0, "diffusion_faces": 320.0, "stage_update": 2559.0}
+KERNEL_FP64_FLOPS = {"prepass": 80.0, "kg_faces": 259.0, "diffusion_faces": 320.0, "stage_update": 1297.0,
+                     "stage_transport": 18.0}
 # DRAM bytes per cell (dram__bytes_read.sum + dram__bytes_write.sum of one
 # launch) measured by ncu on the 96^3 case (state larger than L2); the
 # per-launch traffic scales with the cells (profiles/stage_kernels_air96_hybrid.md).
-KERNEL_DRAM_BYTES = {"prepass": 248.0, "kg_faces": 124.0, "diffusion_faces": 316.0, "stage_update": 1029.0}
+KERNEL_DRAM_BYTES = {"prepass": 248.0, "kg_faces": 124.0, "diffusion_faces": 316.0, "stage_update": 1202.0,
+                     "stage_transport": 139.0}
 
 
 STATE_FIELDS = ["Conserved", "pressure", "temperature", "MassFracs", "MolarFracs", "velocity",
@@ -522,7 +524,9 @@ def run_served(args, device, rate=200.0):
     session) and asking for 20-100 RK3 steps (the served configuration's
     100-2000 scaled by 1/20 so the run stays bounded).  The server
     (continuous batching: the tubes of one mixture stepped together in one
-    strip, the boxes as per-request CUDA graphs, on 8 streams; 150 GB budget)
+    strip, the boxes as per-request CUDA graphs, on 8 streams; each round
+    steps the boxes with the least remaining work up to --serve-round-cells
+    cells; 150 GB budget)
     against the plain per-request path (one request at a time, task
     kernels)."""
     mix = serve.prepare(serve.request_mix(args.serve, rate=rate, seed=777, steps=(20, 100), tube=(256, 8192),
@@ -831,7 +835,10 @@ def run_gpu(args):
     # Conserved back.  Two device states alternate so that the copies of one
     # step overlap the compute of the previous one (copy streams + events).
     log("end-to-end")
+    clocks_e2e = ClockSampler(local)
+    clocks_e2e.start()
     e2e_value, h2d, d2h, e2e_steps = e2e_pipelined(dev, gh, dt, args.steps, runtime, barrier, device)
+    clk_e2e = clocks_e2e.stop()
 
     result = None
     if rank == 0:
@@ -865,7 +872,8 @@ def run_gpu(args):
             "e2e": {"value": e2e_value, "unit": UNIT, "h2d_bytes_per_step": int(h2d),
                     "d2h_bytes_per_step": int(d2h), "steps": e2e_steps,
                     "copies": "11 state fields H2D and Conserved D2H every step, pinned host memory, "
-                              "double-buffered on copy streams overlapping the previous step"},
+                              "double-buffered on copy streams overlapping the previous step",
+                    "clocks": clk_e2e},
             "roofline": roof,
             "teno_face_fraction": teno,
             "kernel_ms_per_stage": prof,
@@ -1012,8 +1020,9 @@ def main():
     p.add_argument("--no-cpu-baseline", dest="cpu_baseline", action="store_false")
     p.add_argument("--tubes", type=int, default=4096, help="batched shock tubes (0: skip)")
     p.add_argument("--serve", type=int, default=32, help="served requests (0: skip)")
-    p.add_argument("--serve-rates", default="200", help="Poisson arrival rates per s of the served mix, first reported")
-    p.add_argument("--serve-round-cells", type=float, default=0,
+    p.add_argument("--serve-rates", default="200,50,2000",
+                   help="Poisson arrival rates per s of the served mix, first reported")
+    p.add_argument("--serve-round-cells", type=float, default=2e6,
                    help="cells of the boxes stepped per server round, least remaining work first (0: all)")
     p.add_argument("--wall", default="512,192,128", help="boundary-layer interior cells nx,ny,nz ('' skips)")
     p.add_argument("--wall-steps", type=int, default=10)

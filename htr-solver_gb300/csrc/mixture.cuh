@@ -69,6 +69,7 @@ struct AirReac {  // one reaction, standard or third-body
   double A, n, EovR;
   double nuE[2], nuP[2];
   double effm1[5];  // efficiency - 1
+  double sumNu;     // sum nuP - sum nuE
   int nEd, nPd, nTb;
   int ed[2], pd[2], tb[5];
   bool backward;
@@ -85,6 +86,7 @@ struct AirDev {
   double cp[NS][3][7];   // NASA coefficients c0..c6 per range (0 high, 1 mid, 2 low)
   double hc[NS][3][8];   // enthalpy: -c0, c1, c7, c2, c3*0.50, c4/3, c5*0.25, c6/5
   double gc[NS][3][9];   // free enthalpy: -0.5*c0, c1, c2, c7, c8, c3, c4/3, c5/6, c6
+  double gf[NS][3][9];   // the same regrouped (FreeEnthalpyFast): g0, g1+g3, g1, g2, g2-g4, g5/2, g6/2, g7/2, g8/20
   // transport (T-independent factors of Species.inl:145-351, MultiComponent.inl:231-311)
   double muNum[NS];      // PI*W/Na*kb  (mu numerator is 5*sqrt(muNum*T))
   double muDen[NS];      // 16*PI*sigma^2
@@ -121,6 +123,7 @@ struct AirDev {
   AirReac reac[5];
   // reference scales
   double TRef, PRef, rhoRef, iMixWRef, ieRef, iCpRef, imuRef, ilamRef, iDiRef, iwiRef;
+  double MixWRef;  // 1 / iMixWRef
 
   HTR_HD int range(int i, double T) const { return (T > TS2[i]) ? 0 : ((T > TS1[i]) ? 1 : 2); }
 
@@ -141,6 +144,18 @@ struct AirDev {
     const double *c = gc[i][range(i, T)];
     const double G = c[0] * Tinv * Tinv + c[1] * Tinv * (1.0 + logT) + c[2] * (1.0 - logT) + c[3] * Tinv - c[4];
     return G - 0.5 * T * (c[5] + T * (c[6] + T * (c[7] + 0.1 * T * c[8])));
+  }
+
+  // The same free enthalpy with its T-independent combinations folded on the
+  // host: G = Tinv (g0 Tinv + g1 + g3) + logT (g1 Tinv - g2) + (g2 - g4)
+  //         - T (g5/2 + T (g6/2 + T (g7/2 + T g8/20)))
+  // (nine operations; the explicit chemistry sources)
+  HTR_D double FreeEnthalpyFast(int i, double T, double Tinv, double logT) const {
+    const double *c = gf[i][range(i, T)];
+    const double a = fma(c[0], Tinv, c[1]) * Tinv;
+    const double b = fma(fma(c[2], Tinv, -c[3]), logT, a) + c[4];
+    const double q = fma(fma(fma(c[8], T, c[7]), T, c[6]), T, c[5]);
+    return fma(-T, q, b);
   }
 
   HTR_HD void ClipYi(double *Y) const {
@@ -309,11 +324,13 @@ struct AirDev {
         const double r = (Tn - Td) * Tinv;
         if (fabs(r) < 0.0009765625) {
           logT += r * (1.0 + r * (-0.5 + r * (1.0 / 3 + r * (-0.25 + r * (0.2 + r * (-1.0 / 6))))));
+          // 1/(T (1 + r)) = (1/T) (1 - r + r^2 - ... - r^5), remainder below 2^-60
+          Tinv *= 1.0 + r * (-1.0 + r * (1.0 + r * (-1.0 + r * (1.0 - r))));
         } else {
           logT = log(Tn);
+          Tinv = 1.0 / Tn;
         }
         Td = Tn;
-        Tinv = 1.0 / Td;
       }
       if (j == 0 && h0 != nullptr) {
 #pragma unroll
@@ -328,7 +345,9 @@ struct AirDev {
 #pragma unroll
       for (int i = 0; i < NS; i++) e += Y[i] * (h[i] - rOvW[i] * Td);
       const double f = e0 - e * ieRef;
-      if (fabs(f / dfdT) < TOL) break;
+      // |f / dfdT| < TOL without the division (dfdT, a heat capacity, is
+      // positive)
+      if (fabs(f) < TOL * dfdT) break;
       double d = 0.0;
 #pragma unroll
       for (int i = 0; i < NS; i++) d += Y[i] * (cpk[i] - rOvW[i]);
@@ -707,15 +726,17 @@ struct AirDev {
                               const double *Y) const {
     const double P = Pn * PRef;
     const double rho = rhon * rhoRef;
-    const double lnRP = log(kRGAS / P);
+    // collider concentration P / (R T), and log(R T / P) = -log(cM) for the
+    // equilibrium constants
+    const double cM = P * Tinv * (1.0 / kRGAS);
+    const double lncM = log(cM);
     double G[NS], C[NS];
 #pragma unroll
     for (int i = 0; i < NS; i++) {
       w[i] = 0.0;
       C[i] = Y[i] * rho * iW[i];
-      G[i] = FreeEnthalpy(i, T, Tinv, logT);
+      G[i] = FreeEnthalpyFast(i, T, Tinv, logT);
     }
-    const double cM = P / (kRGAS * T);
 #pragma unroll
     for (int k = 0; k < 5; k++) {
       const AirReac &r = reac[k];
@@ -731,20 +752,15 @@ struct AirDev {
         if (i < r.nEd) a *= (r.nuE[i] == 1.0) ? C[r.ed[i]] : ((r.nuE[i] == 2.0) ? C[r.ed[i]] * C[r.ed[i]] : pow(C[r.ed[i]], r.nuE[i]));
       double Kb = 0.0, b = 1.0;
       if (r.backward) {
-        double sumNu = 0.0, sumNuG = 0.0;
+        double sumNuG = 0.0;
 #pragma unroll
         for (int i = 0; i < 2; i++)
-          if (i < r.nEd) {
-            sumNu -= r.nuE[i];
-            sumNuG -= r.nuE[i] * G[r.ed[i]];
-          }
+          if (i < r.nEd) sumNuG -= r.nuE[i] * G[r.ed[i]];
 #pragma unroll
         for (int i = 0; i < 2; i++)
-          if (i < r.nPd) {
-            sumNu += r.nuP[i];
-            sumNuG += r.nuP[i] * G[r.pd[i]];
-          }
-        const double lnKc = -sumNuG - sumNu * (logT + lnRP);
+          if (i < r.nPd) sumNuG += r.nuP[i] * G[r.pd[i]];
+        // ln Kc = -sum nu G - sum nu log(R T / P)
+        const double lnKc = r.sumNu * lncM - sumNuG;
         Kb = r.A * exp_table(arg - lnKc);
 #pragma unroll
         for (int i = 0; i < 2; i++)

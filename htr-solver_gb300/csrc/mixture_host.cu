@@ -228,6 +228,8 @@ bool derive(const htr_airmix_t &s, AirDev &d) {
       for (int k = 0; k < 8; k++) d.hc[i][r][k] = h[k];
       const double g[9] = {-0.5 * c[0], c[1], c[2], c[7], c[8], c[3], c[4] / 3, c[5] / 6, c[6]};
       for (int k = 0; k < 9; k++) d.gc[i][r][k] = g[k];
+      const double gf[9] = {g[0], g[1] + g[3], g[1], g[2], g[2] - g[4], 0.5 * g[5], 0.5 * g[6], 0.5 * g[7], 0.05 * g[8]};
+      for (int k = 0; k < 9; k++) d.gf[i][r][k] = gf[k];
     }
     d.muNum[i] = kPI * sp.W / kNa * kKb;
     d.muDen[i] = 16 * kPI * std::pow(sp.DiffCoeff.sigma, 2);
@@ -296,6 +298,9 @@ bool derive(const htr_airmix_t &s, AirDev &d) {
       r.tb[i] = (i < nt) ? tb[i].ind : 0;
       r.effm1[i] = (i < nt) ? double(tb[i].eff) - 1.0 : 0.0;
     }
+    r.sumNu = 0.0;
+    for (int i = 0; i < ne; i++) r.sumNu -= double(ed[i].nu);
+    for (int i = 0; i < np; i++) r.sumNu += double(pd[i].nu);
   };
   for (int k = 0; k < 2; k++) {
     const htr_reaction_t &r = s.reactions[k];
@@ -318,6 +323,7 @@ bool derive(const htr_airmix_t &s, AirDev &d) {
   d.ilamRef = s.ilamRef;
   d.iDiRef = s.iDiRef;
   d.iwiRef = s.iwiRef;
+  d.MixWRef = 1.0 / s.iMixWRef;
   // double-float copies for TransportDF
   for (int i = 0; i < 5; i++) {
     d.xkbOveps[i] = df_from(d.kbOveps[i]);

@@ -305,7 +305,7 @@ HTR_D void refresh_cell(const UpdateArgs &A, const Mix &mix, const long long *p,
       A.tcache[(3 + k) * n + i] = hk[k];
       A.tcache[(3 + NS + k) * n + i] = cpk[k];
     }
-    const double Pn = rho * Tn * s / mix.iMixWRef;
+    const double Pn = rho * Tn * s * mix.MixWRef;
     *A.T.at(p) = Tn;
     *A.P.at(p) = Pn;
     double *xp = A.X.at(p), *up = A.u.at(p);
@@ -313,6 +313,10 @@ HTR_D void refresh_cell(const UpdateArgs &A, const Mix &mix, const long long *p,
     for (int k = 0; k < NS; k++) xp[k] = x[k];
 #pragma unroll
     for (int k = 0; k < 3; k++) up[k] = vel[k];
+    // the molar weight and the mass fractions recomputed from X, as the
+    // reference's property refresh does: they normalise the clipped Yi,
+    // whose sum differs from 1 where clipping raised negative partial
+    // densities
     const double MixWx = mix.MolarWeightFromXi(x);
     const double Wr = MixWx * mix.iMixWRef;
     const double iTn = Tinv * mix.TRef;
@@ -320,6 +324,7 @@ HTR_D void refresh_cell(const UpdateArgs &A, const Mix &mix, const long long *p,
     // viscosity, conductivity and diffusivities: stage_transport, from the
     // T, P, X and cached c_p written here
     const double iMixWx = 1.0 / MixWx;
+    const double iWr = iMixWx * mix.MixWRef;
     double c = 0.0;
 #pragma unroll
     for (int k = 0; k < NS; k++) {
@@ -327,7 +332,6 @@ HTR_D void refresh_cell(const UpdateArgs &A, const Mix &mix, const long long *p,
       c += y2[k] * cpk[k];
     }
     c *= mix.iCpRef;
-    const double iWr = 1.0 / Wr;
     const double gamma = c / (c - iWr);
     *A.SoS.at(p) = sqrt(gamma * Tn * iWr);
   } else {
