@@ -182,7 +182,7 @@ __global__ void primitive_kernel(CellRange R, Fd<double> C, Fd<double> T, Fd<dou
     for (int i = 0; i < 3; i++) vel[i] = ld(&c[NS + i]) * rhoInv;
     const double e = ld(&c[NS + 3]) * rhoInv - 0.5 * mod2(vel);
     int its = 0;
-    const double Tn = mix.TFromInternalEnergy(e, *T.at(p), Yi, &its);
+    const double Tn = mix.TFromInternalEnergyFast(e, *T.at(p), Yi, &its);
     if (its >= 1000) flag_status(status, HTR_ERR_ITERATION_CAP);
     *T.at(p) = Tn;
     *P.at(p) = mix.PFromRhoAndT(rho, MixW, Tn);

@@ -163,10 +163,9 @@ template <class Mix, int D> struct EulerFace {
     const double PovRho = R.H - R.e - 0.5 * mod2(R.vel);
     const double MixW = mix.MolarWeightFromYi(R.Yi);
     const double Teos = mix.TFromRhoAndP(R.rho, MixW, PovRho * R.rho);
-    const double T = mix.TFromInternalEnergy(R.e, Teos, R.Yi, nullptr);
-    const double gamma = mix.Gamma(T, MixW, R.Yi);
+    double gamma;
+    mix.RoeThermo(R.e, Teos, MixW, R.Yi, gamma, R.dpdrhoi);
     R.dpde = mix.dpde(R.rho, gamma);
-    mix.dpdrhoi(R.dpdrhoi, gamma, T, R.Yi);
     const double dp = PR - PL;
     const double de = eR - eL;
     double drhoi[NS];

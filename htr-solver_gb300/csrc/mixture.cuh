@@ -41,6 +41,9 @@ struct ConstPropDev {
   HTR_HD double TFromInternalEnergy(double e0, double, const double *, int *) const {
     return e0 * (gamma - 1.0) / R;
   }
+  HTR_HD double TFromInternalEnergyFast(double e0, double T, const double *Y, int *its) const {
+    return TFromInternalEnergy(e0, T, Y, its);
+  }
   HTR_HD double TFromRhoAndP(double rho, double MixW, double P) const { return P * MixW / (rho * kRGAS); }
   HTR_HD double PFromRhoAndT(double rho, double MixW, double T) const { return rho * kRGAS * T / MixW; }
   HTR_D double Viscosity(double T, const double *) const {
@@ -58,6 +61,13 @@ struct ConstPropDev {
   HTR_HD void ProductionRates(double *w, double, double, double, const double *) const { w[0] = 0.0; }
   HTR_HD void ProductionRatesRef(double *w, double, double, double, const double *) const { w[0] = 0.0; }
   HTR_HD double dpde(double rho, double g) const { return rho * (g - 1); }
+  // temperature, gamma and dp/drho_i of a Roe-averaged state (the Euler flux)
+  HTR_D double RoeThermo(double e, double Teos, double MixW, const double *Y, double &gamma_, double *dpdrhoi_) const {
+    const double T = TFromInternalEnergy(e, Teos, Y, nullptr);
+    gamma_ = Gamma(T, MixW, Y);
+    dpdrhoi(dpdrhoi_, gamma_, T, Y);
+    return T;
+  }
   HTR_HD void dpdrhoi(double *d, double, double T, const double *) const { d[0] = R * T; }
 };
 
@@ -263,6 +273,38 @@ struct AirDev {
     }
 #pragma unroll
     for (int i = 0; i < NS; i++) d[i] = (kRGAS * T / W[i] + (g - 1) * (e - d[i])) * ieRef;
+  }
+
+  // The reference's Newton for T from e with the fused species h and c_p
+  // (the task kernels' primitive recovery)
+  HTR_D double TFromInternalEnergyFast(double e0, double T, const double *Y, int *its) const {
+    double cpk[NS], Td, Tinv, logT;
+    return TFromInternalEnergyCp(e0, T, Y, its, cpk, Td, Tinv, logT);
+  }
+  // Temperature, gamma and dp/drho_i of a Roe-averaged state (the Euler
+  // flux, rhs.inl:198-279): the reference's Newton from Teos
+  // (TFromInternalEnergy: same start, tolerance and test) evaluated with the
+  // fused species h and c_p of TFromInternalEnergyCp, whose values at the
+  // returned temperature then give gamma (HeatCapacity) and dp/drho_i
+  // (dpdrhoi) without evaluating them again.
+  HTR_D double RoeThermo(double e, double Teos, double MixW, const double *Y, double &gamma_,
+                         double *dpdrhoi_) const {
+    double cpk[NS], h[NS], Td, Tinv, logT;
+    const double T = TFromInternalEnergyCp(e, Teos, Y, nullptr, cpk, Td, Tinv, logT, false, nullptr, nullptr, h);
+    double c = 0.0;
+#pragma unroll
+    for (int i = 0; i < NS; i++) c += Y[i] * cpk[i];
+    c *= iCpRef;
+    gamma_ = c / (c - 1.0 / (MixW * iMixWRef));
+    double ed = 0.0;
+#pragma unroll
+    for (int i = 0; i < NS; i++) {
+      dpdrhoi_[i] = h[i] - rOvW[i] * Td;
+      ed += Y[i] * dpdrhoi_[i];
+    }
+#pragma unroll
+    for (int i = 0; i < NS; i++) dpdrhoi_[i] = (rOvW[i] * Td + (gamma_ - 1) * (ed - dpdrhoi_[i])) * ieRef;
+    return T;
   }
 
   // --- transport (Species.inl:145-351, MultiComponent.inl:231-311) ----------
