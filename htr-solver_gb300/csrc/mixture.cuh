@@ -80,6 +80,7 @@ struct AirReac {  // one reaction, standard or third-body
   double nuE[2], nuP[2];
   double effm1[5];  // efficiency - 1
   double sumNu;     // sum nuP - sum nuE
+  int nuEk[2], nuPk[2];  // 1 or 2 where nu is exactly that, else 0 (tested on the integer pipe)
   int nEd, nPd, nTb;
   int ed[2], pd[2], tb[5];
   bool backward;
@@ -93,6 +94,7 @@ struct AirDev {
   // species
   double W[NS], rOvW[NS];  // rOvW = RGAS/W
   double TS1[NS], TS2[NS]; // NASA range switches (the reference's floats, promoted)
+  long long TS1b[NS], TS2b[NS];  // their bit patterns (range)
   double cp[NS][3][7];   // NASA coefficients c0..c6 per range (0 high, 1 mid, 2 low)
   double hc[NS][3][8];   // enthalpy: -c0, c1, c7, c2, c3*0.50, c4/3, c5*0.25, c6/5
   double gc[NS][3][9];   // free enthalpy: -0.5*c0, c1, c2, c7, c8, c3, c4/3, c5/6, c6
@@ -135,7 +137,14 @@ struct AirDev {
   double TRef, PRef, rhoRef, iMixWRef, ieRef, iCpRef, imuRef, ilamRef, iDiRef, iwiRef;
   double MixWRef;  // 1 / iMixWRef
 
-  HTR_HD int range(int i, double T) const { return (T > TS2[i]) ? 0 : ((T > TS1[i]) ? 1 : 2); }
+  // T > TS2 ? 0 : (T > TS1 ? 1 : 2), compared on the integer pipe: the bit
+  // patterns of doubles order like their values when the switch
+  // temperatures are positive (a negative T is below both, as compared in
+  // double)
+  HTR_HD int range(int i, double T) const {
+    const long long b = (long long)df_bits(T);
+    return (b > TS2b[i]) ? 0 : ((b > TS1b[i]) ? 1 : 2);
+  }
 
   // Species.inl:84-101
   HTR_D double Cp(int i, double T, double Tinv) const {
@@ -718,7 +727,7 @@ struct AirDev {
       double a = 1.0;
 #pragma unroll
       for (int i = 0; i < 2; i++)
-        if (i < r.nEd) a *= (r.nuE[i] == 1.0) ? C[r.ed[i]] : pow(C[r.ed[i]], r.nuE[i]);
+        if (i < r.nEd) a *= (r.nuEk[i] == 1) ? C[r.ed[i]] : pow(C[r.ed[i]], r.nuE[i]);
       double Kb = 0.0, b = 1.0;
       if (r.backward) {
         double sumNu = 0.0, sumNuG = 0.0;
@@ -738,7 +747,7 @@ struct AirDev {
         Kb = Kf * exp(-lnKc);
 #pragma unroll
         for (int i = 0; i < 2; i++)
-          if (i < r.nPd) b *= (r.nuP[i] == 1.0) ? C[r.pd[i]] : pow(C[r.pd[i]], r.nuP[i]);
+          if (i < r.nPd) b *= (r.nuPk[i] == 1) ? C[r.pd[i]] : pow(C[r.pd[i]], r.nuP[i]);
       }
       double R = Kf * a - Kb * b;
       if (r.nTb > 0) {
@@ -791,7 +800,7 @@ struct AirDev {
       double a = 1.0;
 #pragma unroll
       for (int i = 0; i < 2; i++)
-        if (i < r.nEd) a *= (r.nuE[i] == 1.0) ? C[r.ed[i]] : ((r.nuE[i] == 2.0) ? C[r.ed[i]] * C[r.ed[i]] : pow(C[r.ed[i]], r.nuE[i]));
+        if (i < r.nEd) a *= (r.nuEk[i] == 1) ? C[r.ed[i]] : ((r.nuEk[i] == 2) ? C[r.ed[i]] * C[r.ed[i]] : pow(C[r.ed[i]], r.nuE[i]));
       double Kb = 0.0, b = 1.0;
       if (r.backward) {
         double sumNuG = 0.0;
@@ -806,7 +815,7 @@ struct AirDev {
         Kb = r.A * exp_table(arg - lnKc);
 #pragma unroll
         for (int i = 0; i < 2; i++)
-          if (i < r.nPd) b *= (r.nuP[i] == 1.0) ? C[r.pd[i]] : ((r.nuP[i] == 2.0) ? C[r.pd[i]] * C[r.pd[i]] : pow(C[r.pd[i]], r.nuP[i]));
+          if (i < r.nPd) b *= (r.nuPk[i] == 1) ? C[r.pd[i]] : ((r.nuPk[i] == 2) ? C[r.pd[i]] * C[r.pd[i]] : pow(C[r.pd[i]], r.nuP[i]));
       }
       double c = 1.0;
       if (r.nTb > 0) {

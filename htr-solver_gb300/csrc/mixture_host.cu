@@ -220,6 +220,8 @@ bool derive(const htr_airmix_t &s, AirDev &d) {
     d.rOvW[i] = kRGAS / sp.W;
     d.TS1[i] = sp.cpCoeff.TSwitch1;
     d.TS2[i] = sp.cpCoeff.TSwitch2;
+    std::memcpy(&d.TS1b[i], &d.TS1[i], sizeof(double));
+    std::memcpy(&d.TS2b[i], &d.TS2[i], sizeof(double));
     const double *poly[3] = {sp.cpCoeff.cpH, sp.cpCoeff.cpM, sp.cpCoeff.cpL};
     for (int r = 0; r < 3; r++) {
       const double *c = poly[r];
@@ -298,6 +300,11 @@ bool derive(const htr_airmix_t &s, AirDev &d) {
       r.tb[i] = (i < nt) ? tb[i].ind : 0;
       r.effm1[i] = (i < nt) ? double(tb[i].eff) - 1.0 : 0.0;
     }
+    for (int i = 0; i < 2; i++) {
+      const double nuE = r.nuE[i], nuP = r.nuP[i];
+      r.nuEk[i] = nuE == 1.0 ? 1 : (nuE == 2.0 ? 2 : 0);
+      r.nuPk[i] = nuP == 1.0 ? 1 : (nuP == 2.0 ? 2 : 0);
+    }
     r.sumNu = 0.0;
     for (int i = 0; i < ne; i++) r.sumNu -= double(ed[i].nu);
     for (int i = 0; i < np; i++) r.sumNu += double(pd[i].nu);
@@ -351,6 +358,9 @@ bool derive(const htr_airmix_t &s, AirDev &d) {
   d.ximuRef = df_from(d.imuRef);
   d.xilamRef = df_from(d.ilamRef);
   d.xiDiRef = df_from(d.iDiRef);
+  // range() compares temperatures with the switches as bit patterns
+  for (int i = 0; i < 5; i++)
+    if (!(d.TS1[i] > 0.0) || !(d.TS2[i] > 0.0)) return false;
   return s.TRef > 0 && s.PRef > 0;
 }
 

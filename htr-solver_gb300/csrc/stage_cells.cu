@@ -624,11 +624,13 @@ __global__ void __launch_bounds__(128) stage_update(const UpdateArgs A, const __
     const double *old = A.Cold.at(p);
     double u_[NE];
     const double dtu = A.dt_cell ? ld(&A.dt_cell[i]) * A.dt_h : A.dt;
+    // c1 old + c2 cons + c3 dt ct, contracted (rounding-level against the
+    // reference's product-then-sum order)
+    const double c3dt = A.c3 * dtu;
 #pragma unroll
     for (int k = 0; k < NE; k++) {
       ctp[k] = ct[k];
-      u_[k] = __dadd_rn(__dadd_rn(__dmul_rn(A.c1, ld(&old[k])), __dmul_rn(A.c2, cons[k])),
-                        __dmul_rn(__dmul_rn(A.c3, ct[k]), dtu));
+      u_[k] = fma(A.c1, ld(&old[k]), fma(A.c2, cons[k], c3dt * ct[k]));
       cons[k] = u_[k];
     }
     if constexpr (BC) {
