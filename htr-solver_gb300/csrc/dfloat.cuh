@@ -173,6 +173,23 @@ DF_HD dfloat df_from_bits(double x) {
   if (sign) lo = -lo;
   return fast_two_sum(hi, lo);
 }
+// double -> float rounded to nearest, ties to even, on the integer pipe:
+// the same value as the conversion instruction for |x| in float's normal
+// range (including the carry into the exponent and overflow to infinity);
+// |x| below 2^-126 gives a zero of x's sign (the instruction would give a
+// subnormal: an absolute difference below 2^-126).  x must not be NaN.
+DF_HD float df_round_float(double x) {
+  const unsigned long long b = df_bits(x);
+  const unsigned sign = (unsigned)(b >> 32) & 0x80000000u;
+  const int e = (int)((b >> 52) & 0x7ff) - 1023;
+  if (e < -126) return df_float(sign);
+  if (e > 127) return df_float(sign | 0x7f800000u);
+  const unsigned long long m = b & 0xfffffffffffffULL;
+  unsigned t = ((unsigned)(e + 127) << 23) | (unsigned)(m >> 29);
+  const unsigned rem = (unsigned)(m & 0x1fffffffu);
+  t += (rem > 0x10000000u || (rem == 0x10000000u && (t & 1u))) ? 1u : 0u;
+  return df_float(sign | t);
+}
 // float -> double by its bit pattern (normal floats; zero and subnormal
 // floats give 0, infinities and NaN go through the conversion instruction)
 DF_HD double df_widen(float f) {

@@ -12,6 +12,7 @@
 #pragma once
 
 #include "common.cuh"
+#include "dfloat.cuh"
 
 namespace htr {
 
@@ -269,12 +270,14 @@ HTR_D FastX fast_x(const Smooth &s, double eps) {
   FastX f;
   const double big = 1e30;
   f.ok = (s.tau6 < big) && (s.s1 < big) && (s.s2 < big) && (s.s3 < big) && (s.s4 < big);
-  const float t = __double2float_rn(s.tau6);
+  // round-to-nearest conversions on the integer pipe; values below 2^-126
+  // become zero, negligible against eps >= 1e-16
+  const float t = df_round_float(s.tau6);
   const float e = __double2float_rn(eps);
-  f.x[0] = __fadd_rn(1.0f, __fdiv_rn(t, __fadd_rn(__double2float_rn(s.s1), e)));
-  f.x[1] = __fadd_rn(1.0f, __fdiv_rn(t, __fadd_rn(__double2float_rn(s.s2), e)));
-  f.x[2] = __fadd_rn(1.0f, __fdiv_rn(t, __fadd_rn(__double2float_rn(s.s3), e)));
-  f.x[3] = __fadd_rn(1.0f, __fdiv_rn(t, __fadd_rn(__double2float_rn(s.s4), e)));
+  f.x[0] = __fadd_rn(1.0f, __fdiv_rn(t, __fadd_rn(df_round_float(s.s1), e)));
+  f.x[1] = __fadd_rn(1.0f, __fdiv_rn(t, __fadd_rn(df_round_float(s.s2), e)));
+  f.x[2] = __fadd_rn(1.0f, __fdiv_rn(t, __fadd_rn(df_round_float(s.s3), e)));
+  f.x[3] = __fadd_rn(1.0f, __fdiv_rn(t, __fadd_rn(df_round_float(s.s4), e)));
   return f;
 }
 HTR_D float pow6f(float r) {
@@ -393,11 +396,11 @@ HTR_D double teno(double ym2, double ym1, double y, double yp1, double yp2, doub
     if (KIND == kTENOA) {
       fcut = double(kP10[4]);
     } else if (KIND == kTENOLAD) {
-      const float e = __double2float_rn(eps), tt = __double2float_rn(s.tau6);
-      float cm = __fdiv_rn(tt, __fadd_rn(__double2float_rn(s.s1), e));
-      cm = fmaxf(cm, __fdiv_rn(tt, __fadd_rn(__double2float_rn(s.s2), e)));
-      cm = fmaxf(cm, __fdiv_rn(tt, __fadd_rn(__double2float_rn(s.s3), e)));
-      cm = fmaxf(cm, __fdiv_rn(tt, __fadd_rn(__double2float_rn(s.s4), e)));
+      const float e = __double2float_rn(eps), tt = df_round_float(s.tau6);
+      float cm = __fdiv_rn(tt, __fadd_rn(df_round_float(s.s1), e));
+      cm = fmaxf(cm, __fdiv_rn(tt, __fadd_rn(df_round_float(s.s2), e)));
+      cm = fmaxf(cm, __fdiv_rn(tt, __fadd_rn(df_round_float(s.s3), e)));
+      cm = fmaxf(cm, __fdiv_rn(tt, __fadd_rn(df_round_float(s.s4), e)));
       const float arg = 3.0f + 9.5f / (1.0f + cm * 0.1f);
       const float fl = floorf(arg);
       // the exact argument 3 + 9.5 theta is never below 3 (theta > 0), so a
@@ -563,10 +566,13 @@ HTR_D double sensor_cut(double Phi) {
 HTR_D int sensor_prefilter(double ym2, double ym1, double y0, double yp1, double yp2, double yp3,
                            double cut) {
   const float u = 5.9604645e-08f;
-  const float v0 = __double2float_rn(ym2), v1 = __double2float_rn(ym1), v2 = __double2float_rn(y0),
-              v3 = __double2float_rn(yp1), v4 = __double2float_rn(yp2), v5 = __double2float_rn(yp3);
+  // round-to-nearest conversions on the integer pipe (the conversion
+  // instruction runs at the FP64 rate on this part); values below 2^-126
+  // become zero, within the u M conversion bound as long as M >= 2^-100
+  const float v0 = df_round_float(ym2), v1 = df_round_float(ym1), v2 = df_round_float(y0),
+              v3 = df_round_float(yp1), v4 = df_round_float(yp2), v5 = df_round_float(yp3);
   float M = fmaxf(fmaxf(fmaxf(fabsf(v0), fabsf(v1)), fmaxf(fabsf(v2), fabsf(v3))), fmaxf(fabsf(v4), fabsf(v5)));
-  if (!(M < 1e6f)) return -1;
+  if (!(M < 1e6f) || !(M >= 7.88860905e-31f)) return -1;  // 2^-100
   const SmoothF sm = smooth_f32(v0, v1, v2, v3, v4, v5, u * M);
   const float tau = sm.tau, et = sm.et;
   const float s1 = sm.s[0], s2 = sm.s[1], s3 = sm.s[2], s4 = sm.s[3];
@@ -614,7 +620,7 @@ HTR_D int sensor_prefilter(double ym2, double ym1, double y0, double yp1, double
 // than 1e-3 from an integer, otherwise the exact double-precision path runs.
 HTR_D double sensor_cut_fast(double Phi) {
   if (Phi >= 0.0 && Phi <= 1.0) {
-    const float P = __double2float_rn(Phi);
+    const float P = df_round_float(Phi);
     const float w = __fsub_rn(1.0f, P);
     const float w2 = __fmul_rn(w, w), w3 = __fmul_rn(w2, w), w6 = __fmul_rn(w3, w3), w12 = __fmul_rn(w6, w6);
     const float d = __fmul_rn(w12, __fadd_rn(1.0f, __fmul_rn(12.0f, P)));

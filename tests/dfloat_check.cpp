@@ -27,7 +27,7 @@ int main() {
   const double u2 = std::ldexp(1.0, -48);
   double e_add = 0, e_addpos = 0, e_mul = 0, e_mulf = 0, e_div = 0, e_rcp = 0, e_sqrt = 0, e_conv = 0;
   double e_bits = 0, e_bits_small = 0, e_same = 0;
-  long bits_back_mismatch = 0;
+  long bits_back_mismatch = 0, round_mismatch = 0;
   for (int k = 0; k < 2000000; k++) {
     const dfloat a = rnd(-20, 20, true), b = rnd(-20, 20, true);
     const dfloat p = rnd(-20, 20, false), q = rnd(-20, 20, false);
@@ -56,10 +56,17 @@ int main() {
     const dfloat fy = htr::df_from_bits(y);
     e_bits = std::fmax(e_bits, std::fabs(htr::df_to_double(fy) - y) / std::fabs(y) / u2);
     if (htr::df_to_double_bits(fy) != htr::df_to_double(fy)) bits_back_mismatch++;
+    // round-to-nearest conversion on the integer pipe: the conversion's value
+    // in float's normal range, ties (x built on a half-ulp) included
+    const double w = (uniform() < 0.5 ? -1 : 1) * std::exp2(-125 + 252 * uniform()) * (1.0 + uniform());
+    if (htr::df_round_float(w) != (float)w) round_mismatch++;
+    const float f = (float)std::exp2(-120 + 240 * uniform()) * (1.0f + (float)uniform());
+    const double tie = (double)f + 0.5 * ((double)std::nextafter(f, 2.0f * f) - (double)f);
+    if (htr::df_round_float(tie) != (float)tie || htr::df_round_float(-tie) != (float)-tie) round_mismatch++;
     const double z = std::exp2(-126 + 52 * uniform()) * (1.0 + uniform());
     e_bits_small = std::fmax(e_bits_small, std::fabs(htr::df_to_double(htr::df_from_bits(z)) - z) / z);
   }
-  std::printf("same %.3f ", e_same);
+  std::printf("same %.3f round_mismatch %ld ", e_same, round_mismatch);
   std::printf("add %.3f addpos %.3f mul %.3f mulf %.3f div %.3f rcp %.3f sqrt %.3f conv %.3f bits %.3f "
               "bits_small %.3e bits_back_mismatch %ld zero %d\n", e_add, e_addpos, e_mul, e_mulf, e_div, e_rcp, e_sqrt,
               e_conv, e_bits, e_bits_small, bits_back_mismatch,

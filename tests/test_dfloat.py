@@ -8,7 +8,9 @@ algorithm on operands of one sign too),
 multiplication 4 (DWTimesDW3), by a float 2 (DWTimesFP3); division,
 reciprocal and square root (one Newton correction) 10.  The integer-pipe
 conversion from double keeps 2^-48 (2^-23 below 2^-74, 0 below 2^-126), and
-the conversion back equals the conversion instructions' result."""
+the conversion back equals the conversion instructions' result; the
+round-to-nearest conversion to float equals the conversion instruction's
+(ties included) over float's normal range."""
 import os
 import shutil
 import subprocess
@@ -34,4 +36,5 @@ def test_dfloat_error_bounds(tmp_path):
     for k, b in bounds.items():
         assert err[k] <= b, (k, err[k], b)
     assert err["bits_back_mismatch"] == 0
+    assert err["round_mismatch"] == 0
     assert err["zero"] == 1
