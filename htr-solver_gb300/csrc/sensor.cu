@@ -62,38 +62,48 @@ __global__ void ducros_kernel(const SensorArgs a, double eps, long long n) {
   }
 }
 
+// The TENO-A shock sensor of one direction E at cell p: true when every
+// species' partial density is smooth there.  The species loop is not
+// unrolled and each direction is its own instantiation: one copy of the
+// sensor test per direction keeps the kernel inside the instruction cache
+// (unrolled over 5 species and 3 directions, instruction-cache misses
+// stalled it more than anything else).
+template <int NS, int E>
+HTR_D bool shock_dir(const SensorArgs &a, const long long *p) {
+  const Fd<int> &nt = E == 0 ? a.nx : (E == 1 ? a.ny : a.nz);
+  const int t = ld(nt.at(p));
+  long long q[6][3];
+  shift(a, q[0], p, E, kNode[t].off[0], false);
+  shift(a, q[1], p, E, kNode[t].off[1], false);
+  q[2][0] = p[0];
+  q[2][1] = p[1];
+  q[2][2] = p[2];
+  shift(a, q[3], p, E, kNode[t].off[2], true);
+  shift(a, q[4], p, E, kNode[t].off[3], true);
+  shift(a, q[5], p, E, kNode[t].off[4], true);
+  double Phi = ld(a.duc.at(q[0]));
+#pragma unroll
+  for (int k = 1; k < 6; k++) Phi = smax(Phi, ld(a.duc.at(q[k])));
+  const double cut = sensor_cut_fast(Phi);
+  const double *c[6];
+#pragma unroll
+  for (int k = 0; k < 6; k++) c[k] = a.C.at(q[k]);
+  bool s = true;
+#pragma unroll 1
+  for (int h = 0; h < NS && s; h++)
+    s = teno_a_sensor(ld(&c[0][h]), ld(&c[1][h]), ld(&c[2][h]), ld(&c[3][h]), ld(&c[4][h]), ld(&c[5][h]), t, cut);
+  return s;
+}
+
 template <int NS>
-__global__ void shock_kernel(const SensorArgs a, int dirmask, long long n) {
+__global__ void __launch_bounds__(256, 4) shock_kernel(const SensorArgs a, int dirmask, long long n) {
   for (long long idx = blockIdx.x * (long long)blockDim.x + threadIdx.x; idx < n;
        idx += (long long)gridDim.x * blockDim.x) {
     long long p[3];
     cell_of(a, idx, p);
-#pragma unroll
-    for (int e = 0; e < 3; e++) {
-      if (!(dirmask & (1 << e))) continue;
-      const Fd<int> &nt = e == 0 ? a.nx : (e == 1 ? a.ny : a.nz);
-      const int t = ld(nt.at(p));
-      long long q[6][3];
-      shift(a, q[0], p, e, kNode[t].off[0], false);
-      shift(a, q[1], p, e, kNode[t].off[1], false);
-      q[2][0] = p[0];
-      q[2][1] = p[1];
-      q[2][2] = p[2];
-      shift(a, q[3], p, e, kNode[t].off[2], true);
-      shift(a, q[4], p, e, kNode[t].off[3], true);
-      shift(a, q[5], p, e, kNode[t].off[4], true);
-      double Phi = ld(a.duc.at(q[0]));
-#pragma unroll
-      for (int k = 1; k < 6; k++) Phi = smax(Phi, ld(a.duc.at(q[k])));
-      const double cut = sensor_cut_fast(Phi);
-      bool s = true;
-#pragma unroll
-      for (int h = 0; h < NS; h++)
-        s = s && teno_a_sensor(ld(&a.C.at(q[0])[h]), ld(&a.C.at(q[1])[h]), ld(&a.C.at(q[2])[h]),
-                               ld(&a.C.at(q[3])[h]), ld(&a.C.at(q[4])[h]), ld(&a.C.at(q[5])[h]), t, cut);
-      const Fd<bool> &out = e == 0 ? a.sx : (e == 1 ? a.sy : a.sz);
-      *out.at(p) = s;
-    }
+    if (dirmask & 1) *a.sx.at(p) = shock_dir<NS, 0>(a, p);
+    if (dirmask & 2) *a.sy.at(p) = shock_dir<NS, 1>(a, p);
+    if (dirmask & 4) *a.sz.at(p) = shock_dir<NS, 2>(a, p);
   }
 }
 
