@@ -109,7 +109,7 @@ def check_fields(got, want, names, tol=RHS_REL_TOL):
 NEWTON_TOL = 1e-8
 
 
-def check_state_after_step(got, want, names, max_flip_fraction=1e-6):
+def check_state_after_step(got, want, names, max_flip_fraction=5e-6):
     """The state after a step: the pointwise bar everywhere except in cells
     where the two temperatures differ beyond it -- cells where rounding put
     the last Newton correction of one side on the other side of the
@@ -117,7 +117,10 @@ def check_state_after_step(got, want, names, max_flip_fraction=1e-6):
     cells must be rare (at most max_flip_fraction of the cells, and at least
     4 allowed), their temperatures within 2 x 1e-8 of each other, and every
     other field there within 20 x 1e-8 / T relative (the fields that follow
-    T move in proportion).  Conserved is checked without exception."""
+    T move in proportion).  Conserved is checked without exception.  On the
+    256^3 air box 13 to 16 of the 16.8 M cells (about 1e-6) flipped across
+    builds that differ only in rounding; the count bound leaves 5 times
+    that, the temperature bound is the tolerance itself (measured: 1.00006e-8)."""
     T_got = np.asarray(got["temperature"], dtype=np.float64)
     T_want = np.asarray(want["temperature"], dtype=np.float64)
     scale = np.abs(T_want).max()
