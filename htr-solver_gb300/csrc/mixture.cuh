@@ -93,6 +93,7 @@ struct AirDev {
   static constexpr bool kReactive = true;
   // species
   double W[NS], rOvW[NS];  // rOvW = RGAS/W
+  double rOvWe[NS];        // rOvW * ieRef
   double TS1[NS], TS2[NS]; // NASA range switches (the reference's floats, promoted)
   long long TS1b[NS], TS2b[NS];  // their bit patterns (range)
   double cp[NS][3][7];   // NASA coefficients c0..c6 per range (0 high, 1 mid, 2 low)
@@ -227,6 +228,16 @@ struct AirDev {
   HTR_D double SpeciesEnthalpy(int i, double Tn) const {
     const double T = Tn * TRef;
     return Enthalpy(i, T, 1.0 / T, log(T)) * ieRef;
+  }
+  // nondimensional species enthalpies at T (dimensional) with 1/T and log T
+  // supplied (R/W and the energy scale folded into one factor)
+  HTR_D void SpeciesEnthalpiesAt(double *h, double T, double Tinv, double logT) const {
+#pragma unroll
+    for (int i = 0; i < NS; i++) {
+      const double *c = hc[i][range(i, T)];
+      h[i] = (c[0] * Tinv + c[1] * logT + c[2] + T * (c[3] + T * (c[4] + T * (c[5] + T * (c[6] + c[7] * T))))) *
+             rOvWe[i];
+    }
   }
   HTR_D void SpeciesEnthalpies(double *h, double Tn) const {
     const double T = Tn * TRef;

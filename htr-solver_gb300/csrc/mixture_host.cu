@@ -331,6 +331,7 @@ bool derive(const htr_airmix_t &s, AirDev &d) {
   d.iDiRef = s.iDiRef;
   d.iwiRef = s.iwiRef;
   d.MixWRef = 1.0 / s.iMixWRef;
+  for (int i = 0; i < 5; i++) d.rOvWe[i] = d.rOvW[i] * d.ieRef;
   // double-float copies for TransportDF
   for (int i = 0; i < 5; i++) {
     d.xkbOveps[i] = df_from(d.kbOveps[i]);

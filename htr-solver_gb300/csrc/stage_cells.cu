@@ -130,7 +130,28 @@ struct DiffFaceArgs {
   const double *prep;
   FaceGrid g;
   double *fd;
+  const double *tcache;  // the update kernel's stage cache (multi-species)
 };
+
+// log T and 1/T at a face temperature Ts (dimensional) next to cell p whose
+// stage cache holds log(Tp) and 1/Tp for its current temperature: by series
+// in r = (Ts - Tp) / Tp when |r| < 2^-7 (eight terms of log(1 + r) and
+// 1/(1 + r), remainders below 2^-59), else from the math library.
+HTR_D void face_log_inv(double Ts, double Tp, const double *tcache, long long n, long long ip, double &logT,
+                        double &Tinv) {
+  if (tcache != nullptr && __double_as_longlong(tcache[ip]) == __double_as_longlong(Tp)) {
+    const double Tinvp = tcache[2 * n + ip];
+    const double r = (Ts * Tinvp) - 1.0;
+    if (fabs(r) < 0.0078125) {
+      logT = tcache[n + ip] +
+             r * (1.0 + r * (-0.5 + r * (1.0 / 3 + r * (-0.25 + r * (0.2 + r * (-1.0 / 6 + r * (1.0 / 7 - 0.125 * r)))))));
+      Tinv = Tinvp * (1.0 + r * (-1.0 + r * (1.0 + r * (-1.0 + r * (1.0 + r * (-1.0 + r * (1.0 + r * (-1.0 + r))))))));
+      return;
+    }
+  }
+  Tinv = 1.0 / Ts;
+  logT = log(Ts);
+}
 
 template <class Mix, int D>
 __global__ void __launch_bounds__(128) diffusion_faces(const DiffFaceArgs A, const __grid_constant__ Mix mix) {
@@ -177,8 +198,10 @@ __global__ void __launch_bounds__(128) diffusion_faces(const DiffFaceArgs A, con
     double heat = interp2(t, ld(A.lam.at(p)), ld(A.lam.at(q))) * m_s * (Tp - Tq);
     double F[NE];
     if constexpr (NS > 1) {
-      double h[NS];
-      mix.SpeciesEnthalpies(h, T_s);
+      double h[NS], logTs, Tinvs;
+      const double Tsd = T_s * mix.TRef;
+      face_log_inv(Tsd, Tp, A.tcache, ncell, ip, logTs, Tinvs);
+      mix.SpeciesEnthalpiesAt(h, Tsd, Tinvs, logTs);
       double ViCorr = 0.0;
 #pragma unroll
       for (int i = 0; i < NS; i++) {
@@ -794,6 +817,7 @@ cudaError_t launch_stage(const htr_fluid_view &v, const htr_rect3 &my, const htr
     A.prep = prep;
     A.g = g;
     A.fd = w.fd[D];
+    A.tcache = w.tcache;
     const int db = stage_tuning().diffusion_block;
     const dim3 gr = grid_for(g.nf[D], db);
     if (D == 0) diffusion_faces<Mix, 0><<<gr, db, 0, s>>>(A, mix);
