@@ -314,3 +314,48 @@ def test_fused_step_rejects_bad_workspace(gpu, case):
     st = gpu.htr_rk3_step_ws(C.byref(v), inner, dev.bounds(), C.byref(p), gh,
                              C.c_void_p(buf.data_ptr()), nb, C.byref(used), None, runtime.stream_handle())
     assert st == abi.HTR_ERR_UNSUPPORTED
+
+
+@pytest.mark.parametrize("fused", [False, True], ids=["tasks", "fused"])
+def test_step_with_pure_nitrogen_cells(port, gpu, fused):
+    """Cells of nearly pure N2 (every other species at a mole fraction of
+    1e-30) beside air.  The double-float transport properties keep the FP64
+    routine for cells where fewer than two species have a mole fraction of
+    1e-20 (their diffusion partner sums underflow in float range): the
+    properties of the prepared state, pure cells included, within the
+    pointwise bar of the oracle.  Then one step through the task path and
+    the fused pipeline, every field within the bar, except the species
+    diffusivities of cells whose second most abundant species has a mole
+    fraction below 1e-6: there the dominant species' diffusivity is a mean
+    over trace mole fractions of 1e-20 and less, which no bar on the state
+    pins (a one-ulp change of the state moves the reference's own value by
+    up to 2e-10 relative).  (Exact zeros are outside the reference's domain:
+    its diffusivity of the one species present is 0/0 there.)"""
+    import torch
+    fl, h, m = util.make_air_state(port, (12, 10, 8), seed=23)
+    X = fl["MolarFracs"].copy()
+    pure = np.zeros(X.shape[:3], dtype=bool)
+    # eight of twelve cells along x: the middle ones stay nearly pure
+    # through the first stage (their stencils see only nitrogen)
+    pure[:, :, 2:10] = True
+    X[pure] = np.array([1.0, 1e-30, 1e-30, 1e-30, 1e-30])
+    fl["MolarFracs"] = X
+    workloads.derive_state(port, fl, h)
+    assert np.all(fl["MassFracs"][pure][:, 1:] < 1e-29)
+    gh = runtime.load_mixture(fl.meta["eos"], m)
+    host, dev = _run_both(port, gpu, fl, h, gh, "htr_UpdatePropertiesFromPrimitive",
+                          lambda v, f, mm, s: (v, f.bounds(), mm, s))
+    util.check_fields(dev, host, ("rho", "mu", "lam", "Di", "SoS", "MassFracs"))
+    host = fl.copy()
+    oracle.step(port, host, h, dt=1e-9, chemistry=True)
+    dv = fl.to_device("cuda")
+    status = torch.zeros(1, dtype=torch.int32, device="cuda")
+    runtime.rk3_step(dv, gh, dt=1e-9, chemistry=True, fused=fused, status_dev=C.c_void_p(status.data_ptr()))
+    torch.cuda.synchronize()
+    assert status.item() == 0
+    out = dv.to_host()
+    util.check_fields(out, host, tuple(f for f in STEP_FIELDS if f != "Di"))
+    second = np.sort(host["MolarFracs"], axis=-1)[..., -2]
+    mixed = second >= 1e-6
+    assert 0 < mixed.sum() < mixed.size
+    util.check(out["Di"][mixed], host["Di"][mixed], "Di")
