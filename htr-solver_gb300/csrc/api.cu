@@ -344,7 +344,7 @@ int htr_load_mixture(int eos, const void *mix, size_t bytes, htr_mixture_t *out)
   e = cudaGetDeviceProperties(&prop, dev);
   if (e != cudaSuccess) return fail(HTR_ERR_NO_DEVICE, "cudaGetDeviceProperties: %s", cudaGetErrorString(e));
   if (prop.major != 10 || prop.minor != 3)
-    return fail(HTR_ERR_NO_DEVICE, "this build targets sm_103 (GB300); device is %s", prop.name);
+    return fail(HTR_ERR_NO_DEVICE, "the library targets sm_103 (GB300); device is %s", prop.name);
   // set-up of htr_rk3_step_static on this device (loads its module)
   if (int st = static_scratch(nullptr, true)) return st;
   htr_mixture_s *m = new (std::nothrow) htr_mixture_s();

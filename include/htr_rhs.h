@@ -48,7 +48,7 @@ typedef enum {
   HTR_ERR_LAYOUT = 2,        /* stride not a multiple of the element size, misaligned base */
   HTR_ERR_CUDA = 3,          /* a CUDA call failed (message in htr_last_error) */
   HTR_ERR_ITERATION_CAP = 4, /* a device Newton / Rosenbrock loop hit its cap */
-  HTR_ERR_UNSUPPORTED = 5,   /* configuration outside this build (e.g. other mixtures) */
+  HTR_ERR_UNSUPPORTED = 5,   /* configuration the library does not support (e.g. other mixtures) */
   HTR_ERR_NO_DEVICE = 6,     /* no usable sm_103 device */
   HTR_ERR_IO = 7,            /* a file could not be opened, read or written */
   HTR_ERR_FORMAT = 8         /* a file is not HDF5, is truncated, or lacks what a restart holds */
