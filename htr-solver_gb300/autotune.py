@@ -18,7 +18,7 @@ from . import abi, runtime
 
 CANDIDATES = {
     "kg_x_tile": (64, 128, 256),
-    "teno_blocks_per_sm": (4, 8, 16),
+    "teno_blocks_per_sm": (0, 4, 8, 16),
     "update_block": (64, 128),
     "diffusion_block": (64, 128),
     "prepass_block": (128, 256),

@@ -712,7 +712,7 @@ int htr_rk3_set_tuning(const htr_stage_tuning *t) {
   if (t == nullptr) return fail(HTR_ERR_ARGUMENT, "null tuning%s");
   auto pow2_in = [](int v, int lo, int hi) { return v >= lo && v <= hi && (v & (v - 1)) == 0; };
   if (!pow2_in(t->prepass_block, 64, 256) || !pow2_in(t->diffusion_block, 32, 128) ||
-      !pow2_in(t->update_block, 32, 128) || t->teno_blocks_per_sm < 1 || t->teno_blocks_per_sm > 32 ||
+      !pow2_in(t->update_block, 32, 128) || t->teno_blocks_per_sm < 0 || t->teno_blocks_per_sm > 32 ||
       !(t->kg_x_tile == 64 || t->kg_x_tile == 128 || t->kg_x_tile == 256))
     return fail(HTR_ERR_ARGUMENT, "tuning value outside the supported set%s");
   htr::StageTuning &g = htr::stage_tuning();

@@ -111,7 +111,8 @@ struct StageTuning {
   int prepass_block = 256;      // threads per block, per-cell prepass (64..256)
   int diffusion_block = 128;    // threads per block, diffusion faces (32..128)
   int update_block = 128;       // threads per block, per-cell update (32..128)
-  int teno_blocks_per_sm = 8;   // grid of the TENO kernel
+  int teno_blocks_per_sm = 0;   // grid of the TENO queue kernel: 0 one queued face per thread,
+                                // 1..32 that many blocks per SM striding over the queue
   int kg_x_tile = 128;          // faces per x tile of the KG kernel (64, 128, 256)
 };
 StageTuning &stage_tuning();

@@ -2,9 +2,9 @@
 // -fmad=false) and the Euler orchestration of one stage.
 //
 // euler_teno_faces: the faces the hybrid sensor rejected (queued by the
-// Kennedy-Gruber kernel, stage_kg.cu), spread over every SM with a
-// grid-stride loop, so the expensive reconstruction is load-balanced
-// independently of where the shocks are.  euler_teno_faces_dir: every face of
+// Kennedy-Gruber kernel, stage_kg.cu), one queued face per thread over the
+// whole GPU, so the expensive reconstruction is load-balanced independently
+// of where the shocks are.  euler_teno_faces_dir: every face of
 // one direction for the TENO schemes, one face per thread.  The arithmetic
 // per face is the one of the per-direction task kernels (euler_face.cuh), so
 // selection flags and face fluxes are bit-identical to theirs.
@@ -173,7 +173,11 @@ cudaError_t launch_stage_euler(const htr_fluid_view &v, const htr_rect3 &my, con
     for (int k = 0; k < 3; k++) {
       const int D = order[k];
       if (!(p.active & (1u << D))) continue;
-      const long long blocks = (g.nf[D] + 127) / 128, cap = (long long)sms * 64;
+      // one face per thread: a grid capped at 64 blocks per SM (each thread
+      // then striding over ~10 faces) made the 512 x 192 x 128 boundary-layer
+      // step 26 % slower (1642 ms against 1305 ms); the stride loop only
+      // remains for grids beyond the launch limit
+      const long long blocks = (g.nf[D] + 127) / 128, cap = 0x7fffffffLL;
       const dim3 gd((unsigned)(blocks < cap ? blocks : cap));
       if (p.kind == kTENO) launch_teno_dir<Mix, kTENO>(T, mix, D, gd, s);
       else if (p.kind == kTENOA) launch_teno_dir<Mix, kTENOA>(T, mix, D, gd, s);
@@ -183,11 +187,18 @@ cudaError_t launch_stage_euler(const htr_fluid_view &v, const htr_rect3 &my, con
     return mark(3);
   }
   // the hybrid scheme's sensor-rejected faces (plain TENO, rhs.inl:622-759),
-  // one launch per direction over that direction's queue
-  dim3 grid((unsigned)(sms * stage_tuning().teno_blocks_per_sm));
+  // one launch per direction over that direction's queue.  By default the
+  // grid covers every face of the direction, one queued face per thread (the
+  // blocks past the queue's length exit at once): on the 512 x 192 x 128
+  // boundary layer a grid of 8 blocks per SM striding over the queue made the
+  // hybrid step 8 % slower (1167 ms against 1083 ms), and the 256^3 air box
+  // (a short queue) runs the same either way
+  const int tb = stage_tuning().teno_blocks_per_sm;
   for (int k = 0; k < 3; k++) {
     const int D = order[k];
     if (!(p.active & (1u << D))) continue;
+    const long long blocks = tb > 0 ? (long long)sms * tb : (g.nf[D] + 127) / 128;
+    const dim3 grid((unsigned)(blocks < 1 ? 1 : (blocks > 0x7fffffffLL ? 0x7fffffffLL : blocks)));
     if (D == 0) euler_teno_faces<Mix, 0, kTENO><<<grid, 128, 0, s>>>(T, mix);
     else if (D == 1) euler_teno_faces<Mix, 1, kTENO><<<grid, 128, 0, s>>>(T, mix);
     else euler_teno_faces<Mix, 2, kTENO><<<grid, 128, 0, s>>>(T, mix);

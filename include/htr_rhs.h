@@ -431,8 +431,10 @@ size_t htr_rk3_static_scratch_bytes(void);
 /* Launch shapes of the fused stage, no counterpart in the reference
  * (process-wide; chosen by the autotuner of the batched form).  Allowed:
  * prepass_block 64/128/256, diffusion_block and update_block 32/64/128,
- * teno_blocks_per_sm 1..32, kg_x_tile 64/128/256.  Defaults 256, 128, 128,
- * 8, 128.  Set it before launching (or capturing) the steps that use it. */
+ * teno_blocks_per_sm 0..32 (0: the TENO queue kernel runs one queued face per
+ * thread, its grid sized to the direction's face count; 1..32: that many
+ * blocks per SM stride over the queue), kg_x_tile 64/128/256.  Defaults 256,
+ * 128, 128, 0, 128.  Set it before launching (or capturing) the steps that use it. */
 typedef struct {
   int prepass_block, diffusion_block, update_block, teno_blocks_per_sm, kg_x_tile;
 } htr_stage_tuning;

@@ -22,12 +22,12 @@ def test_tuning_validation_and_roundtrip():
     at = _lib_or_skip()
     default = at.get_tuning()
     assert default.as_dict() == dict(prepass_block=256, diffusion_block=128, update_block=128,
-                                     teno_blocks_per_sm=8, kg_x_tile=128)
+                                     teno_blocks_per_sm=0, kg_x_tile=128)
     t = at.htr_stage_tuning(128, 64, 64, 16, 256)
     at.set_tuning(t)
     assert at.get_tuning().as_dict() == t.as_dict()
     for bad in (at.htr_stage_tuning(100, 64, 64, 16, 256), at.htr_stage_tuning(128, 256, 64, 16, 256),
-                at.htr_stage_tuning(128, 64, 64, 0, 256), at.htr_stage_tuning(128, 64, 64, 8, 96)):
+                at.htr_stage_tuning(128, 64, 64, -1, 256), at.htr_stage_tuning(128, 64, 64, 33, 256), at.htr_stage_tuning(128, 64, 64, 8, 96)):
         with pytest.raises(abi.HtrError):
             at.set_tuning(bad)
     at.set_tuning(default)
