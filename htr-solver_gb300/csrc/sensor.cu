@@ -132,9 +132,11 @@ static SensorArgs sensor_args(const htr_fluid_view &v, const htr_rect3 &my, cons
   return a;
 }
 
+// One cell per thread (the grid-stride loops only matter past the launch
+// limit; a grid capped at 152 x 64 blocks was slower on a 256^3 box).
 static dim3 grid_for(long long n, int threads) {
   long long b = (n + threads - 1) / threads;
-  if (b > 152LL * 64) b = 152LL * 64;
+  if (b > 0x7fffffffLL) b = 0x7fffffffLL;
   return dim3((unsigned)(b > 0 ? b : 1));
 }
 

