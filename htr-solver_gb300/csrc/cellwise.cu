@@ -35,9 +35,11 @@ static CellRange cells(const htr_rect3 &r) {
   return c;
 }
 
+// One cell per thread (the grid-stride loops only matter past the launch
+// limit).
 static dim3 grid_for(long long n, int threads) {
   long long b = (n + threads - 1) / threads;
-  if (b > 152LL * 32) b = 152LL * 32;
+  if (b > 0x7fffffffLL) b = 0x7fffffffLL;
   return dim3((unsigned)(b > 0 ? b : 1));
 }
 

@@ -33,9 +33,12 @@ static CellRange cells(const htr_rect3 &r) {
   return c;
 }
 
+// One cell per thread (the grid-stride loops only matter past the launch
+// limit): a grid capped at 152 x 32 blocks made the implicit step of a 96^3
+// air box 10 % slower (257 / 240 ms against 233 / 216 ms on two states).
 static dim3 grid_for(long long n, int threads) {
   long long b = (n + threads - 1) / threads;
-  if (b > 152LL * 32) b = 152LL * 32;
+  if (b > 0x7fffffffLL) b = 0x7fffffffLL;
   return dim3((unsigned)(b > 0 ? b : 1));
 }
 
