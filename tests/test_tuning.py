@@ -54,3 +54,46 @@ def test_tuned_step_is_bit_identical(kind):
     for o in outs[1:]:
         for name in o.arrays:
             assert np.array_equal(o[name], outs[0][name], equal_nan=True), name
+
+
+def test_autotune_descent_keeps_only_real_gains(monkeypatch):
+    """Coordinate descent of autotune() with the stage timer replaced by a
+    cost model (no GPU): each parameter is tried from the best setting so
+    far, a candidate is kept only when it beats the best by more than
+    `gain`, and the winner is installed at the end."""
+    from htr_gb300 import autotune as at
+    state = {"t": at.htr_stage_tuning(256, 128, 128, 0, 128)}
+    installed = []
+
+    def get_tuning():
+        return at.htr_stage_tuning(**state["t"].as_dict())
+
+    def set_tuning(t):
+        state["t"] = at.htr_stage_tuning(**t.as_dict())
+        installed.append(t.as_dict())
+
+    teno = {0: 10.0, 4: 12.0, 8: 11.0, 16: 9.5}
+    tile = {64: 1.0, 128: 0.0, 256: -0.5}
+    upd = {64: -0.05, 128: 0.0}  # 0.5 % faster: below the 1 % gain
+
+    def stage_ms(grids, reps=3, workspace=None, originals=None):
+        t = state["t"]
+        return teno[t.teno_blocks_per_sm] + tile[t.kg_x_tile] + upd[t.update_block]
+
+    class Fluid:
+        def copy(self):
+            return Fluid()
+
+    monkeypatch.setattr(at, "get_tuning", get_tuning)
+    monkeypatch.setattr(at, "set_tuning", set_tuning)
+    monkeypatch.setattr(at, "stage_ms", stage_ms)
+    best, t_best, t0, trials = at.autotune([(Fluid(), None, 1e-9, True)], reps=1)
+    assert t0 == 10.0
+    assert best == dict(prepass_block=256, diffusion_block=128, update_block=128, teno_blocks_per_sm=16,
+                        kg_x_tile=256)
+    assert t_best == 9.0
+    assert installed[-1] == best and state["t"].as_dict() == best
+    # every candidate of every parameter tried once, except the current value
+    n_trials = sum(len(v) - 1 for v in at.CANDIDATES.values())
+    assert len(trials) == 1 + n_trials
+    assert 0 in at.CANDIDATES["teno_blocks_per_sm"]
